@@ -1,0 +1,729 @@
+"""CPU oracle for the damped Gauss-Newton CPD path of Tensor Fox v1.2.1.
+
+TEST INFRASTRUCTURE ONLY.  This module restates, in vectorised NumPy, the
+algorithm of the reference's dGN path so that the CUDA implementation can be
+checked against it.  Only ``tests/``, ``__graft_entry__.smoke()`` and the CPU
+legs of ``bench.py`` may import it; the product package never does.
+
+Parity pin: every function below is compared against golden vectors produced by
+running the reference itself (``tests/golden/make_golden.py``), see
+``tests/test_oracle_golden.py``.
+
+Conventions shared with the reference
+-------------------------------------
+* factors ``W[l]`` are ``(d_l, R)`` float arrays; the flat point ``x`` is
+  ``concat_l vec_F(W[l])`` (GaussNewton.py:125, Conversion.py:21-44);
+* the mode-``m`` unfolding uses Kolda's column order (Critical.py:124-146):
+  ``unfold(T, m) == moveaxis(T, m-1, 0).reshape(d_m, -1, order='F')``;
+* NumPy's global RNG is used exactly where the reference uses it, so a seeded
+  run draws the same numbers in the same order.
+"""
+from copy import deepcopy
+
+import numpy as np
+from numpy.linalg import norm
+from scipy.linalg import qr as sp_qr, svd as sp_svd
+
+# ----------------------------------------------------------------------------
+# options (Auxiliar.py:242-362)
+# ----------------------------------------------------------------------------
+_DEFAULTS = dict(maxiter=200, tol=1e-16, tol_step=1e-6, tol_improv=1e-6, tol_grad=1e-6,
+                 tol_jump=10, method='dGN', inner_method='cg', cg_maxiter=100, cg_factor=1,
+                 cg_tol=1e-16, initialization='random', trunc_dims=0,
+                 mlsvd_method='seq', tol_mlsvd=1e-16, init_damp=1, refine=False, symm=False,
+                 factors_norm=0, trials=3, display=0, epochs=1, gpu=False, mkl_dot=True,
+                 svd_n_components=None)
+
+
+class Options:
+    pass
+
+
+def make_options(options=None):
+    """Defaults overridden by any attribute the caller's object defines (Auxiliar.py:256-353)."""
+    out = Options()
+    for k, v in _DEFAULTS.items():
+        setattr(out, k, v)
+    out.bi_method_parameters = ['als', 500, 1e-6]
+    if options is None or options is False:
+        return out
+    names = dir(options)
+    for k in _DEFAULTS:
+        if k in names:
+            setattr(out, k, getattr(options, k))
+    if out.gpu and 'mlsvd_method' not in names:          # Auxiliar.py:359-360
+        out.mlsvd_method = 'gpu'
+    return out
+
+
+# ----------------------------------------------------------------------------
+# layout helpers (Conversion.py, Critical.py)
+# ----------------------------------------------------------------------------
+def unfold(T, mode):
+    """Mode-``mode`` (1-based) unfolding, Kolda order (Conversion.py:207-252)."""
+    d = T.shape[mode - 1]
+    return np.ascontiguousarray(np.moveaxis(T, mode - 1, 0).reshape(d, -1, order='F'), dtype=np.float64)
+
+
+def foldback(Tl, mode, dims):
+    """Inverse of :func:`unfold` (Conversion.py:305-315)."""
+    dims = tuple(int(v) for v in dims)
+    m = mode - 1
+    moved = (dims[m],) + tuple(d for i, d in enumerate(dims) if i != m)
+    return np.moveaxis(np.asarray(Tl).reshape(moved, order='F'), 0, m).copy()
+
+
+def khatri_rao(A, B):
+    """Row-block Khatri-Rao product: row ``i*b1+k`` is ``A[i]*B[k]`` (MultilinearAlgebra.py:248-274)."""
+    return (A[:, None, :] * B[None, :, :]).reshape(A.shape[0] * B.shape[0], A.shape[1])
+
+
+def kr_chain(mats):
+    """``mats[0] ⊙ mats[1] ⊙ ...`` with the first matrix varying slowest."""
+    M = mats[0]
+    for X in mats[1:]:
+        M = khatri_rao(M, X)
+    return M
+
+
+def x2cpd(x, factors, eq=True):
+    """Writes the flat point into the factor matrices, then balances them (Conversion.py:21-49)."""
+    R = factors[0].shape[1]
+    s = 0
+    for l in range(len(factors)):
+        d = factors[l].shape[0]
+        factors[l][:, :] = x[s:s + d * R].reshape(R, d).T
+        s += d * R
+    if eq:
+        factors = equalize(factors, R)
+    return factors
+
+
+def cpd2flat(factors):
+    return np.concatenate([W.flatten('F') for W in factors])
+
+
+def equalize(factors, R):
+    """Rescales column r of every mode to the geometric mean of their norms (Conversion.py:361-387)."""
+    L = len(factors)
+    for r in range(R):
+        nr = np.array([norm(factors[l][:, r]) for l in range(L)])
+        p = np.prod(nr)
+        if p != 0.0:
+            g = p ** (1 / L)
+            for l in range(L):
+                factors[l][:, r] = (g / nr[l]) * factors[l][:, r]
+    return factors
+
+
+def transform(factors, symm, factors_norm):
+    """Symmetrisation / fixed-norm rescaling (Conversion.py:412-444); both default off."""
+    L = len(factors)
+    if symm:
+        s = factors[0]
+        for l in range(1, L):
+            s = s + factors[l]
+        factors[0] = s / L
+        for l in range(1, L):
+            factors[l] = factors[0]
+    if factors_norm > 0:
+        for l in range(L):
+            factors[l] = factors_norm * (1 / norm(factors[l])) * factors[l]
+    return factors
+
+
+def cpd2unfold1(factors):
+    """``W0 · (W_{L-1} ⊙ ... ⊙ W_1)^T`` (Conversion.py:117-141)."""
+    L = len(factors)
+    M = factors[1]
+    for l in range(2, L):
+        M = khatri_rao(factors[l], M)
+    return factors[0] @ M.T
+
+
+def cpd2tens(factors):
+    """Dense tensor of a CPD (Conversion.py:52-79)."""
+    dims = [W.shape[0] for W in factors]
+    return foldback(cpd2unfold1(factors), 1, dims)
+
+
+def fastnorm(A, B):
+    """Frobenius norm of ``A - B`` (Critical.py:14-22)."""
+    return float(np.sqrt(np.sum((np.asarray(A) - np.asarray(B)) ** 2)))
+
+
+def sparse_fastnorm(data, idxs, dims, factors):
+    """Norm of ``data - model(idxs)`` over the stored entries only (Critical.py:25-53)."""
+    idxs = np.asarray(idxs).astype(np.int64)
+    R = factors[0].shape[1]
+    p = np.ones((len(idxs), R))
+    for l in range(len(dims)):
+        p *= factors[l][idxs[:, l], :]
+    approx = p.sum(axis=1)
+    return float(norm(np.asarray(data, dtype=np.float64) - approx))
+
+
+# ----------------------------------------------------------------------------
+# dGN building blocks (GaussNewton.py)
+# ----------------------------------------------------------------------------
+def sum_dims_of(dims, R):
+    return np.array([R * int(sum(dims[:l])) for l in range(len(dims) + 1)])
+
+
+def gramians(factors):
+    """``Gr[l] = W_l^T W_l``; ``P2[l][k] = ∘_{m∉{l,k}} Gr[m]``; ``P1[l] = ∘_{m≠l} Gr[m]``.
+
+    Follows GaussNewton.py:520-548 including the product order and the untouched
+    diagonal blocks ``P2[l][l] = 1`` (they are never read).
+    """
+    L = len(factors)
+    R = factors[0].shape[1]
+    Gr = np.array([W.T @ W for W in factors])
+    P1 = np.ones((L, R, R))
+    P2 = np.ones((L, L, R, R))
+    for l in range(1, L):
+        for ll in range(l):
+            acc = np.ones((R, R))
+            for m in range(L):
+                if m != l and m != ll:
+                    acc = acc * Gr[m]
+            P2[l, ll] = acc
+            P2[ll, l] = acc
+        if l < L - 1:
+            P1[l] = P2[l, l - 1] * Gr[l - 1]
+        else:
+            P1[l] = P2[l, 0] * Gr[0]
+    P1[0] = P2[0, 1] * Gr[1]
+    return Gr, P1, P2
+
+
+def regularization(P1, dims, R):
+    """Tikhonov diagonal (GaussNewton.py:584-607).
+
+    Reproduces the reference exactly: ``gamma[l, r] = tmp * sqrt(|P1[l][r, r]|)``
+    where ``tmp`` is max|P1| of the LAST mode (the running max ``s`` is unused).
+    """
+    L = len(dims)
+    tmp = np.max(np.abs(P1[L - 1]))
+    gamma = tmp * np.sqrt(np.abs(np.array([np.diag(P1[l]) for l in range(L)])))
+    Gamma = np.concatenate([np.repeat(gamma[l], dims[l]) for l in range(L)])
+    return Gamma, gamma
+
+
+def precond(Gamma, gamma, damp, dims):
+    """``M = 1/sqrt(gamma^2 + damp^2 Gamma^2)`` per column block (GaussNewton.py:610-627)."""
+    L = len(dims)
+    g = np.concatenate([np.repeat(gamma[l], dims[l]) for l in range(L)])
+    return 1 / np.sqrt(g ** 2 + damp ** 2 * Gamma ** 2)
+
+
+def mttkrp(Tl, factors, l):
+    """``T_(l) · (W_{L-1} ⊙ ... ⊙ W_{l+1} ⊙ W_{l-1} ⊙ ... ⊙ W_0)`` (GaussNewton.py:411-423)."""
+    L = len(factors)
+    order = [k for k in reversed(range(L)) if k != l]
+    return Tl[l] @ kr_chain([factors[k] for k in order])
+
+
+def compute_grad(Tl, factors, P1):
+    """``g_l = W_l P1_l - T_(l) KR_l`` stacked as vec_F (GaussNewton.py:401-427)."""
+    return np.concatenate([(factors[l] @ P1[l] - mttkrp(Tl, factors, l)).T.ravel()
+                           for l in range(len(factors))])
+
+
+def _split(v, dims, R):
+    sd = sum_dims_of(dims, R)
+    return [v[sd[l]:sd[l + 1]].reshape(R, dims[l]) for l in range(len(dims))]
+
+
+def matvec(factors, P1, P2, v):
+    """Jacobian-free ``J^T J v`` (GaussNewton.py:551-581 with the A/B set-up of :371-377)."""
+    L = len(factors)
+    R = factors[0].shape[1]
+    dims = [W.shape[0] for W in factors]
+    V = _split(v, dims, R)
+    A = [V[l] @ factors[l] for l in range(L)]
+    B = [V[l].T @ P1[l] for l in range(L)]
+    out = []
+    for l in range(L):
+        acc = np.zeros((R, R))
+        for ll in range(L):
+            if ll != l:
+                acc += P2[l, ll] * A[ll]
+        out.append((factors[l] @ acc + B[l]).T.ravel())
+    return np.concatenate(out)
+
+
+def cg(Tl, factors, damp, maxiter, tol):
+    """Preconditioned, regularised CG for the dGN step (GaussNewton.py:315-398).
+
+    Returns ``(M*y, grad, JT_J_grad, itn+1, residualnorm)`` like the reference.
+    """
+    L = len(factors)
+    R = factors[0].shape[1]
+    dims = [W.shape[0] for W in factors]
+    nx = R * sum(dims)
+    if nx > 100:
+        maxiter = min(maxiter, nx)
+    else:
+        tol = 0
+    Gr, P1, P2 = gramians(factors)
+    Gamma, gamma = regularization(P1, dims, R)
+    M = precond(Gamma, gamma, damp, dims)
+    y = np.zeros(nx)
+    grad = -compute_grad(Tl, factors, P1)
+    JT_J_grad = matvec(factors, P1, P2, grad)
+    r = M * grad
+    P = r
+    rn = float(r @ r)
+    if rn == 0.0:
+        rn = 1e-6
+    itn = 0
+    for itn in range(maxiter):
+        Q = M * P
+        z = matvec(factors, P1, P2, Q) + damp * Gamma * Q
+        z = M * z
+        den = float(P @ z)
+        if den == 0.0:
+            den = 1e-6
+        alpha = rn / den
+        y = y + alpha * P
+        r = r - alpha * z
+        rn_new = float(r @ r)
+        beta = rn_new / rn
+        rn = rn_new
+        if itn == 0:
+            # GaussNewton.py:349 binds P to the residual array itself, and the
+            # in-place update at :388 moves it along, so the first new direction
+            # is (1 + beta) * r instead of r + beta * r_old.
+            P = r + beta * r
+        else:
+            P = r + beta * P
+        if rn <= tol:
+            break
+    return M * y, grad, JT_J_grad, itn + 1, rn
+
+
+def cg_budget(it, L, cg_factor):
+    """CG iteration cap of the 'cg' inner method; draws from NumPy's global RNG (GaussNewton.py:267)."""
+    return 1 + (L - 2) * int(cg_factor * np.random.randint(1 + it ** 0.4, 2 + it ** 0.9))
+
+
+def update_gain_ratio(damp, old_error, error, Tsize, old_x, x, grad):
+    """Gain ratio (GaussNewton.py:472-487)."""
+    num = (Tsize ** 2) * (old_error ** 2 - error ** 2)
+    den = float(np.dot(x - old_x, grad + damp * (x - old_x)))
+    if den != 0.0:
+        return num / den
+    if num != 0.0:
+        return np.sign(num) * np.inf
+    return -np.inf
+
+
+def update_damp(damp, init_damp, gain_ratio, it):
+    """×3 below 0.25, ÷3 above 0.75, or the user's schedule (GaussNewton.py:490-503)."""
+    if type(init_damp) == list:
+        return init_damp[it]
+    if gain_ratio < 0.25:
+        return 3 * damp
+    if gain_ratio > 0.75:
+        return damp / 3
+    return damp
+
+
+def update_delta(delta, gain_ratio, step_size):
+    """Trust-region radius of the dogleg fallback (GaussNewton.py:506-517)."""
+    if gain_ratio > 0.75:
+        return max(delta, 2 * step_size)
+    sigma = 0.25 / (1 + np.exp(-14 * (gain_ratio - 0.75))) + 0.75
+    return min(sigma * delta, delta)
+
+
+def dogleg(y, grad, JT_J_grad, delta):
+    """Dogleg step between the steepest-descent and the CG step (GaussNewton.py:766-795)."""
+    alpha = norm(grad) ** 2 / np.dot(grad, JT_J_grad)
+    y_sd = alpha * grad
+    c1 = norm(y_sd)
+    c2 = np.dot(y - y_sd, y_sd)
+    c3 = norm(y - y_sd) ** 2
+    c4 = delta ** 2 - c1 ** 2
+    m = c2 ** 2 + c3 * c4
+    if norm(y) < delta:
+        return y
+    if c1 >= delta:
+        return (delta / c1) * y_sd
+    if m < 0:
+        return y
+    c5 = np.sqrt(m)
+    beta = (-c2 + c5) / c3 if c2 <= 0 else c4 / (c2 + c5)
+    return y_sd + beta * (y - y_sd)
+
+
+def compute_dogleg_steps(Tsize, T1, factors, grad, JT_J_grad, x, y, error, damp, symm, factors_norm):
+    """Up to 11 dogleg trials after a rejected step (GaussNewton.py:713-763)."""
+    count = 0
+    best_x, best_y, best_error = x.copy(), y.copy(), error
+    best_factors = deepcopy(factors)
+    gain_ratio, delta = 1, 1
+    while gain_ratio > 0:
+        old_x, old_error = x, error
+        y = dogleg(y, grad, JT_J_grad, delta)
+        x = x + y
+        factors = x2cpd(x, factors, eq=False)
+        factors = transform(factors, symm, factors_norm)
+        error = fastnorm(T1, cpd2unfold1(factors)) / Tsize
+        gain_ratio = update_gain_ratio(damp, old_error, error, Tsize, old_x, x, grad)
+        if error < old_error:
+            best_x, best_y, best_error = x.copy(), y.copy(), error
+            best_factors = deepcopy(factors)
+        delta = update_delta(delta, gain_ratio, norm(x - old_x))
+        count += 1
+        if count > 10:
+            break
+    return best_factors, best_x, best_y, best_error
+
+
+def dGN(T, factors, R, options, budgets=None, trace=None):
+    """Damped Gauss-Newton (GaussNewton.py:29-251).
+
+    ``budgets`` optionally fixes the CG cap per iteration instead of drawing it;
+    ``trace`` (a list) receives per-iteration ``dict(error, damp, itn, y_norm)``.
+    Returns ``(best_factors, step_sizes, errors, improv, gradients, stop)``.
+    """
+    o = options
+    init_damp, maxiter = o.init_damp, o.maxiter
+    tol, tol_step, tol_improv, tol_grad = o.tol, o.tol_step, o.tol_improv, o.tol_grad
+    L = len(factors)
+    factors = [np.array(W, dtype=np.float64) for W in factors]
+    dims = T.shape
+    Tsize = norm(T)
+    error = 1
+    best_error = np.inf
+    stop = 5
+    damp = init_damp[0] if type(init_damp) == list else init_damp * np.mean(np.abs(T))
+    const = 1 + int(maxiter / 10)
+    if R * sum(dims) <= 100:
+        tol = tol_step = tol_improv = tol_grad = 0
+    x = cpd2flat(factors)
+    y = np.zeros(R * sum(dims))
+    step_sizes, errors = np.zeros(maxiter), np.zeros(maxiter)
+    improv, gradients = np.zeros(maxiter), np.zeros(maxiter)
+    best_factors = deepcopy(factors)
+    Tl = [unfold(np.asarray(T, dtype=np.float64), l + 1) for l in range(L)]
+    it = 0
+    for it in range(maxiter):
+        old_x, old_error = x, error
+        inner = o.inner_method[it] if type(o.inner_method) == list else o.inner_method
+        if budgets is not None:
+            cgmax = int(budgets[it])
+        elif inner == 'cg':
+            cgmax = cg_budget(it, L, o.cg_factor)
+        elif inner == 'cg_static':
+            cgmax = o.cg_maxiter
+        else:
+            raise NotImplementedError("inner_method " + repr(inner))
+        y, grad, JT_J_grad, itn, residualnorm = cg(Tl, factors, damp, cgmax, o.cg_tol)
+        x = x + y
+        factors = x2cpd(x, factors)
+        factors = transform(factors, o.symm, o.factors_norm)
+        error = fastnorm(Tl[0], cpd2unfold1(factors)) / Tsize
+        if it > 3 and error > o.tol_jump * old_error:
+            x = x - y
+            factors, x, y, error = compute_dogleg_steps(Tsize, Tl[0], factors, grad, JT_J_grad,
+                                                        x, y, error, damp, o.symm, o.factors_norm)
+        gain_ratio = update_gain_ratio(damp, old_error, error, Tsize, old_x, x, grad)
+        if trace is not None:
+            trace.append(dict(error=error, damp=damp, itn=itn, budget=cgmax))
+        damp = update_damp(damp, init_damp, gain_ratio, it)
+        if error < best_error:
+            best_error = error
+            best_factors = deepcopy(factors)
+        errors[it] = error
+        step_sizes[it] = norm(x - old_x) / norm(old_x)
+        gradients[it] = norm(grad, np.inf)
+        improv[it] = errors[it] if it == 0 else abs(errors[it] - errors[it - 1])
+        if it > 1:
+            if errors[it] < tol:
+                stop = 0
+                break
+            if step_sizes[it] < tol_step:
+                stop = 1
+                break
+            if improv[it] < tol_improv:
+                stop = 2
+                break
+            if gradients[it] < tol_grad:
+                stop = 3
+                break
+            if it > 2 * const and it % const == 0:
+                mean1 = np.mean(errors[it - 2 * const: it - const])
+                mean2 = np.mean(errors[it - const: it])
+                if mean1 - mean2 <= tol_improv:
+                    stop = 4
+                    break
+                mean3 = np.mean(improv[it - const: it])
+                if mean3 < 1e-3 * mean2:
+                    stop = 7
+                    break
+            if error > max(1, Tsize ** 2) / (1e-16 + tol):
+                stop = 6
+                break
+    n = it + 1
+    return best_factors, step_sizes[:n], errors[:n], improv[:n], gradients[:n], stop
+
+
+# ----------------------------------------------------------------------------
+# compression (Compression.py)
+# ----------------------------------------------------------------------------
+def svd_flip(u, v, u_based_decision=True):
+    """Deterministic signs: largest |loading| positive (Compression.py:521-564)."""
+    if u_based_decision:
+        idx = np.argmax(np.abs(u), axis=0)
+        signs = np.sign(u[idx, range(u.shape[1])])
+    else:
+        idx = np.argmax(np.abs(v), axis=1)
+        signs = np.sign(v[range(v.shape[0]), idx])
+    return u * signs, v * signs[:, None]
+
+
+def randomized_svd(M, n_components, n_oversamples=10, n_iter=2):
+    """Halko et al. range finder with ``n_iter`` power iterations (Compression.py:337-518)."""
+    n_random = n_components + n_oversamples
+    transpose = M.shape[0] < M.shape[1]
+    if transpose:
+        M = M.T
+    Q = np.random.normal(size=(M.shape[1], n_random))
+    if M.dtype.kind == 'f':
+        Q = Q.astype(M.dtype, copy=False)
+    for _ in range(n_iter):
+        Q = M @ Q
+        Q = M.T @ Q
+    Q, _ = sp_qr(M @ Q, mode='economic')
+    B = Q.T @ M
+    Uhat, s, V = sp_svd(B, full_matrices=False)
+    U = Q @ Uhat
+    U, V = svd_flip(U, V, u_based_decision=not transpose)
+    if transpose:
+        return V[:n_components, :].T, s[:n_components], U[:, :n_components].T
+    return U[:, :n_components], s[:n_components], V[:n_components, :]
+
+
+def clean_compression(U, sigma, Vt, tol_mlsvd, L):
+    """Energy truncation: first i with Σσ[i:]²/Σσ² < tol/L (Compression.py:261-301)."""
+    eps = tol_mlsvd / L
+    tot = np.sum(sigma ** 2)
+    for i in range(1, len(sigma)):
+        if np.sum(sigma[i:] ** 2) / tot < eps:
+            return U[:, :i], sigma[:i], Vt[:i, :], i
+    return U, sigma, Vt, sigma.size
+
+
+def sparse_unfold(data, idxs, dims, mode):
+    """COO → CSR mode unfolding with Kolda column keys (Conversion.py:255-302)."""
+    from scipy.sparse import coo_matrix
+    L = len(dims)
+    dims = [int(d) for d in dims]
+    others = [l for l in range(L) if l != mode - 1]
+    K = np.zeros(L, dtype=np.uint64)
+    s = 1
+    for l in others:
+        K[l] = s
+        s *= dims[l]
+    idxs = np.asarray(idxs, dtype=np.uint64)
+    rows = idxs[:, mode - 1]
+    cols = np.sum(K * idxs, axis=1, dtype=np.uint64)
+    return coo_matrix((data, (rows, cols)), shape=(dims[mode - 1], s)).tocsr()
+
+
+def sparse_multilin_mult(UT, data, idxs, dims):
+    """Dense core ``S = T ×_1 U_1^T ... ×_L U_L^T`` from COO (MultilinearAlgebra.py:145-190)."""
+    idxs = np.asarray(idxs).astype(np.int64)
+    L = len(dims)
+    G = [UT[l][:, idxs[:, l]] for l in range(L)]            # (n_l, nnz)
+    S = G[0] * np.asarray(data, dtype=np.float64)[None, :]
+    for l in range(1, L):
+        S = np.einsum('...k,jk->...jk', S, G[l])
+    return S.sum(axis=-1)
+
+
+def multilin_mult(UT, T):
+    """``(U_1^T, ..., U_L^T) · T`` (MultilinearAlgebra.py:72-105)."""
+    S = T
+    for l in range(len(UT)):
+        S = np.moveaxis(np.tensordot(UT[l], S, axes=(1, l)), 0, l)
+    return S
+
+
+def compute_svd(Tl, dims, R, method, tol_mlsvd, L, l, svd_n_components):
+    """SVD of one unfolding (Compression.py:192-237)."""
+    low_rank = min(R, int(dims[l]))
+    if method == 'sparse':
+        G = Tl
+        n = svd_n_components if svd_n_components is not None else \
+            int(max(L, np.log10(dims[l] * dims[l] * L)) * low_rank)
+        U, s, Vt = randomized_svd(G, n, n_oversamples=10, n_iter=2)
+        s = np.sqrt(s)
+    else:
+        n = svd_n_components if svd_n_components is not None else low_rank
+        U, s, Vt = randomized_svd(Tl, n, n_oversamples=10, n_iter=2)
+    return clean_compression(U, s, Vt, tol_mlsvd, L)
+
+
+def mlsvd(T, Tsize, R, options):
+    """Truncated MLSVD, 'seq' / 'classic' / sparse branches (Compression.py:48-189)."""
+    o = make_options(options)
+    tol_mlsvd = o.tol_mlsvd
+    sparse_in = isinstance(T, list)
+    if sparse_in:
+        data, idxs, dims = T
+        data = np.asarray(data, dtype=np.float64)
+        idxs = np.asarray(idxs, dtype=np.uint64)
+        dims = np.asarray(dims)
+    else:
+        dims = T.shape
+    L = len(dims)
+    if type(tol_mlsvd) == list:
+        tol_mlsvd = tol_mlsvd[0] if L > 3 else tol_mlsvd[1]
+    U, sigmas = [], []
+    if tol_mlsvd == -1:
+        return T, [np.identity(dims[l]) for l in range(L)], unfold(T, 1), [np.ones(dims[l]) for l in range(L)]
+    if sparse_in:
+        T1 = sparse_unfold(data, idxs, dims, 1)
+        for l in range(L):
+            Tl = sparse_unfold(data, idxs, dims, l + 1)
+            G = (Tl @ Tl.T).toarray()
+            Ul, sl, _, _ = compute_svd(G, dims, R, 'sparse', tol_mlsvd, L, l, o.svd_n_components)
+            U.append(Ul)
+            sigmas.append(sl)
+        S = sparse_multilin_mult([u.T for u in U], data, idxs, dims)
+    elif o.mlsvd_method == 'seq':
+        S = np.asarray(T, dtype=np.float64)
+        S_dims = list(dims)
+        T1 = unfold(S, 1)
+        for l in range(L):
+            Sl = unfold(S, l + 1)
+            Ul, sl, Vlt, dim = compute_svd(Sl, dims, R, 'seq', tol_mlsvd, L, l, o.svd_n_components)
+            U.append(Ul)
+            sigmas.append(sl)
+            S_dims[l] = dim
+            S = foldback((Vlt.T * sl).T, l + 1, S_dims)
+    elif o.mlsvd_method == 'classic':
+        T = np.asarray(T, dtype=np.float64)
+        T1 = unfold(T, 1)
+        for l in range(L):
+            Ul, sl, _, _ = compute_svd(unfold(T, l + 1), dims, R, 'classic', tol_mlsvd, L, l,
+                                       o.svd_n_components)
+            U.append(Ul)
+            sigmas.append(sl)
+        S = multilin_mult([u.T for u in U], T)
+    else:
+        raise NotImplementedError("mlsvd_method " + repr(o.mlsvd_method))
+    if type(o.trunc_dims) == list:
+        sl_ = []
+        for l in range(L):
+            sl_.append(slice(0, o.trunc_dims[l]))
+            U[l] = U[l][:, :min(o.trunc_dims[l], U[l].shape[1])]
+        S = S[tuple(sl_)]
+    return S, U, T1, sigmas
+
+
+# ----------------------------------------------------------------------------
+# initialisation and driver (Initialization.py, Auxiliar.py, TensorFox.py)
+# ----------------------------------------------------------------------------
+def clean_zeros(init_factors, dims, R):
+    """Replaces exact zeros by ``1e-4 * randn() * ||W||`` (Initialization.py:361-386)."""
+    for l in range(len(dims)):
+        W = init_factors[l]
+        for i in range(dims[l]):
+            for r in range(R):
+                if W[i, r] == 0.0:
+                    W[i, r] = 1e-4 * np.random.randn() * norm(W)
+    return init_factors
+
+
+def starting_point(S, U, R, ordering, options):
+    """'random' or user-list initial factors in the compressed space (Initialization.py:20-94)."""
+    init = options.initialization
+    dims = S.shape
+    L = len(dims)
+    if type(init) == list:
+        return [U[l].T @ init[ordering[l]] for l in range(L)]
+    if init != 'random':
+        raise NotImplementedError("initialization " + repr(init))
+    f = [np.random.randn(dims[l], R) for l in range(L)]
+    f = clean_zeros(f, dims, R)
+    f = equalize(f, R)
+    return transform(f, options.symm, options.factors_norm)
+
+
+def sort_dims(T):
+    """Modes in decreasing size (Auxiliar.py:93-115)."""
+    if isinstance(T, list):
+        data, idxs, dims = T
+        idxs = np.asarray(idxs, dtype=np.uint64)
+        dims = np.asarray(dims)
+        ordering = np.argsort(-dims)
+        return [data, idxs[:, ordering], tuple(dims[ordering])], ordering
+    dims = np.array(T.shape)
+    ordering = np.argsort(-dims)
+    return np.moveaxis(T, ordering, np.arange(-len(dims), 0)), ordering
+
+
+def unsort_dims(factors, ordering):
+    """Inverse permutation of :func:`sort_dims` (Auxiliar.py:118-128)."""
+    out = [None] * len(factors)
+    for l in range(len(factors)):
+        out[ordering[l]] = factors[l]
+    return out
+
+
+class Output:
+    pass
+
+
+def cpd(T, R, options=None):
+    """``cpd`` → ``tricpd`` for method 'dGN' (TensorFox.py:69-255, 424-655).
+
+    Returns ``(factors, output)`` where ``output`` carries num_steps, rel_error,
+    accuracy, step_sizes, errors, improv, gradients and stop like the reference's.
+    """
+    o = make_options(options)
+    sparse_in = isinstance(T, list)
+    if sparse_in:
+        data_orig = np.asarray(T[0], dtype=np.float64)
+        idxs_orig = np.asarray(T[1], dtype=np.uint64)
+        dims_orig = np.asarray(T[2])
+    Ts, ordering = sort_dims(T)
+    if sparse_in:
+        Tsize = norm(Ts[0])
+        if (o.tol_mlsvd if type(o.tol_mlsvd) != list else o.tol_mlsvd[0]) < 0:
+            o.tol_mlsvd = 1e-16
+    else:
+        Ts = np.asarray(Ts, dtype=np.float64)
+        Tsize = norm(Ts)
+    S, U, T1, sigmas = mlsvd(Ts, Tsize, R, o)
+    init = starting_point(S, U, R, ordering, o)
+    factors, ss, er, im, gr, st = dGN(S, init, R, o)
+    factors = [U[l] @ factors[l] for l in range(len(factors))]
+    refine = o.refine and not sparse_in
+    if refine:
+        factors, ss2, er2, im2, gr2, st2 = dGN(Ts, factors, R, o)
+    else:
+        ss2, er2, im2, gr2, st2 = np.array([0]), np.array([0]), np.array([0]), np.array([0]), 8
+    out = Output()
+    if sparse_in:
+        factors = unsort_dims(factors, ordering)
+        rel_error = sparse_fastnorm(data_orig, idxs_orig, dims_orig, factors) / Tsize
+    else:
+        approx = cpd2unfold1(factors)
+        factors = unsort_dims(factors, ordering)
+        rel_error = er2[-1] if refine else fastnorm(unfold(Ts, 1), approx) / Tsize
+    out.num_steps = len(ss) + (len(ss2) if refine else 0)
+    out.rel_error = rel_error
+    out.accuracy = max(0, 100 * (1 - rel_error))
+    out.step_sizes = [ss, ss2]
+    out.errors = [er, er2]
+    out.improv = [im, im2]
+    out.gradients = [gr, gr2]
+    out.stop = [st, st2]
+    out.options = o
+    return factors, out

@@ -1,0 +1,240 @@
+"""Generates the golden fixtures in this folder by running the reference itself.
+
+Run from the repository root, in a container where the reference source tree is
+mounted (see ``ref_harness.py``):
+
+    python tests/golden/make_golden.py
+
+Each ``.npz`` holds seeded inputs and the reference's outputs for one case.  The
+fixtures are small (a few hundred KB in total) and committed; tests compare both
+the oracle (``oracle/tfx_oracle.py``) and the CUDA path against them.
+"""
+import io
+import contextlib
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+from ref_harness import load_reference  # noqa: E402
+
+tfx = load_reference()
+import TensorFox.GaussNewton as gn  # noqa: E402
+import TensorFox.Conversion as cnv  # noqa: E402
+import TensorFox.Critical as crt  # noqa: E402
+import TensorFox.Compression as cmpr  # noqa: E402
+import TensorFox.MultilinearAlgebra as mla  # noqa: E402
+
+
+def save(name, **arrays):
+    path = os.path.join(HERE, name + ".npz")
+    np.savez_compressed(path, **{k: np.asarray(v) for k, v in arrays.items()})
+    print("wrote", path)
+
+
+def planted(dims, R, noise, seed):
+    rng = np.random.default_rng(seed)
+    W = [rng.standard_normal((d, R)) for d in dims]
+    T = cnv.cpd2tens([w.copy() for w in W])
+    if noise:
+        E = rng.standard_normal(T.shape)
+        T = T + noise * np.linalg.norm(T) / np.linalg.norm(E) * E
+    return T, W
+
+
+def units(name, dims, R, seed, damp=0.7, cg_iters=6):
+    """gramians / regularization / precond / grad / matvec / cg on seeded inputs."""
+    rng = np.random.default_rng(seed)
+    L = len(dims)
+    T = rng.standard_normal(dims)
+    W = [rng.standard_normal((d, R)) for d in dims]
+    v = rng.standard_normal(R * sum(dims))
+    data = gn.prepare_data(dims, R)
+    Gr, P1, P2, A, B, P_VT_W, result, result_tmp, Gamma, gamma, sum_dims, M, rc, P, Q, z, g, JtJg, N, gg = data
+    Gr, P1, P2 = gn.gramians([w.copy() for w in W], Gr, P1, P2)
+    Gamma, gamma = gn.regularization(Gamma, gamma, P1, np.array(dims), sum_dims)
+    M = gn.precond(Gamma, gamma, M.copy(), damp, np.array(dims), sum_dims)
+    Tl = [cnv.unfold_C(T, l + 1) for l in range(L)]
+    grad = gn.compute_grad(Tl, [w.copy() for w in W], P1, g.copy(), N, gg, np.array(dims), sum_dims).copy()
+    V = [v[sum_dims[l]:sum_dims[l + 1]].reshape(R, dims[l]) for l in range(L)]
+    for l in range(L):
+        np.dot(V[l], W[l], out=A[l])
+        np.dot(V[l].T, P1[l], out=B[l])
+    mv = gn.matvec([w.copy() for w in W], P2, P_VT_W, result, result_tmp, z.copy(), A, B, np.array(dims), sum_dims).copy()
+    data = gn.prepare_data(dims, R)
+    y0 = np.zeros(R * sum(dims))
+    y, cgrad, jtj, itn, rn = gn.cg(Tl, [w.copy() for w in W], data, y0, damp, cg_iters, 0.0)
+    T1a = np.empty(Tl[0].shape)
+    T1a = cnv.cpd2unfold1(T1a, [w.copy() for w in W])
+    fn = crt.fastnorm(Tl[0], T1a)
+    x = np.concatenate([w.flatten('F') for w in W])
+    eqf = cnv.x2cpd(x.copy() * 1.5, [w.copy() for w in W])
+    save(name, dims=np.array(dims), R=R, T=T, x=x, v=v, damp=damp, cg_iters=cg_iters,
+         Gr=Gr, P1=P1, P2=P2, Gamma=Gamma, gamma=gamma, M=M, grad=grad, matvec=mv,
+         cg_y=y, cg_grad=cgrad, cg_jtj=jtj, cg_itn=itn, cg_rn=rn, T1_approx=T1a, fastnorm=fn,
+         eq_x=np.concatenate([f.flatten('F') for f in eqf]))
+
+
+class Opt:
+    pass
+
+
+def dgn_case(name, dims, R, seed, noise=1e-3, **opts):
+    """dGN trajectory from an explicit start; 'cg' budgets replayed from a fixed seed."""
+    T, W = planted(dims, R, noise, seed)
+    rng = np.random.default_rng(seed + 1000)
+    init = [w + 0.3 * rng.standard_normal(w.shape) for w in W]
+    o = Opt()
+    for k, v in opts.items():
+        setattr(o, k, v)
+    o = tfx.make_options(o)
+    np.random.seed(seed)
+    bf, ss, er, im, gr, st = gn.dGN(T, [w.copy() for w in init], R, o)
+    save(name, T=T, init_x=np.concatenate([w.flatten('F') for w in init]), R=R, seed=seed,
+         dims=np.array(dims), best_x=np.concatenate([w.flatten('F') for w in bf]),
+         step_sizes=ss, errors=er, improv=im, gradients=gr, stop=st,
+         opt_names=np.array(list(opts.keys())), opt_values=np.array([repr(v) for v in opts.values()]))
+
+
+def mlsvd_case(name, dims, R, seed, method='seq', noise=1e-2):
+    T, _ = planted(dims, R, noise, seed)
+    o = Opt()
+    o.mlsvd_method = method
+    o = tfx.make_options(o)
+    np.random.seed(seed)
+    S, U, T1, sig = cmpr.mlsvd(T, np.linalg.norm(T), R, o)
+    save(name, T=T, R=R, seed=seed, S=S, sigmas=np.concatenate(sig),
+         ranks=np.array([u.shape[1] for u in U]), U=np.concatenate([u.flatten('F') for u in U]),
+         method=method)
+
+
+def cpd_case(name, dims, R, seed, noise, **opts):
+    T, W = planted(dims, R, noise, seed)
+    o = Opt()
+    for k, v in opts.items():
+        setattr(o, k, v)
+    np.random.seed(seed)
+    f, out = tfx.cpd(T, R, o)
+    save(name, T=T, R=R, seed=seed, planted=np.concatenate([w.flatten('F') for w in W]),
+         factors=np.concatenate([w.flatten('F') for w in f]), rel_error=out.rel_error,
+         num_steps=out.num_steps, errors=out.errors[0], stop=np.array(out.stop),
+         opt_names=np.array(list(opts.keys())), opt_values=np.array([repr(v) for v in opts.values()]))
+
+
+def sparse_case(name, dims, R, nnz, seed):
+    rng = np.random.default_rng(seed)
+    L = len(dims)
+    lin = rng.choice(int(np.prod(dims)), size=nnz, replace=False)
+    idxs = np.stack(np.unravel_index(lin, dims), axis=1).astype(np.int64)
+    W = [rng.standard_normal((d, R)) for d in dims]
+    vals = np.ones(nnz)
+    for l in range(L):
+        vals = vals * 0 + vals  # keep dtype
+    model = np.ones((nnz, R))
+    for l in range(L):
+        model *= W[l][idxs[:, l]]
+    data = model.sum(1) + 0.01 * rng.standard_normal(nnz)
+    fnorm = crt.sparse_fastnorm(data, idxs.astype(np.uint64), np.array(dims), [w.copy() for w in W])
+    grams = []
+    for l in range(L):
+        Tl = cnv.sparse_unfold(data, idxs.astype(np.uint64), np.array(dims), l + 1)
+        grams.append((Tl @ Tl.T).toarray().flatten())
+    UT = [rng.standard_normal((min(R + 1, d), d)) for d in dims]
+    S = mla.sparse_multilin_mult([u.copy() for u in UT], data, idxs.astype(np.uint64), np.array(dims))
+    np.random.seed(seed)
+    f, out = tfx.cpd([data, idxs, np.array(dims)], R)
+    save(name, dims=np.array(dims), R=R, idxs=idxs, data=data, W=np.concatenate([w.flatten('F') for w in W]),
+         sparse_fastnorm=fnorm, grams=np.concatenate(grams), UT=np.concatenate([u.flatten() for u in UT]),
+         UT_rows=np.array([u.shape[0] for u in UT]), S=S, cpd_rel_error=out.rel_error,
+         cpd_factors=np.concatenate([w.flatten('F') for w in f]), cpd_stop=np.array(out.stop))
+
+
+def dogleg_units(name, seed):
+    """dogleg() on every branch and compute_dogleg_steps() from a long step (‖y‖ > delta)."""
+    rng = np.random.default_rng(seed)
+    n = 30
+    rows = []
+    grad = rng.standard_normal(n)
+    H = rng.standard_normal((n, n))
+    H = H @ H.T + n * np.eye(n)
+    jtj = H @ grad
+    for scale, delta in [(0.01, 1.0), (5.0, 0.001), (5.0, 1.0), (5.0, 3.0), (2.0, 0.2)]:
+        y = scale * rng.standard_normal(n)
+        rows.append(np.concatenate([y, [delta], gn.dogleg(y, grad, jtj, delta)]))
+    dims, R = [7, 6, 5], 3
+    T, W = planted(dims, R, 0.05, seed)
+    Tl = [cnv.unfold_C(T, l + 1) for l in range(3)]
+    x = np.concatenate([w.flatten('F') for w in W]) + 0.05 * rng.standard_normal(R * sum(dims))
+    y = 4.0 * rng.standard_normal(R * sum(dims))
+    g2 = rng.standard_normal(R * sum(dims))
+    j2 = 50 * g2 + rng.standard_normal(R * sum(dims))
+    factors = [np.zeros((d, R)) for d in dims]
+    err = 10.0
+    ip = (0.3, 'cg', 100, 1, 1e-16, 10, False, 0, -1)
+    bf, bx, by, be = gn.compute_dogleg_steps(np.linalg.norm(T), Tl, np.empty(Tl[0].shape), factors, g2, j2,
+                                             x.copy(), y.copy(), err, ip)
+    save(name, grad=grad, jtj=jtj, rows=np.array(rows), T=T, x=x, y=y, g2=g2, j2=j2, err=err, damp=0.3,
+         best_x=bx, best_y=by, best_error=be, best_f=np.concatenate([f.flatten('F') for f in bf]))
+
+
+def kr_case(name, seed):
+    rng = np.random.default_rng(seed)
+    A, B = rng.standard_normal((4, 3)), rng.standard_normal((5, 3))
+    M = mla.khatri_rao(A, B, np.empty((20, 3)))
+    T = rng.standard_normal((4, 3, 5, 2))
+    unf = [cnv.unfold(T, m + 1) for m in range(4)]
+    save(name, A=A, B=B, KR=M, T=T, unf=np.concatenate([u.flatten() for u in unf]))
+
+
+def reference_tests_case(name):
+    """The 2x2x2 tensor of tests/simple_tensor_cpd_options.py:8-15 at R=3 and options."""
+    m = 2
+    T = np.zeros((m, m, m))
+    s = 0
+    for k in range(m):
+        for i in range(m):
+            for j in range(m):
+                T[i, j, k] = s
+                s += 1
+    errs = []
+    for seed in range(10):
+        np.random.seed(seed)
+        f, out = tfx.cpd(T, 3)
+        errs.append(out.rel_error)
+    o = Opt()
+    o = tfx.make_options(o)
+    o.initialization = [np.ones((m, 3))] * 3
+    np.random.seed(0)
+    _, out_ones = tfx.cpd(T, 3, o)
+    save(name, T=T, best_of_10=np.array(errs), ones_init_error=out_ones.rel_error,
+         ones_init_errors=out_ones.errors[0])
+
+
+def main():
+    with contextlib.redirect_stdout(io.StringIO()):
+        pass
+    units("units_L3", [7, 5, 4], 3, 1)
+    units("units_L4", [5, 4, 3, 3], 2, 2)
+    units("units_L3_big", [12, 10, 9], 4, 3, damp=0.2, cg_iters=9)
+    units("units_L5", [4, 3, 3, 2, 2], 3, 4)
+    kr_case("kr_unfold", 5)
+    dogleg_units("dogleg_units", 6)
+    dgn_case("dgn_static_L3", [9, 8, 7], 3, 11, inner_method='cg_static', cg_maxiter=8, maxiter=40)
+    dgn_case("dgn_cg_L3", [12, 10, 9], 4, 12, maxiter=60)
+    dgn_case("dgn_cg_L4", [6, 5, 5, 4], 3, 13, maxiter=50)
+    dgn_case("dgn_dogleg_L3", [8, 7, 6], 3, 14, noise=0.2, tol_jump=0.99, maxiter=30)
+    dgn_case("dgn_small_L3", [4, 4, 3], 2, 15, maxiter=80)
+    mlsvd_case("mlsvd_seq", [20, 15, 12], 4, 21)
+    mlsvd_case("mlsvd_classic", [18, 14, 11], 3, 22, method='classic')
+    mlsvd_case("mlsvd_seq_L4", [10, 9, 8, 7], 3, 23)
+    cpd_case("cpd_c1_small", [30, 25, 20], 5, 31, 1e-6)
+    cpd_case("cpd_L4", [12, 11, 10, 9], 3, 32, 1e-4)
+    cpd_case("cpd_refine", [15, 12, 10], 4, 33, 1e-3, refine=True)
+    sparse_case("sparse_L3", [10, 9, 8], 3, 60, 41)
+    reference_tests_case("ref_tests_2x2x2")
+
+
+if __name__ == "__main__":
+    main()

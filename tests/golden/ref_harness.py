@@ -1,0 +1,79 @@
+"""Loads the reference Tensor Fox package (v1.2.1) for fixture generation only.
+
+The reference needs Numba, matplotlib, pandas and IPython at import time; none is
+installed here, so this module registers minimal stand-ins:
+
+* ``numba.njit`` / ``numba.prange`` become identity / ``range`` (the reference's
+  ``@njit`` kernels then run as plain Python with identical arithmetic);
+* plotting and display modules become empty namespaces.
+
+It also removes the one-second ``time.sleep`` in ``Auxiliar.consistency``
+(Auxiliar.py:76) and replaces ``Compression.sparse_dot_mkl_call``
+(Compression.py:240-258) by the SciPy product ``(Tl @ Tl.T).toarray()``, which is
+the dense matrix MKL's ``dot_product_mkl(..., dense=True)`` returns.
+
+Only ``tests/golden/make_golden.py`` imports this file, and only in a container
+where the reference source tree is mounted.  Nothing shipped or run on a GPU
+machine reads the reference.
+"""
+import os
+import sys
+import types
+
+REF_MODULES = os.environ.get("TFX_REFERENCE_MODULES", "/root/reference/modules")
+
+
+def _stub_modules():
+    if "numba" not in sys.modules:
+        numba = types.ModuleType("numba")
+
+        def njit(*args, **kwargs):
+            if len(args) == 1 and callable(args[0]) and not kwargs:
+                return args[0]
+            return lambda f: f
+
+        numba.njit = njit
+        numba.jit = njit
+        numba.prange = range
+        errors = types.ModuleType("numba.errors")
+        for name in ("NumbaDeprecationWarning", "NumbaPendingDeprecationWarning",
+                     "NumbaPerformanceWarning"):
+            setattr(errors, name, type(name, (Warning,), {}))
+        numba.errors = errors
+        sys.modules["numba"] = numba
+        sys.modules["numba.errors"] = errors
+    for name in ("matplotlib", "matplotlib.pyplot", "IPython", "IPython.display", "pandas"):
+        if name not in sys.modules:
+            sys.modules[name] = types.ModuleType(name)
+    sys.modules["matplotlib"].pyplot = sys.modules["matplotlib.pyplot"]
+    sys.modules["IPython"].display = sys.modules["IPython.display"]
+
+
+_TFX = None
+
+
+def load_reference():
+    """Import and patch the reference package; returns the ``TensorFox`` module."""
+    global _TFX
+    if _TFX is not None:
+        return _TFX
+    if not os.path.isdir(REF_MODULES):
+        raise RuntimeError("reference source tree not found at " + REF_MODULES)
+    _stub_modules()
+    if REF_MODULES not in sys.path:
+        sys.path.insert(0, REF_MODULES)
+    import io
+    import contextlib
+    with contextlib.redirect_stderr(io.StringIO()):
+        import TensorFox as tfx  # noqa: E402
+    import TensorFox.Auxiliar as aux
+    import TensorFox.Compression as cmpr
+
+    aux.time = types.SimpleNamespace(sleep=lambda s: None, time=__import__("time").time)
+
+    def _dense_gram(Tl, display):
+        return (Tl @ Tl.T).toarray()
+
+    cmpr.sparse_dot_mkl_call = _dense_gram
+    _TFX = tfx
+    return tfx
