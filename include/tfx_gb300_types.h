@@ -1,0 +1,68 @@
+/* Plain-C descriptor types shared by the C ABI (tfx_gb300.h) and the kernels. */
+#ifndef TFX_GB300_TYPES_H
+#define TFX_GB300_TYPES_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define TFX_MAX_ORDER 12
+
+/* Status codes returned by every entry point. */
+enum tfx_status {
+  TFX_STATUS_OK = 0,
+  TFX_STATUS_ERR_ARG = 1,        /* invalid argument (shape, rank, pointer) */
+  TFX_STATUS_ERR_NUMERIC = 2,    /* non-finite value met where the reference would stop */
+  TFX_STATUS_ERR_TIMEOUT = 3,    /* a bounded device wait ran out */
+  TFX_STATUS_ERR_CUDA = 4,       /* CUDA runtime error (message via tfx_last_error) */
+  TFX_STATUS_ERR_UNSUPPORTED = 5 /* configuration outside the supported set */
+};
+
+/* Element type of tensors and factors. */
+enum tfx_dtype { TFX_F32 = 0, TFX_F64 = 1 };
+
+/* One dense damped Gauss-Newton problem (GaussNewton.py:29 dGN(T, factors, R, options)).
+ * All pointers are device pointers owned by the caller.
+ *   tensor : C-order array of prod(dims) elements
+ *   x      : flat start point, concat_l vec_F(W_l), R*sum(dims) elements (read)
+ *   best   : best factors found, same layout (written)
+ *   work   : scratch of tfx_dgn_workspace_bytes() bytes
+ *   budgets: [maxiter] CG iteration caps (GaussNewton.py:267 or cg_maxiter)
+ *   damp_sched: [maxiter] damping schedule when options.init_damp is a list, else NULL
+ *   stats  : [4*maxiter] errors, step_sizes, improv, gradients (written)
+ *   result : [4] stop code, iterations run, status, dogleg fallbacks (written)
+ *   info   : [4] |T|, best error, final damping, mean|T| (written) */
+typedef struct tfx_dgn_problem {
+  int L;
+  int R;
+  int dims[TFX_MAX_ORDER];
+  const void* tensor;
+  const void* x;
+  void* best;
+  void* work;
+  const int* budgets;
+  const double* damp_sched;
+  double* stats;
+  int* result;
+  double* info;
+} tfx_dgn_problem;
+
+/* Solver options (Auxiliar.py:258-283 defaults; TensorFox.py:84-213 meaning). */
+typedef struct tfx_dgn_options {
+  int maxiter;
+  double tol;
+  double tol_step;
+  double tol_improv;
+  double tol_grad;
+  double tol_jump;
+  double cg_tol;
+  double init_damp;
+  int use_damp_sched; /* 1: damp_sched holds init_damp as a list */
+  int symm;           /* options.symm */
+  double factors_norm; /* options.factors_norm (0 = off) */
+} tfx_dgn_options;
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,55 @@
+// C ABI of the dGN engine: workspace sizing, validation and dispatch.
+#include "dgn_engine.cuh"
+
+using namespace tfx;
+
+extern "C" size_t tfx_dgn_workspace_bytes(int dtype, int L, const int* dims, int R) {
+  if (L < 2 || L > TFX_MAX_ORDER || R < 1 || dims == nullptr) return 0;
+  int s = 0;
+  for (int l = 0; l < L; ++l) s += dims[l];
+  return ws_layout(L, R, R * s, dtype == TFX_F64 ? 8 : 4).total;
+}
+
+extern "C" int tfx_dgn_solve(int dtype, const tfx_dgn_problem* h_probs, tfx_dgn_problem* d_probs, int nprob,
+                             const tfx_dgn_options* op, int cluster, void* stream) {
+  if (h_probs == nullptr || d_probs == nullptr || op == nullptr || nprob < 1)
+    return tfx_set_error(TFX_STATUS_ERR_ARG, "null argument");
+  if (cluster != 1 && cluster != 2 && cluster != 4 && cluster != 8 && cluster != 16)
+    return tfx_set_error(TFX_STATUS_ERR_ARG, "cluster must be 1, 2, 4, 8 or 16");
+  if (op->maxiter < 1) return tfx_set_error(TFX_STATUS_ERR_ARG, "maxiter must be >= 1");
+  int maxL = 0, maxR = 0, maxd = 0, maxdim_or_R = 0;
+  for (int p = 0; p < nprob; ++p) {
+    const tfx_dgn_problem& q = h_probs[p];
+    if (q.L < 2 || q.L > TFX_MAX_ORDER || q.R < 1) return tfx_set_error(TFX_STATUS_ERR_ARG, "bad order or rank");
+    if (q.R < cluster) return tfx_set_error(TFX_STATUS_ERR_ARG, "rank smaller than cluster size");
+    if (!q.tensor || !q.x || !q.best || !q.work || !q.budgets || !q.stats || !q.result || !q.info)
+      return tfx_set_error(TFX_STATUS_ERR_ARG, "null device pointer in problem");
+    if (op->use_damp_sched && !q.damp_sched) return tfx_set_error(TFX_STATUS_ERR_ARG, "missing damp schedule");
+    long long n = 1;
+    for (int l = 0; l < q.L; ++l) {
+      if (q.dims[l] < 1) return tfx_set_error(TFX_STATUS_ERR_ARG, "bad dimension");
+      n *= q.dims[l];
+      maxd = q.dims[l] > maxd ? q.dims[l] : maxd;
+    }
+    if (n > (1LL << 40)) return tfx_set_error(TFX_STATUS_ERR_ARG, "tensor too large");
+    if (op->symm) {
+      for (int l = 1; l < q.L; ++l)
+        if (q.dims[l] != q.dims[0]) return tfx_set_error(TFX_STATUS_ERR_ARG, "symm needs equal dims");
+    }
+    maxL = q.L > maxL ? q.L : maxL;
+    maxR = q.R > maxR ? q.R : maxR;
+  }
+  maxdim_or_R = maxd > maxR ? maxd : maxR;
+  const int TS = maxdim_or_R <= 16 ? 1 : (maxdim_or_R <= 32 ? 2 : 4);
+  const int maxncol = (maxR + cluster - 1) / cluster;
+  const size_t es = dtype == TFX_F64 ? 8 : 4;
+  if (op->maxiter > 4096) return tfx_set_error(TFX_STATUS_ERR_UNSUPPORTED, "maxiter above 4096");
+  SmemPlan sp = smem_plan(TS, es, maxL, maxR, maxd, maxncol, op->maxiter);
+  if (sp.total > 220 * 1024) return tfx_set_error(TFX_STATUS_ERR_UNSUPPORTED, "problem too large for the engine's shared memory; use a larger cluster");
+  cudaStream_t st = (cudaStream_t)stream;
+  cudaError_t e = cudaMemcpyAsync(d_probs, h_probs, sizeof(tfx_dgn_problem) * nprob, cudaMemcpyHostToDevice, st);
+  if (e != cudaSuccess) return tfx_set_cuda_error(e, "descriptor copy");
+  if (dtype == TFX_F32) return launch_dgn_f32(TS, d_probs, nprob, op, cluster, sp, st);
+  if (dtype == TFX_F64) return launch_dgn_f64(TS, d_probs, nprob, op, cluster, sp, st);
+  return tfx_set_error(TFX_STATUS_ERR_ARG, "dtype");
+}

@@ -1,0 +1,10 @@
+"""Tensor Fox's damped Gauss-Newton CPD path, rebuilt on GB300 (sm_103a) CUDA kernels.
+
+Drop-in functions (same names, arguments and return values as Tensor Fox 1.2.1):
+``cpd``, ``mlsvd``, ``dGN``, ``make_options``, ``cpd2tens``, ``cpd2unfold1``,
+``unfold``, ``foldback``.  All computation runs in ``libtfx_gb300.so`` on the GPU.
+"""
+__version__ = "1.2.1+gb300"
+
+from .options import make_options, Options  # noqa: F401
+from .gauss_newton import dGN  # noqa: F401

@@ -1,0 +1,89 @@
+"""ctypes binding of ``libtfx_gb300.so`` (the C ABI declared in include/tfx_gb300.h).
+
+The library is the only compute path: every public routine of this package calls
+into it and raises if it is missing or if no CUDA device is present.
+"""
+import ctypes
+import os
+from ctypes import POINTER, c_double, c_int, c_longlong, c_size_t, c_void_p, c_char_p
+
+MAX_ORDER = 12
+F32, F64 = 0, 1
+
+STATUS = {0: "ok", 1: "invalid argument", 2: "numeric error", 3: "timeout", 4: "CUDA error",
+          5: "unsupported configuration"}
+
+
+class TfxError(RuntimeError):
+    """Raised when an entry point of the C ABI returns a non-zero status."""
+
+
+class DgnProblem(ctypes.Structure):
+    _fields_ = [("L", c_int), ("R", c_int), ("dims", c_int * MAX_ORDER),
+                ("tensor", c_void_p), ("x", c_void_p), ("best", c_void_p), ("work", c_void_p),
+                ("budgets", c_void_p), ("damp_sched", c_void_p), ("stats", c_void_p),
+                ("result", c_void_p), ("info", c_void_p)]
+
+
+class DgnOptions(ctypes.Structure):
+    _fields_ = [("maxiter", c_int), ("tol", c_double), ("tol_step", c_double), ("tol_improv", c_double),
+                ("tol_grad", c_double), ("tol_jump", c_double), ("cg_tol", c_double),
+                ("init_damp", c_double), ("use_damp_sched", c_int), ("symm", c_int),
+                ("factors_norm", c_double)]
+
+
+_LIB = None
+
+
+def lib_path():
+    from ._build import LIB
+    return LIB
+
+
+def load():
+    """Loads the compiled library (building it first if it is absent)."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    path = lib_path()
+    if not os.path.exists(path):
+        from ._build import build
+        build()
+    lib = ctypes.CDLL(path)
+    _declare(lib)
+    _LIB = lib
+    return lib
+
+
+def _declare(lib):
+    lib.tfx_last_error.restype = c_char_p
+    lib.tfx_launch_count.restype = c_longlong
+    lib.tfx_version.restype = c_int
+    lib.tfx_dgn_workspace_bytes.restype = c_size_t
+    lib.tfx_dgn_workspace_bytes.argtypes = [c_int, c_int, POINTER(c_int), c_int]
+    lib.tfx_dgn_solve.restype = c_int
+    lib.tfx_dgn_solve.argtypes = [c_int, POINTER(DgnProblem), c_void_p, c_int, POINTER(DgnOptions), c_int,
+                                  c_void_p]
+    for name, args in _EXTRA_SIGNATURES.items():
+        fn = getattr(lib, name, None)
+        if fn is not None:
+            fn.restype = c_int
+            fn.argtypes = args
+
+
+# Remaining entry points: (name -> argtypes); all return an int status.
+_EXTRA_SIGNATURES = {}
+
+
+def register(name, *args):
+    _EXTRA_SIGNATURES[name] = list(args)
+
+
+def check(status):
+    if status != 0:
+        msg = _LIB.tfx_last_error().decode() if _LIB is not None else ""
+        raise TfxError("%s: %s" % (STATUS.get(status, "status %d" % status), msg))
+
+
+def launch_count():
+    return int(load().tfx_launch_count())

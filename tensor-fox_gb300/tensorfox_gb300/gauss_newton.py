@@ -1,0 +1,183 @@
+"""Damped Gauss-Newton on the device (GaussNewton.py:29 ``dGN``).
+
+``dGN(T, factors, R, options)`` keeps the reference's signature and return
+tuple.  The whole iteration (CG inner solves, dogleg fallback, damping updates
+and stop tests) runs as one launch of the cluster-persistent engine
+(``tfx_dgn_solve``); the host only prepares the CG caps and reads the results.
+
+The 'cg' inner method draws its CG cap from NumPy's global RNG once per
+iteration (GaussNewton.py:267).  The caps are drawn here from a copy of the RNG
+state, and afterwards the real RNG is advanced by exactly the draws the
+reference would have made, so seeded runs stay in step with it.
+"""
+import ctypes
+
+import numpy as np
+import torch
+
+from . import _dev, _lib
+from .options import make_options
+
+
+def _inner_of(options, it):
+    im = options.inner_method
+    return im[it] if isinstance(im, list) else im
+
+
+def cg_budgets(options, L):
+    """CG caps for every iteration, drawn without consuming the global RNG."""
+    state = np.random.get_state()
+    out = np.zeros(options.maxiter, dtype=np.int32)
+    try:
+        for it in range(options.maxiter):
+            inner = _inner_of(options, it)
+            if inner == 'cg':
+                out[it] = 1 + (L - 2) * int(options.cg_factor * np.random.randint(1 + it ** 0.4, 2 + it ** 0.9))
+            elif inner == 'cg_static':
+                out[it] = options.cg_maxiter
+            else:
+                raise NotImplementedError(
+                    "inner_method %r is outside the damped Gauss-Newton CG path" % (inner,))
+    finally:
+        np.random.set_state(state)
+    return out
+
+
+def advance_rng(options, iterations):
+    """Consumes the RNG draws the reference's 'cg' caps make in ``iterations`` steps."""
+    for it in range(iterations):
+        if _inner_of(options, it) == 'cg':
+            np.random.randint(1 + it ** 0.4, 2 + it ** 0.9)
+
+
+def auto_cluster(dims, R):
+    n = int(np.prod(dims))
+    work = n * R * len(dims)
+    for c, lim in ((1, 2e6), (2, 8e6), (4, 3e7), (8, 1e8)):
+        if work < lim:
+            return max(1, min(c, R))
+    return max(1, min(16, R))
+
+
+def _cluster_candidates(c, R):
+    cands = [x for x in (1, 2, 4, 8, 16) if x >= c and x <= max(R, 1)]
+    return cands or [1]
+
+
+class _Batch:
+    """Device buffers for a set of dGN problems solved in one engine launch."""
+
+    def __init__(self, tensors, xs, R_list, options, precision):
+        self.precision = precision
+        dt = _dev.torch_dtype(precision)
+        self.es = 8 if precision == "fp64" else 4
+        lib = _lib.load()
+        self.n = len(tensors)
+        self.options = options
+        self.maxiter = int(options.maxiter)
+        self.tensors = tensors
+        self.xs = xs
+        self.dims = [tuple(int(d) for d in t.shape) for t in tensors]
+        self.R = R_list
+        self.best = [torch.empty_like(x) for x in xs]
+        self.ws = []
+        for t, R in zip(tensors, R_list):
+            L = t.dim()
+            dims_c = (ctypes.c_int * L)(*t.shape)
+            nb = lib.tfx_dgn_workspace_bytes(_dev.lib_dtype(precision), L, dims_c, int(R))
+            self.ws.append(torch.empty(int(nb), dtype=torch.uint8, device=t.device))
+        self.budgets = [torch.from_numpy(cg_budgets(options, t.dim())).to(t.device) for t in tensors]
+        sched = options.init_damp if isinstance(options.init_damp, list) else None
+        self.sched = None
+        if sched is not None:
+            self.sched = torch.tensor(np.asarray(sched, dtype=np.float64), device=tensors[0].device)
+        self.stats = torch.zeros((self.n, 4 * self.maxiter), dtype=torch.float64, device=tensors[0].device)
+        self.result = torch.zeros((self.n, 4), dtype=torch.int32, device=tensors[0].device)
+        self.info = torch.zeros((self.n, 4), dtype=torch.float64, device=tensors[0].device)
+        self.desc = (_lib.DgnProblem * self.n)()
+        for p in range(self.n):
+            d = self.desc[p]
+            d.L = len(self.dims[p])
+            d.R = int(R_list[p])
+            for l, v in enumerate(self.dims[p]):
+                d.dims[l] = v
+            d.tensor = _dev.ptr(tensors[p])
+            d.x = _dev.ptr(xs[p])
+            d.best = _dev.ptr(self.best[p])
+            d.work = _dev.ptr(self.ws[p])
+            d.budgets = _dev.ptr(self.budgets[p])
+            d.damp_sched = _dev.ptr(self.sched) if self.sched is not None else None
+            d.stats = _dev.ptr(self.stats[p])
+            d.result = _dev.ptr(self.result[p])
+            d.info = _dev.ptr(self.info[p])
+        self.d_desc = torch.empty(ctypes.sizeof(_lib.DgnProblem) * self.n, dtype=torch.uint8,
+                                  device=tensors[0].device)
+        o = _lib.DgnOptions()
+        o.maxiter = self.maxiter
+        o.tol, o.tol_step, o.tol_improv = float(options.tol), float(options.tol_step), float(options.tol_improv)
+        o.tol_grad, o.tol_jump, o.cg_tol = float(options.tol_grad), float(options.tol_jump), float(options.cg_tol)
+        o.init_damp = 0.0 if sched is not None else float(options.init_damp)
+        o.use_damp_sched = 1 if sched is not None else 0
+        o.symm = 1 if options.symm else 0
+        o.factors_norm = float(options.factors_norm)
+        self.opts = o
+
+    def launch(self, cluster, stream=None):
+        lib = _lib.load()
+        st = _dev.stream() if stream is None else stream
+        cands = _cluster_candidates(cluster, min(self.R))
+        last = None
+        for c in cands:
+            status = lib.tfx_dgn_solve(_dev.lib_dtype(self.precision), self.desc, ctypes.c_void_p(_dev.ptr(self.d_desc)),
+                                       self.n, ctypes.byref(self.opts), c, ctypes.c_void_p(st))
+            if status == 5:      # does not fit: retry with a wider cluster
+                last = status
+                continue
+            _lib.check(status)
+            return c
+        _lib.check(last)
+
+
+def _precision_of(T, options):
+    p = getattr(options, 'precision', None)
+    if p in ('fp64', 'fp32'):
+        return p
+    if p not in (None, 'auto'):
+        raise ValueError("precision must be 'fp64', 'fp32' or None")
+    if isinstance(T, torch.Tensor):
+        return 'fp64' if T.dtype == torch.float64 else 'fp32'
+    return 'fp64' if np.asarray(T).dtype == np.float64 else 'fp32'
+
+
+def dGN_device(Td, x0d, R, options, precision, cluster=None):
+    """Runs the engine on device-resident inputs; returns device results."""
+    b = _Batch([Td], [x0d], [R], options, precision)
+    c = cluster if cluster is not None else (options.cluster or auto_cluster(Td.shape, R))
+    b.launch(c)
+    return b
+
+
+def dGN(T, factors, R, options=None, precision=None):
+    """Damped Gauss-Newton (GaussNewton.py:29-251) on the device.
+
+    Returns ``(best_factors, step_sizes, errors, improv, gradients, stop)`` with
+    NumPy float64 arrays, exactly like the reference.
+    """
+    _dev.require_cuda()
+    options = make_options(options) if not hasattr(options, 'bi_method_parameters') else options
+    if precision is not None:
+        options.precision = precision
+    prec = _precision_of(T, options)
+    dt = _dev.torch_dtype(prec)
+    Td = _dev.to_device(T, dt)
+    dims = tuple(Td.shape)
+    x0 = torch.from_numpy(_dev.flat_factors(factors)).to(device=Td.device, dtype=dt)
+    b = dGN_device(Td, x0, R, options, prec)
+    res = b.result[0].cpu().numpy()
+    stats = b.stats[0].cpu().numpy()
+    n = int(res[1])
+    advance_rng(options, n)
+    best = _dev.unflat(b.best[0].double().cpu().numpy(), dims, R)
+    m = options.maxiter
+    return (best, stats[m:m + n].copy(), stats[:n].copy(), stats[2 * m:2 * m + n].copy(),
+            stats[3 * m:3 * m + n].copy(), int(res[0]))

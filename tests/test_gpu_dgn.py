@@ -1,0 +1,97 @@
+"""Device dGN engine vs the reference's golden trajectories and the oracle."""
+import numpy as np
+import pytest
+
+import tfx_oracle as orc
+from conftest import load_golden, split_x
+
+pytestmark = pytest.mark.gpu
+
+tfx = pytest.importorskip("tensorfox_gb300")
+
+
+def _opts(g, mod):
+    o = mod.Options()
+    for k, v in zip(g["opt_names"], g["opt_values"]):
+        setattr(o, str(k), eval(str(v)))
+    return mod.make_options(o)
+
+
+@pytest.mark.parametrize("name", ["dgn_static_L3", "dgn_cg_L3", "dgn_cg_L4", "dgn_small_L3"])
+def test_dgn_fp64_matches_reference_trajectory(name):
+    g = load_golden(name)
+    dims, R = [int(d) for d in g["dims"]], int(g["R"])
+    np.random.seed(int(g["seed"]))
+    bf, ss, er, im, gr, st = tfx.dGN(g["T"], split_x(g["init_x"], dims, R), R, _opts(g, tfx))
+    assert st == int(g["stop"])
+    assert len(er) == len(g["errors"])
+    np.testing.assert_allclose(er, g["errors"], rtol=1e-6, atol=1e-12)
+    np.testing.assert_allclose(ss, g["step_sizes"], rtol=1e-5, atol=1e-12)
+    np.testing.assert_allclose(gr, g["gradients"], rtol=1e-5, atol=1e-12)
+    np.testing.assert_allclose(np.concatenate([w.flatten('F') for w in bf]), g["best_x"], rtol=1e-5, atol=1e-8)
+
+
+def test_dgn_rng_stays_in_step_with_reference():
+    """After a 'cg' solve the global RNG is where the reference leaves it."""
+    g = load_golden("dgn_cg_L3")
+    dims, R = [int(d) for d in g["dims"]], int(g["R"])
+    np.random.seed(5)
+    orc.dGN(g["T"], split_x(g["init_x"], dims, R), R, orc.make_options(None))
+    want = np.random.rand()
+    np.random.seed(5)
+    tfx.dGN(g["T"], split_x(g["init_x"], dims, R), R, tfx.make_options(None))
+    assert np.random.rand() == want
+
+
+def test_dgn_until_first_dogleg():
+    g = load_golden("dgn_dogleg_L3")
+    dims, R = [int(d) for d in g["dims"]], int(g["R"])
+    np.random.seed(int(g["seed"]))
+    _, ss, er, im, gr, st = tfx.dGN(g["T"], split_x(g["init_x"], dims, R), R, _opts(g, tfx))
+    np.testing.assert_allclose(er[:7], g["errors"][:7], rtol=1e-8)
+    assert np.all(np.isfinite(er))
+
+
+@pytest.mark.parametrize("cluster", [1, 2, 4])
+def test_dgn_cluster_sizes_agree(cluster):
+    g = load_golden("dgn_static_L3")
+    dims, R = [int(d) for d in g["dims"]], int(g["R"])
+    o = _opts(g, tfx)
+    o.cluster = cluster
+    if cluster > R:
+        pytest.skip("cluster wider than rank")
+    bf, ss, er, im, gr, st = tfx.dGN(g["T"], split_x(g["init_x"], dims, R), R, o)
+    np.testing.assert_allclose(er, g["errors"], rtol=1e-6, atol=1e-12)
+
+
+def test_dgn_fp32_within_tolerance():
+    """FP32 engine: per-iteration errors within 1e-5 relative of the FP64 oracle
+    for the first iterations (the trajectories then drift apart by rounding)."""
+    g = load_golden("dgn_static_L3")
+    dims, R = [int(d) for d in g["dims"]], int(g["R"])
+    o = _opts(g, tfx)
+    o.precision = 'fp32'
+    bf, ss, er, im, gr, st = tfx.dGN(g["T"], split_x(g["init_x"], dims, R), R, o)
+    np.testing.assert_allclose(er[:8], g["errors"][:8], rtol=1e-4)
+    assert er[-1] < 1.5 * g["errors"][-1]
+
+
+def test_dgn_larger_core_vs_oracle():
+    """A 24x20x16 core at R=8 with cluster 4 against the oracle (cg_static)."""
+    rng = np.random.default_rng(7)
+    dims, R = (24, 20, 16), 8
+    W = [rng.standard_normal((d, R)) for d in dims]
+    T = orc.cpd2tens(W) + 1e-3 * rng.standard_normal(dims)
+    init = [w + 0.2 * rng.standard_normal(w.shape) for w in W]
+
+    class O:
+        inner_method = 'cg_static'
+        cg_maxiter = 12
+        maxiter = 25
+    _, ss0, er0, _, _, st0 = orc.dGN(T, [w.copy() for w in init], R, orc.make_options(O))
+    for c in (1, 4, 8):
+        o = tfx.make_options(O)
+        o.cluster = c
+        _, ss1, er1, _, _, st1 = tfx.dGN(T, [w.copy() for w in init], R, o)
+        assert st1 == st0
+        np.testing.assert_allclose(er1, er0, rtol=1e-7)
