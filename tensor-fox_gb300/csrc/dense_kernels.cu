@@ -1,0 +1,656 @@
+// Grid-level dense kernels of the compression (MLSVD) and full-tensor stages.
+//
+//   tfx_mode_gram      S_(l) S_(l)^T of a C-order tensor viewed as (P, D, Q)
+//                      (Compression.py:192-237: the Gram route replaces the
+//                      randomized SVD's streaming passes over the unfolding)
+//   tfx_gemm           strided batched C = alpha A B + beta C (TTM, subspace
+//                      products, decompression U_l W_l; TensorFox.py:573-574)
+//   tfx_orthonormalize CGS2 on the columns of a tall matrix (one CTA)
+//   tfx_sym_eig        cyclic parallel Jacobi eigensolver (one CTA)
+//   tfx_cp_residual    ||T - [[W]]||^2 fused (Conversion.py:117-141 +
+//                      Critical.py:14-22) -- the model tile is never stored
+//   tfx_tensor_norms   sum t^2 and sum |t| (TensorFox.py:503, GaussNewton.py:113)
+//   tfx_flip_signs     largest |entry| of every column made positive
+//                      (Compression.py:521-564)
+#include <math.h>
+
+#include <algorithm>
+
+#include "tfx_capi_internal.h"
+#include "tfx_common.cuh"
+
+namespace tfx {
+
+// ---------------------------------------------------------------------------
+// mode Gram: partial[s][i][j] = sum_{k in split s} A(i,k) A(j,k),
+// A(i, k) = S[p*D*Q + i*Q + q] with k = p*Q + q; upper tile pairs only.
+// ---------------------------------------------------------------------------
+template <class T, int TS>
+__global__ void __launch_bounds__(TFX_THREADS) k_mode_gram(const T* __restrict__ S, long long P, int D, long long Q,
+                                                           int ksplit, T* __restrict__ part) {
+  using TL = Tile<TS, TS>;
+  __shared__ T sA[TFX_BK * TL::LDA];
+  __shared__ T sB[TFX_BK * TL::LDB];
+  const int nt = (D + TL::BM - 1) / TL::BM;
+  // tile pair index -> (bi, bj), bi <= bj
+  int t = blockIdx.x, bi = 0;
+  while (t >= nt - bi) {
+    t -= nt - bi;
+    ++bi;
+  }
+  const int bj = bi + t;
+  const int i0 = bi * TL::BM, j0 = bj * TL::BN;
+  const long long K = P * Q;
+  const long long kb = K * blockIdx.y / ksplit, ke = K * (blockIdx.y + 1) / ksplit;
+  const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+  T acc[TS][TS];
+  tile_zero<T, TS, TS>(acc);
+  const bool kfast = Q > 1;
+  for (long long k0 = kb; k0 < ke; k0 += TFX_BK) {
+    const int kc = (int)min((long long)TFX_BK, ke - k0);
+    for (int e = tid; e < TFX_BK * TL::BM; e += TFX_THREADS) {
+      int kk, mm;
+      if (kfast) {
+        mm = e / TFX_BK;
+        kk = e - mm * TFX_BK;
+      } else {
+        kk = e / TL::BM;
+        mm = e - kk * TL::BM;
+      }
+      T va = T(0), vb = T(0);
+      if (kk < kc) {
+        const long long k = k0 + kk, p = k / Q, q = k - p * Q;
+        const long long base = p * (long long)D * Q + q;
+        if (i0 + mm < D) va = S[base + (long long)(i0 + mm) * Q];
+        if (j0 + mm < D) vb = S[base + (long long)(j0 + mm) * Q];
+      }
+      sA[kk * TL::LDA + mm] = va;
+      sB[kk * TL::LDB + mm] = vb;
+    }
+    __syncthreads();
+    tile_fma<T, TS, TS>(sA, sB, acc, kc);
+    __syncthreads();
+  }
+  T* out = part + (size_t)blockIdx.y * D * D;
+#pragma unroll
+  for (int u = 0; u < TS; ++u)
+#pragma unroll
+    for (int v = 0; v < TS; ++v) {
+      const int i = i0 + ty + 16 * u, j = j0 + tx + 16 * v;
+      if (i < D && j < D) out[(size_t)i * D + j] = acc[u][v];
+    }
+}
+
+template <class T, int BMt>
+__global__ void k_gram_reduce(const T* __restrict__ part, int D, int ksplit, T* __restrict__ G) {
+  const long long n = (long long)D * D;
+  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(e / D), j = (int)(e - (long long)i * D);
+    const long long src = (i / BMt <= j / BMt) ? e : (long long)j * D + i;
+    double s = 0.0;
+    for (int k = 0; k < ksplit; ++k) s += (double)part[(size_t)k * n + src];
+    G[e] = (T)s;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// strided batched GEMM: C[b](m,n) = alpha * sum_k A[b](m,k) B[b](k,n) + beta C
+// ---------------------------------------------------------------------------
+struct GemmArgs {
+  long long M, N, K, batch;
+  long long sAb, sAm, sAk, sBb, sBk, sBn, sCb, sCm, sCn;
+  double alpha, beta;
+};
+
+template <class T, int TS>
+__global__ void __launch_bounds__(TFX_THREADS) k_gemm(const T* __restrict__ A, const T* __restrict__ B, T* C,
+                                                      GemmArgs g) {
+  using TL = Tile<TS, TS>;
+  __shared__ T sA[TFX_BK * TL::LDA];
+  __shared__ T sB[TFX_BK * TL::LDB];
+  const long long tilesM = (g.M + TL::BM - 1) / TL::BM;
+  const long long m0 = (blockIdx.x % tilesM) * TL::BM;
+  const long long n0 = (blockIdx.x / tilesM) * TL::BN;
+  for (long long b = blockIdx.y; b < g.batch; b += gridDim.y) {
+    const T* Ab = A + b * g.sAb;
+    const T* Bb = B + b * g.sBb;
+    T* Cb = C + b * g.sCb;
+    const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+    T acc[TS][TS];
+    tile_zero<T, TS, TS>(acc);
+    const bool a_mfast = g.sAm == 1, b_nfast = g.sBn == 1;
+    for (long long k0 = 0; k0 < g.K; k0 += TFX_BK) {
+      const int kc = (int)min((long long)TFX_BK, g.K - k0);
+      for (int e = tid; e < TFX_BK * TL::BM; e += TFX_THREADS) {
+        int kk, mm;
+        if (a_mfast) {
+          kk = e / TL::BM;
+          mm = e - kk * TL::BM;
+        } else {
+          mm = e / TFX_BK;
+          kk = e - mm * TFX_BK;
+        }
+        sA[kk * TL::LDA + mm] = (kk < kc && m0 + mm < g.M) ? Ab[(m0 + mm) * g.sAm + (k0 + kk) * g.sAk] : T(0);
+      }
+      for (int e = tid; e < TFX_BK * TL::BN; e += TFX_THREADS) {
+        int kk, nn;
+        if (b_nfast) {
+          kk = e / TL::BN;
+          nn = e - kk * TL::BN;
+        } else {
+          nn = e / TFX_BK;
+          kk = e - nn * TFX_BK;
+        }
+        sB[kk * TL::LDB + nn] = (kk < kc && n0 + nn < g.N) ? Bb[(k0 + kk) * g.sBk + (n0 + nn) * g.sBn] : T(0);
+      }
+      __syncthreads();
+      tile_fma<T, TS, TS>(sA, sB, acc, kc);
+      __syncthreads();
+    }
+#pragma unroll
+    for (int u = 0; u < TS; ++u)
+#pragma unroll
+      for (int v = 0; v < TS; ++v) {
+        const long long m = m0 + ty + 16 * u, n = n0 + tx + 16 * v;
+        if (m < g.M && n < g.N) {
+          T* c = Cb + m * g.sCm + n * g.sCn;
+          const T r = (T)(g.alpha * (double)acc[u][v]);
+          *c = (g.beta == 0.0) ? r : (T)((double)r + g.beta * (double)*c);
+        }
+      }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// CGS2 orthonormalisation of the k columns of Y (D x k, column-major), in place.
+// ---------------------------------------------------------------------------
+template <class T>
+__global__ void __launch_bounds__(TFX_THREADS) k_orth(T* Y, int D, int k) {
+  // arithmetic in the working precision T: GB300's FP64 rate is a small
+  // fraction of its FP32 rate, and the second CGS pass restores orthogonality
+  __shared__ T coef[1024];
+  __shared__ double red[TFX_THREADS / 32];
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  for (int j = 0; j < k; ++j) {
+    T* yj = Y + (size_t)j * D;
+    for (int pass = 0; pass < 2; ++pass) {
+      for (int i = wid; i < j; i += TFX_THREADS / 32) {
+        const T* yi = Y + (size_t)i * D;
+        T s = T(0);
+        for (int r = lane; r < D; r += 32) s = fma(yi[r], yj[r], s);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        if (lane == 0) coef[i] = s;
+      }
+      __syncthreads();
+      for (int r = tid; r < D; r += TFX_THREADS) {
+        T v = yj[r];
+        for (int i = 0; i < j; ++i) v = fma(-coef[i], Y[(size_t)i * D + r], v);
+        yj[r] = v;
+      }
+      __syncthreads();
+    }
+    double s = 0.0;
+    for (int r = tid; r < D; r += TFX_THREADS) s += (double)yj[r] * (double)yj[r];
+    s = warp_sum(s);
+    if (lane == 0) red[wid] = s;
+    __syncthreads();
+    double nrm = 0.0;
+    for (int w = 0; w < TFX_THREADS / 32; ++w) nrm += red[w];
+    nrm = sqrt(nrm);
+    const T inv = (T)(nrm > 0.0 ? 1.0 / nrm : 0.0);
+    for (int r = tid; r < D; r += TFX_THREADS) yj[r] = yj[r] * inv;
+    __syncthreads();
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Symmetric eigensolver: cyclic Jacobi with the round-robin (tournament)
+// ordering, n/2 disjoint rotations per round applied in parallel.  Input A
+// (n x n, symmetric, row-major), output eigenvalues in descending order and
+// the matching eigenvectors as columns of V (n x n, column-major).
+// ---------------------------------------------------------------------------
+template <class T>
+__global__ void __launch_bounds__(TFX_THREADS) k_jacobi(const T* __restrict__ Ain, int n, T* __restrict__ evals,
+                                                        T* __restrict__ V, int max_sweeps, int* __restrict__ sweeps_out) {
+  extern __shared__ __align__(16) char smem[];
+  const int m = (n + 1) & ~1;  // even size (a zero row/column pads odd n)
+  T* A = (T*)smem;             // m x m
+  T* Vs = A + (size_t)m * m;   // m x m, column p at Vs[p*m]
+  T* cs = Vs + (size_t)m * m;  // c[m/2], s[m/2]
+  int* pr = (int*)(cs + m);    // pairs
+  double* red = (double*)(pr + m + 2);
+  const int tid = threadIdx.x;
+  for (int e = tid; e < m * m; e += TFX_THREADS) {
+    const int i = e / m, j = e - i * m;
+    // symmetrised on load: Rayleigh-Ritz matrices arrive symmetric only up to rounding
+    A[e] = (i < n && j < n) ? (T)(0.5 * ((double)Ain[i * n + j] + (double)Ain[j * n + i])) : T(0);
+    Vs[e] = (i == j) ? T(1) : T(0);
+  }
+  __syncthreads();
+  const double eps = sizeof(T) == 8 ? 1e-14 : 2e-6;
+  int sweep = 0;
+  for (sweep = 0; sweep < max_sweeps; ++sweep) {
+    // convergence: off-diagonal mass vs total
+    double off = 0.0, tot = 0.0;
+    for (int e = tid; e < m * m; e += TFX_THREADS) {
+      const double v = (double)A[e];
+      tot += v * v;
+      if (e / m != e % m) off += v * v;
+    }
+    off = warp_sum(off);
+    tot = warp_sum(tot);
+    if ((tid & 31) == 0) {
+      red[2 * (tid >> 5)] = off;
+      red[2 * (tid >> 5) + 1] = tot;
+    }
+    __syncthreads();
+    double so = 0.0, st = 0.0;
+    for (int w = 0; w < TFX_THREADS / 32; ++w) {
+      so += red[2 * w];
+      st += red[2 * w + 1];
+    }
+    __syncthreads();
+    if (so <= eps * eps * st || st == 0.0) break;
+    for (int round = 0; round < m - 1; ++round) {
+      // pairs of this round
+      for (int kk = tid; kk < m / 2; kk += TFX_THREADS) {
+        const int a = (kk == 0) ? m - 1 : (kk + round) % (m - 1);
+        const int b = (m - 1 - kk + round) % (m - 1);
+        const int p = a < b ? a : b, q = a < b ? b : a;
+        pr[2 * kk] = p;
+        pr[2 * kk + 1] = q;
+        const double apq = (double)A[p * m + q];
+        double c = 1.0, s = 0.0;
+        if (fabs(apq) > 1e-300) {
+          const double tau = ((double)A[q * m + q] - (double)A[p * m + p]) / (2.0 * apq);
+          const double t = (tau >= 0.0 ? 1.0 : -1.0) / (fabs(tau) + sqrt(1.0 + tau * tau));
+          c = 1.0 / sqrt(1.0 + t * t);
+          s = t * c;
+        }
+        cs[kk] = (T)c;
+        cs[m / 2 + kk] = (T)s;
+      }
+      __syncthreads();
+      // columns: A <- A J, V <- V J
+      for (int e = tid; e < (m / 2) * m; e += TFX_THREADS) {
+        const int kk = e / m, i = e - kk * m;
+        const int p = pr[2 * kk], q = pr[2 * kk + 1];
+        const T c = cs[kk], s = cs[m / 2 + kk];
+        const T aip = A[i * m + p], aiq = A[i * m + q];
+        A[i * m + p] = c * aip - s * aiq;
+        A[i * m + q] = s * aip + c * aiq;
+        const T vip = Vs[p * m + i], viq = Vs[q * m + i];
+        Vs[p * m + i] = c * vip - s * viq;
+        Vs[q * m + i] = s * vip + c * viq;
+      }
+      __syncthreads();
+      // rows: A <- J^T A
+      for (int e = tid; e < (m / 2) * m; e += TFX_THREADS) {
+        const int kk = e / m, j = e - kk * m;
+        const int p = pr[2 * kk], q = pr[2 * kk + 1];
+        const T c = cs[kk], s = cs[m / 2 + kk];
+        const T apj = A[p * m + j], aqj = A[q * m + j];
+        A[p * m + j] = c * apj - s * aqj;
+        A[q * m + j] = s * apj + c * aqj;
+      }
+      __syncthreads();
+    }
+  }
+  // sort eigenvalues (descending) with their vectors: rank by counting
+  for (int i = tid; i < n; i += TFX_THREADS) {
+    const T li = A[i * m + i];
+    int rank = 0;
+    for (int j = 0; j < n; ++j) {
+      const T lj = A[j * m + j];
+      if (lj > li || (lj == li && j < i)) ++rank;
+    }
+    evals[rank] = li;
+    for (int r = 0; r < n; ++r) V[(size_t)rank * n + r] = Vs[i * m + r];
+  }
+  if (tid == 0 && sweeps_out) *sweeps_out = sweep;
+}
+
+// ---------------------------------------------------------------------------
+// Column signs: the entry of largest magnitude (first one on ties) of every
+// column of U (D x n, column-major) becomes positive.
+// ---------------------------------------------------------------------------
+template <class T>
+__global__ void k_flip_signs(T* U, int D, int n) {
+  const int lane = threadIdx.x & 31;
+  const int col = blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5);
+  if (col >= n) return;
+  T* u = U + (size_t)col * D;
+  double best = -1.0;
+  int bi = 0;
+  for (int r = lane; r < D; r += 32) {
+    const double a = fabs((double)u[r]);
+    if (a > best) {
+      best = a;
+      bi = r;
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    const double ob = __shfl_xor_sync(0xffffffffu, best, o);
+    const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+    if (ob > best || (ob == best && oi < bi)) {
+      best = ob;
+      bi = oi;
+    }
+  }
+  const bool neg = u[bi] < T(0);
+  if (neg)
+    for (int r = lane; r < D; r += 32) u[r] = -u[r];
+}
+
+// ---------------------------------------------------------------------------
+// ||T - [[W]]||^2, T C-order (d0, Q0) with Q0 = prod_{l>0} d_l; W in the flat
+// column-major factor layout.  Partial sums per block, then one fixed-order sum.
+// ---------------------------------------------------------------------------
+struct CpShape {
+  int L, R;
+  int d[TFX_MAX_ORDER];
+  int off[TFX_MAX_ORDER];
+};
+
+template <class T, int TS>
+__global__ void __launch_bounds__(TFX_THREADS) k_cp_residual(const T* __restrict__ Tt, const T* __restrict__ W,
+                                                             CpShape sh, double* __restrict__ partial) {
+  using TL = Tile<TS, TS>;
+  __shared__ T sA[TFX_BK * TL::LDA];
+  __shared__ T sB[TFX_BK * TL::LDB];
+  __shared__ int sIdx[TL::BN * TFX_MAX_ORDER];
+  __shared__ double red[TFX_THREADS / 32];
+  const int L = sh.L, R = sh.R, d0 = sh.d[0];
+  long long Q0 = 1;
+  for (int l = 1; l < L; ++l) Q0 *= sh.d[l];
+  const int tm_ = (d0 + TL::BM - 1) / TL::BM;
+  const long long ntiles = (long long)tm_ * ((Q0 + TL::BN - 1) / TL::BN);
+  const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+  double part = 0.0;
+  for (long long t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const int m0 = (int)(t % tm_) * TL::BM;
+    const long long q0 = (t / tm_) * TL::BN;
+    if (tid < TL::BN) {
+      long long q = q0 + tid;
+      if (q < Q0)
+        for (int l = L - 1; l >= 1; --l) {
+          sIdx[tid * TFX_MAX_ORDER + l] = (int)(q % sh.d[l]);
+          q /= sh.d[l];
+        }
+    }
+    __syncthreads();
+    T acc[TS][TS];
+    tile_zero<T, TS, TS>(acc);
+    for (int k0 = 0; k0 < R; k0 += TFX_BK) {
+      const int kc = min(TFX_BK, R - k0);
+      for (int e = tid; e < TFX_BK * TL::BM; e += TFX_THREADS) {
+        const int kk = e / TL::BM, mm = e - kk * TL::BM;
+        sA[kk * TL::LDA + mm] = (kk < kc && m0 + mm < d0) ? W[sh.off[0] + (k0 + kk) * d0 + m0 + mm] : T(0);
+      }
+      for (int e = tid; e < TFX_BK * TL::BN; e += TFX_THREADS) {
+        const int kk = e / TL::BN, nn = e - kk * TL::BN;
+        T v = T(0);
+        if (kk < kc && q0 + nn < Q0) {
+          v = T(1);
+          for (int l = L - 1; l >= 1; --l) v *= W[sh.off[l] + (k0 + kk) * sh.d[l] + sIdx[nn * TFX_MAX_ORDER + l]];
+        }
+        sB[kk * TL::LDB + nn] = v;
+      }
+      __syncthreads();
+      tile_fma<T, TS, TS>(sA, sB, acc, kc);
+      __syncthreads();
+    }
+    T ps = T(0);
+#pragma unroll
+    for (int u = 0; u < TS; ++u)
+#pragma unroll
+      for (int v = 0; v < TS; ++v) {
+        const int m = m0 + ty + 16 * u;
+        const long long q = q0 + tx + 16 * v;
+        if (m < d0 && q < Q0) {
+          const T df = Tt[(long long)m * Q0 + q] - acc[u][v];
+          ps = fma(df, df, ps);
+        }
+      }
+    part += (double)ps;
+  }
+  part = warp_sum(part);
+  if ((tid & 31) == 0) red[tid >> 5] = part;
+  __syncthreads();
+  if (tid == 0) {
+    double s = 0.0;
+    for (int w = 0; w < TFX_THREADS / 32; ++w) s += red[w];
+    partial[blockIdx.x] = s;
+  }
+}
+
+template <class T>
+__global__ void k_tensor_norms(const T* __restrict__ Tt, long long N, double* __restrict__ partial) {
+  __shared__ double red[2][TFX_THREADS / 32];
+  double s2 = 0.0, s1 = 0.0;
+  for (long long e = (long long)blockIdx.x * TFX_THREADS + threadIdx.x; e < N; e += (long long)gridDim.x * TFX_THREADS) {
+    const double t = (double)Tt[e];
+    s2 += t * t;
+    s1 += fabs(t);
+  }
+  s2 = warp_sum(s2);
+  s1 = warp_sum(s1);
+  if ((threadIdx.x & 31) == 0) {
+    red[0][threadIdx.x >> 5] = s2;
+    red[1][threadIdx.x >> 5] = s1;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double a = 0.0, b = 0.0;
+    for (int w = 0; w < TFX_THREADS / 32; ++w) {
+      a += red[0][w];
+      b += red[1][w];
+    }
+    partial[2 * blockIdx.x] = a;
+    partial[2 * blockIdx.x + 1] = b;
+  }
+}
+
+// fixed-order sum of `n` partials with stride `stride` into out[0..stride)
+__global__ void k_sum_partials(const double* __restrict__ partial, int n, int stride, double* __restrict__ out) {
+  if (threadIdx.x < stride) {
+    double s = 0.0;
+    for (int i = 0; i < n; ++i) s += partial[(size_t)i * stride + threadIdx.x];
+    out[threadIdx.x] = s;
+  }
+}
+
+}  // namespace tfx
+
+// ============================================================================
+// C ABI
+// ============================================================================
+using namespace tfx;
+
+static int g_num_sms = 0;
+static int num_sms() {
+  if (g_num_sms == 0) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev);
+    if (g_num_sms <= 0) g_num_sms = 1;
+  }
+  return g_num_sms;
+}
+
+static int check_launch(const char* where) {
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return tfx_set_cuda_error(e, where);
+  tfx_count_launch(1);
+  return TFX_STATUS_OK;
+}
+
+extern "C" size_t tfx_mode_gram_scratch_bytes(int dtype, long long P, int D, long long Q) {
+  const int BM = 64;
+  const int nt = (D + BM - 1) / BM;
+  const long long tiles = (long long)nt * (nt + 1) / 2;
+  const long long K = P * Q;
+  long long ks = (4LL * num_sms() + tiles - 1) / tiles;
+  const long long kmax = (K + 255) / 256;
+  if (ks > kmax) ks = kmax;
+  if (ks < 1) ks = 1;
+  if (ks > 64) ks = 64;
+  return (size_t)ks * D * D * (dtype == TFX_F64 ? 8 : 4);
+}
+
+extern "C" int tfx_mode_gram(int dtype, const void* S, long long P, int D, long long Q, void* G, void* scratch,
+                             size_t scratch_bytes, void* stream) {
+  if (!S || !G || !scratch || P < 1 || D < 1 || Q < 1) return tfx_set_error(TFX_STATUS_ERR_ARG, "mode_gram args");
+  const size_t es = dtype == TFX_F64 ? 8 : 4;
+  const int BM = 64;
+  const int nt = (D + BM - 1) / BM;
+  const long long tiles = (long long)nt * (nt + 1) / 2;
+  int ks = (int)(scratch_bytes / ((size_t)D * D * es));
+  const size_t want = tfx_mode_gram_scratch_bytes(dtype, P, D, Q) / ((size_t)D * D * es);
+  if ((size_t)ks > want) ks = (int)want;
+  if (ks < 1) return tfx_set_error(TFX_STATUS_ERR_ARG, "mode_gram scratch too small");
+  cudaStream_t st = (cudaStream_t)stream;
+  dim3 grid((unsigned)tiles, (unsigned)ks);
+  const long long n = (long long)D * D;
+  const int rb = (int)std::min<long long>((n + 255) / 256, 4LL * num_sms());
+  if (dtype == TFX_F32) {
+    k_mode_gram<float, 4><<<grid, TFX_THREADS, 0, st>>>((const float*)S, P, D, Q, ks, (float*)scratch);
+    int s = check_launch("mode_gram");
+    if (s) return s;
+    k_gram_reduce<float, 64><<<rb, 256, 0, st>>>((const float*)scratch, D, ks, (float*)G);
+  } else {
+    k_mode_gram<double, 4><<<grid, TFX_THREADS, 0, st>>>((const double*)S, P, D, Q, ks, (double*)scratch);
+    int s = check_launch("mode_gram");
+    if (s) return s;
+    k_gram_reduce<double, 64><<<rb, 256, 0, st>>>((const double*)scratch, D, ks, (double*)G);
+  }
+  return check_launch("gram_reduce");
+}
+
+extern "C" int tfx_gemm(int dtype, const void* A, const void* B, void* C, long long M, long long N, long long K,
+                        long long batch, const long long* strides /* sAb sAm sAk sBb sBk sBn sCb sCm sCn */,
+                        double alpha, double beta, void* stream) {
+  if (!A || !B || !C || !strides || M < 1 || N < 1 || K < 0 || batch < 1)
+    return tfx_set_error(TFX_STATUS_ERR_ARG, "gemm args");
+  GemmArgs g;
+  g.M = M;
+  g.N = N;
+  g.K = K;
+  g.batch = batch;
+  g.sAb = strides[0];
+  g.sAm = strides[1];
+  g.sAk = strides[2];
+  g.sBb = strides[3];
+  g.sBk = strides[4];
+  g.sBn = strides[5];
+  g.sCb = strides[6];
+  g.sCm = strides[7];
+  g.sCn = strides[8];
+  g.alpha = alpha;
+  g.beta = beta;
+  cudaStream_t st = (cudaStream_t)stream;
+  const long long tiles = ((M + 63) / 64) * ((N + 63) / 64);
+  if (tiles > 0x7fffffffLL) return tfx_set_error(TFX_STATUS_ERR_ARG, "gemm too large");
+  const long long by = std::min<long long>(batch, 65535);
+  dim3 grid((unsigned)tiles, (unsigned)by);
+  if (dtype == TFX_F32)
+    k_gemm<float, 4><<<grid, TFX_THREADS, 0, st>>>((const float*)A, (const float*)B, (float*)C, g);
+  else
+    k_gemm<double, 4><<<grid, TFX_THREADS, 0, st>>>((const double*)A, (const double*)B, (double*)C, g);
+  return check_launch("gemm");
+}
+
+extern "C" int tfx_orthonormalize(int dtype, void* Y, int D, int k, void* stream) {
+  if (!Y || D < 1 || k < 1 || k > 1024) return tfx_set_error(TFX_STATUS_ERR_ARG, "orthonormalize args");
+  cudaStream_t st = (cudaStream_t)stream;
+  if (dtype == TFX_F32)
+    k_orth<float><<<1, TFX_THREADS, 0, st>>>((float*)Y, D, k);
+  else
+    k_orth<double><<<1, TFX_THREADS, 0, st>>>((double*)Y, D, k);
+  return check_launch("orthonormalize");
+}
+
+extern "C" size_t tfx_sym_eig_smem_bytes(int dtype, int n) {
+  const int m = (n + 1) & ~1;
+  const size_t es = dtype == TFX_F64 ? 8 : 4;
+  size_t b = 2 * (size_t)m * m * es + (size_t)m * es + (size_t)(m + 2) * sizeof(int);
+  b = (b + 15) & ~(size_t)15;
+  return b + 2 * (TFX_THREADS / 32) * sizeof(double);
+}
+
+extern "C" int tfx_sym_eig(int dtype, const void* A, int n, void* evals, void* V, int max_sweeps, int* sweeps,
+                           void* stream) {
+  if (!A || !evals || !V || n < 1) return tfx_set_error(TFX_STATUS_ERR_ARG, "sym_eig args");
+  const size_t sm = tfx_sym_eig_smem_bytes(dtype, n);
+  if (sm > 220 * 1024) return tfx_set_error(TFX_STATUS_ERR_UNSUPPORTED, "sym_eig matrix too large");
+  cudaStream_t st = (cudaStream_t)stream;
+  cudaError_t e;
+  if (dtype == TFX_F32) {
+    e = cudaFuncSetAttribute(k_jacobi<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    if (e != cudaSuccess) return tfx_set_cuda_error(e, "sym_eig attr");
+    k_jacobi<float><<<1, TFX_THREADS, sm, st>>>((const float*)A, n, (float*)evals, (float*)V, max_sweeps, sweeps);
+  } else {
+    e = cudaFuncSetAttribute(k_jacobi<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    if (e != cudaSuccess) return tfx_set_cuda_error(e, "sym_eig attr");
+    k_jacobi<double><<<1, TFX_THREADS, sm, st>>>((const double*)A, n, (double*)evals, (double*)V, max_sweeps, sweeps);
+  }
+  return check_launch("sym_eig");
+}
+
+extern "C" int tfx_flip_signs(int dtype, void* U, int D, int n, void* stream) {
+  if (!U || D < 1 || n < 1) return tfx_set_error(TFX_STATUS_ERR_ARG, "flip_signs args");
+  cudaStream_t st = (cudaStream_t)stream;
+  const int blocks = (n + 7) / 8;
+  if (dtype == TFX_F32)
+    k_flip_signs<float><<<blocks, 256, 0, st>>>((float*)U, D, n);
+  else
+    k_flip_signs<double><<<blocks, 256, 0, st>>>((double*)U, D, n);
+  return check_launch("flip_signs");
+}
+
+extern "C" size_t tfx_cp_residual_scratch_bytes(void) { return (size_t)8 * (8 * 1024 + 8); }
+
+extern "C" int tfx_cp_residual(int dtype, const void* T, int L, const int* dims, int R, const void* W, double* out,
+                               void* scratch, void* stream) {
+  if (!T || !dims || !W || !out || !scratch || L < 2 || L > TFX_MAX_ORDER || R < 1)
+    return tfx_set_error(TFX_STATUS_ERR_ARG, "cp_residual args");
+  CpShape sh;
+  sh.L = L;
+  sh.R = R;
+  int s = 0;
+  long long Q0 = 1;
+  for (int l = 0; l < L; ++l) {
+    sh.d[l] = dims[l];
+    sh.off[l] = R * s;
+    s += dims[l];
+    if (l) Q0 *= dims[l];
+  }
+  const long long tiles = ((dims[0] + 63) / 64) * ((Q0 + 63) / 64);
+  const int blocks = (int)std::max<long long>(1, std::min<long long>(tiles, 8LL * num_sms()));
+  cudaStream_t st = (cudaStream_t)stream;
+  double* partial = (double*)scratch;
+  if (dtype == TFX_F32)
+    k_cp_residual<float, 4><<<blocks, TFX_THREADS, 0, st>>>((const float*)T, (const float*)W, sh, partial);
+  else
+    k_cp_residual<double, 4><<<blocks, TFX_THREADS, 0, st>>>((const double*)T, (const double*)W, sh, partial);
+  int r = check_launch("cp_residual");
+  if (r) return r;
+  k_sum_partials<<<1, 32, 0, st>>>(partial, blocks, 1, out);
+  return check_launch("sum_partials");
+}
+
+extern "C" int tfx_tensor_norms(int dtype, const void* T, long long N, double* out2, void* scratch, void* stream) {
+  if (!T || !out2 || !scratch || N < 1) return tfx_set_error(TFX_STATUS_ERR_ARG, "tensor_norms args");
+  const int blocks = (int)std::max<long long>(1, std::min<long long>((N + 255) / 256, 4LL * num_sms()));
+  cudaStream_t st = (cudaStream_t)stream;
+  double* partial = (double*)scratch;
+  if (dtype == TFX_F32)
+    k_tensor_norms<float><<<blocks, TFX_THREADS, 0, st>>>((const float*)T, N, partial);
+  else
+    k_tensor_norms<double><<<blocks, TFX_THREADS, 0, st>>>((const double*)T, N, partial);
+  int r = check_launch("tensor_norms");
+  if (r) return r;
+  k_sum_partials<<<1, 32, 0, st>>>(partial, blocks, 2, out2);
+  return check_launch("sum_partials");
+}

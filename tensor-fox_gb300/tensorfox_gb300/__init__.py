@@ -8,3 +8,5 @@ __version__ = "1.2.1+gb300"
 
 from .options import make_options, Options  # noqa: F401
 from .gauss_newton import dGN  # noqa: F401
+from .api import cpd, tricpd, consistency, Output  # noqa: F401,E402
+from .compression import mlsvd, clean_compression  # noqa: F401,E402

@@ -65,18 +65,40 @@ def _declare(lib):
     lib.tfx_dgn_solve.argtypes = [c_int, POINTER(DgnProblem), c_void_p, c_int, POINTER(DgnOptions), c_int,
                                   c_void_p]
     for name, args in _EXTRA_SIGNATURES.items():
-        fn = getattr(lib, name, None)
-        if fn is not None:
-            fn.restype = c_int
-            fn.argtypes = args
+        fn = getattr(lib, name)
+        fn.restype = c_int
+        fn.argtypes = args
+    for name, args in _SIZE_FUNCS.items():
+        fn = getattr(lib, name)
+        fn.restype = c_size_t
+        fn.argtypes = args
+
+
+def call(name, *args):
+    """Calls an int-status entry point and raises TfxError on failure."""
+    check(getattr(load(), name)(*args))
 
 
 # Remaining entry points: (name -> argtypes); all return an int status.
-_EXTRA_SIGNATURES = {}
-
-
-def register(name, *args):
-    _EXTRA_SIGNATURES[name] = list(args)
+_P = c_void_p
+_I = c_int
+_LL = c_longlong
+_D = c_double
+_SZ = c_size_t
+_EXTRA_SIGNATURES = {
+    "tfx_mode_gram": [_I, _P, _LL, _I, _LL, _P, _P, _SZ, _P],
+    "tfx_gemm": [_I, _P, _P, _P, _LL, _LL, _LL, _LL, POINTER(c_longlong), _D, _D, _P],
+    "tfx_orthonormalize": [_I, _P, _I, _I, _P],
+    "tfx_sym_eig": [_I, _P, _I, _P, _P, _I, _P, _P],
+    "tfx_flip_signs": [_I, _P, _I, _I, _P],
+    "tfx_cp_residual": [_I, _P, _I, POINTER(c_int), _I, _P, _P, _P, _P],
+    "tfx_tensor_norms": [_I, _P, _LL, _P, _P, _P],
+}
+_SIZE_FUNCS = {
+    "tfx_mode_gram_scratch_bytes": [_I, _LL, _I, _LL],
+    "tfx_sym_eig_smem_bytes": [_I, _I],
+    "tfx_cp_residual_scratch_bytes": [],
+}
 
 
 def check(status):

@@ -1,0 +1,209 @@
+"""User API: ``cpd`` / ``tricpd`` with the reference's semantics (TensorFox.py:69-655).
+
+``cpd(T, R, options)`` returns ``(factors, output)`` exactly like Tensor Fox:
+factors are NumPy float64 ``(d_l, R)`` arrays in the caller's mode order and
+``output`` carries num_steps, rel_error, accuracy, step_sizes, errors, improv,
+gradients, stop and options.  Invalid input raises ``SystemExit`` with the
+reference's messages (Auxiliar.py:24-78), without its one-second pause.
+"""
+import sys
+
+import numpy as np
+import torch
+
+from . import _dev, kernels
+from .compression import mlsvd_device
+from .gauss_newton import _Batch, advance_rng, auto_cluster
+from .options import make_options
+
+
+class Output:
+    """Result record of ``cpd`` (Auxiliar.py:161-218)."""
+
+    def stop_msg(self):
+        msgs = {0: '0 - Relative error is small enough.', 1: '1 - Steps are small enough.',
+                2: '2 - Improvement in the relative error is small enough.', 3: '3 - Gradient is small enough.',
+                4: '4 - Average error increased.', 5: '5 - Limit of iterations was reached.',
+                6: '6 - dGN diverged.', 7: '7 - Average improvement is too small compared to the average error.',
+                8: '8 - No refinement was performed.'}
+        print()
+        print('Main stop:')
+        print(msgs.get(self.stop[0], str(self.stop[0])))
+        print()
+        print('Refinement stop:')
+        print(msgs.get(self.stop[1], str(self.stop[1])))
+        return ''
+
+
+def consistency(R, dims, options):
+    """Input checks of Auxiliar.py:24-78 (same messages, no sleep)."""
+    L = len(dims)
+    if L > 12:
+        sys.exit('Tensor Fox does not work with tensors of order higher than 12.')
+    for l in range(L):
+        if dims[l] == 1:
+            sys.exit('At least one dimension is equal to 1. This situation not supported by Tensor Fox.')
+    if (type(R) != int) or (R < 1):
+        sys.exit('Rank must be a positive integer.')
+    if L == 3:
+        m, n, p = int(dims[0]), int(dims[1]), int(dims[2])
+        if R > min(m * n, m * p, n * p):
+            sys.exit('Rank must satisfy 1 <= rank <= min(m*n, m*p, n*p) = ' + str(min(m * n, m * p, n * p)) + '.')
+    if L > 3 and R == 1:
+        sys.exit('Rank must be greater than 1 for tensor with order greater than 3.')
+    if options.symm:
+        for i in range(L):
+            for j in range(L):
+                if dims[i] != dims[j]:
+                    sys.exit('Symmetric tensors must have equal dimensions.')
+    if options.method != 'dGN' and options.method != 'als' and options.method != 'ttcpd':
+        sys.exit("Wrong method name. Must be 'dGN', 'als' or 'ttcpd'.")
+
+
+def sort_dims(shape):
+    """Mode permutation into decreasing sizes (Auxiliar.py:93-115)."""
+    return np.argsort(-np.array(shape))
+
+
+def unsort_dims(factors, ordering):
+    out = [None] * len(factors)
+    for l in range(len(factors)):
+        out[ordering[l]] = factors[l]
+    return out
+
+
+def _precision(T, options):
+    p = options.precision
+    if p in ('fp64', 'fp32'):
+        return p
+    if isinstance(T, torch.Tensor):
+        return 'fp64' if T.dtype == torch.float64 else 'fp32'
+    if isinstance(T, list):
+        return 'fp64'
+    return 'fp64' if np.asarray(T).dtype == np.float64 else 'fp32'
+
+
+def starting_point_random(dims, R, options):
+    """'random' initialisation in the compressed space (Initialization.py:61-94)."""
+    f = [np.random.randn(dims[l], R) for l in range(len(dims))]
+    for l in range(len(dims)):             # clean_zeros (Initialization.py:361-386)
+        W = f[l]
+        for i, r in zip(*np.nonzero(W == 0.0)):
+            W[i, r] = 1e-4 * np.random.randn() * np.linalg.norm(W)
+    for r in range(R):                      # equalize (Conversion.py:361-387)
+        nr = np.array([np.linalg.norm(f[l][:, r]) for l in range(len(dims))])
+        if np.prod(nr) != 0.0:
+            g = np.prod(nr) ** (1 / len(dims))
+            for l in range(len(dims)):
+                f[l][:, r] = (g / nr[l]) * f[l][:, r]
+    if options.symm:
+        s = f[0]
+        for l in range(1, len(dims)):
+            s = s + f[l]
+        f = [s / len(dims)] * len(dims)
+    if options.factors_norm > 0:
+        f = [options.factors_norm * (1 / np.linalg.norm(W)) * W for W in f]
+    return f
+
+
+def _flat_dev(factors, dtype, device):
+    return torch.from_numpy(_dev.flat_factors(factors)).to(device=device, dtype=dtype)
+
+
+def _run_dgn(Td, x0, R, options, prec):
+    b = _Batch([Td], [x0], [R], options, prec)
+    c = options.cluster or auto_cluster(tuple(Td.shape), R)
+    b.launch(c)
+    res = b.result[0].cpu().numpy()
+    stats = b.stats[0].cpu().numpy()
+    n = int(res[1])
+    advance_rng(options, n)
+    m = options.maxiter
+    return (b.best[0], stats[m:m + n].copy(), stats[:n].copy(), stats[2 * m:2 * m + n].copy(),
+            stats[3 * m:3 * m + n].copy(), int(res[0]))
+
+
+def _decompress(Uts, best_flat, core_dims, R):
+    """factors_l = U_l W_l on the device (TensorFox.py:573-574); returns the flat layout."""
+    outs, s = [], 0
+    for l, Ut in enumerate(Uts):
+        n = core_dims[l]
+        WcT = best_flat[s:s + n * R].view(R, n)   # column-major (n x R) core factor
+        outs.append(kernels.matmul(WcT, Ut).reshape(-1))   # (R, d) = column-major (d x R)
+        s += n * R
+    return torch.cat(outs)
+
+
+def tricpd(T, R, options):
+    """Compression, starting point, dGN, decompression, refinement, final error."""
+    o = options
+    if isinstance(T, list):
+        from .sparse import tricpd_sparse
+        return tricpd_sparse(T, R, o)
+    if o.method != 'dGN':
+        raise NotImplementedError("method %r is outside the damped Gauss-Newton path" % (o.method,))
+    prec = _precision(T, o)
+    dt = _dev.torch_dtype(prec)
+    shape = tuple(int(d) for d in T.shape)
+    L = len(shape)
+    ordering = sort_dims(shape)
+    if isinstance(T, torch.Tensor):
+        Td = T.to(device=_dev.device(), dtype=dt).permute(*[int(i) for i in ordering]).contiguous()
+    else:
+        Td = _dev.to_device(np.transpose(np.asarray(T), ordering), dt)
+    dims = tuple(int(d) for d in Td.shape)
+    nrm = kernels.tensor_norms(Td).cpu().numpy()
+    Tsize = float(np.sqrt(nrm[0]))
+    S, Uts, sigmas, core = mlsvd_device(Td, R, o)
+    if o.symm:
+        Rm = min(core)
+        S = S[tuple(slice(Rm) for _ in range(L))].contiguous()
+        Uts = [u[:Rm].contiguous() for u in Uts]
+        core = [Rm] * L
+    if isinstance(o.initialization, list):
+        init = []
+        for l in range(L):
+            W = torch.from_numpy(np.asarray(o.initialization[ordering[l]], dtype=np.float64)).to(Td.device, dt)
+            init.append(kernels.matmul(Uts[l], W).double().cpu().numpy())
+    elif o.initialization == 'random':
+        init = starting_point_random(core, R, o)
+    else:
+        raise NotImplementedError("initialization %r is outside the dGN path" % (o.initialization,))
+    x0 = _flat_dev(init, dt, Td.device)
+    best, ss, er, im, gr, st = _run_dgn(S, x0, R, o, prec)
+    Wf = _decompress(Uts, best, core, R)
+    if o.refine:
+        Wf, ss2, er2, im2, gr2, st2 = _run_dgn(Td, Wf, R, o, prec)
+    else:
+        ss2, er2, im2, gr2, st2 = np.array([0]), np.array([0]), np.array([0]), np.array([0]), 8
+    if o.refine:
+        rel_error = float(er2[-1])
+    else:
+        rel_error = float(np.sqrt(kernels.cp_residual_sq(Td, dims, Wf, R).cpu().numpy()[0])) / Tsize
+    factors = _dev.unflat(Wf.double().cpu().numpy(), dims, R)
+    factors = unsort_dims(factors, ordering)
+    out = Output()
+    out.num_steps = len(ss) + (len(ss2) if o.refine else 0)
+    out.rel_error = rel_error
+    out.accuracy = max(0, 100 * (1 - rel_error))
+    out.step_sizes = [ss, ss2]
+    out.errors = [er, er2]
+    out.improv = [im, im2]
+    out.gradients = [gr, gr2]
+    out.stop = [st, st2]
+    out.options = o
+    return factors, out
+
+
+def cpd(T, R, options=False):
+    """Drop-in for TensorFox.cpd (TensorFox.py:69-255), method 'dGN'."""
+    _dev.require_cuda()
+    if isinstance(T, list):
+        dims_orig = T[2]
+    else:
+        dims_orig = T.shape
+    o = make_options(options)
+    consistency(R, dims_orig, o)
+    if o.method in ('dGN', 'als'):
+        return tricpd(T, R, o)
+    raise NotImplementedError("method %r is outside the damped Gauss-Newton path" % (o.method,))

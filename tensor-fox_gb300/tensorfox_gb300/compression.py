@@ -1,0 +1,148 @@
+"""Truncated MLSVD on the device (Compression.py:48-189).
+
+Per mode, the reference runs a randomized SVD that streams the unfolding
+several times.  Here the unfolding's Gram matrix ``S_(l) S_(l)^T`` is formed in
+one pass over the tensor (``tfx_mode_gram``); its leading eigenvectors come from
+a Rayleigh-Ritz step on ``span(G^3 Omega)`` -- the same Krylov depth as the
+reference's two power iterations -- solved by an in-project Jacobi eigensolver,
+or by Jacobi on ``G`` itself when the mode is small.  ``Omega`` is the very
+Gaussian block the reference draws from NumPy's global RNG, so seeded runs keep
+the RNG in step with the reference (the starting point drawn next is identical).
+
+Singular vectors get the reference's sign convention (largest |entry| of every
+column positive) and the same energy truncation (``clean_compression``).
+"""
+import numpy as np
+import torch
+
+from . import _dev, kernels
+from .options import make_options
+
+
+def _draw_omega(rows, n_random):
+    """The reference's range-finder draw (Compression.py:382), as float64."""
+    return np.random.normal(size=(rows, n_random))
+
+
+def clean_compression(sigma, tol_mlsvd, L):
+    """Smallest i with sum(sigma[i:]^2)/sum(sigma^2) < tol/L (Compression.py:261-301)."""
+    eps = tol_mlsvd / L
+    tot = np.sum(sigma ** 2)
+    for i in range(1, len(sigma)):
+        if np.sum(sigma[i:] ** 2) / tot < eps:
+            return i
+    return len(sigma)
+
+
+def top_eig(G, n, omega=None):
+    """Leading ``n`` eigenpairs of the symmetric D x D device matrix ``G``.
+
+    Returns ``(Ut, lam)``: Ut is (n, D) (rows = eigenvectors, signs fixed),
+    lam a float64 NumPy array (descending).
+    """
+    D = G.shape[0]
+    n = min(n, D)
+    direct = 64 if G.dtype == torch.float32 else 32
+    k = min(n + 10, D)
+    if D <= direct or k >= D:
+        ev, V = kernels.sym_eig(G)
+        Ut = V[:n].contiguous()
+        lam = ev[:n]
+    else:
+        if omega is not None and omega.shape[0] == D:
+            Yt = torch.from_numpy(np.ascontiguousarray(omega[:, :k].T)).to(device=G.device, dtype=G.dtype)
+        else:
+            rng = np.random.default_rng(D * 7919 + k)
+            Yt = torch.from_numpy(rng.standard_normal((k, D))).to(device=G.device, dtype=G.dtype)
+        for _ in range(3):
+            Yt = kernels.matmul(Yt, G)          # (G Y)^T, G symmetric
+            kernels.orthonormalize(Yt)
+        Ht = kernels.matmul(Yt, G)
+        B = kernels.matmul(Yt, Ht, transB=True)  # Y^T G Y
+        ev, V = kernels.sym_eig(B)
+        Ut = kernels.matmul(V[:n].contiguous(), Yt)
+        lam = ev[:n]
+    kernels.flip_signs(Ut)
+    lam = lam.double().cpu().numpy()
+    return Ut, lam
+
+
+def _mode_svd(S, shape, l, n, tol_mlsvd, L, draw_cols):
+    """One mode: Gram, eigenpairs, signs, truncation. Returns (Ut, sigma, dim)."""
+    D = int(shape[l])
+    omega = _draw_omega(draw_cols, n + 10)
+    G = kernels.mode_gram(S, shape, l)
+    Ut, lam = top_eig(G, n, omega)
+    sigma = np.sqrt(np.maximum(lam, 0.0))
+    dim = clean_compression(sigma, tol_mlsvd, L)
+    return Ut[:dim].contiguous(), sigma[:dim], dim
+
+
+def _ref_draw_cols(shape, l):
+    """Row count of the reference's Gaussian block for this unfolding (Compression.py:487-493)."""
+    D = int(shape[l])
+    other = int(np.prod(shape, dtype=np.int64)) // D
+    return D if D < other else other
+
+
+def mlsvd_device(Td, R, options):
+    """Device MLSVD of a dense C-order tensor. Returns (S, Ut_list, sigmas, shape)."""
+    o = options
+    shape = [int(d) for d in Td.shape]
+    L = len(shape)
+    tol_mlsvd = o.tol_mlsvd
+    if isinstance(tol_mlsvd, list):
+        tol_mlsvd = tol_mlsvd[0] if L > 3 else tol_mlsvd[1]
+    if tol_mlsvd == -1:
+        eye = [torch.eye(d, dtype=Td.dtype, device=Td.device) for d in shape]
+        return Td, eye, [np.ones(d) for d in shape], shape
+    Uts, sigmas = [], []
+    if o.mlsvd_method in ('seq', 'gpu'):
+        S, cur = Td, list(shape)
+        for l in range(L):
+            n = o.svd_n_components if o.svd_n_components is not None else min(R, shape[l])
+            Ut, sig, dim = _mode_svd(S, cur, l, n, tol_mlsvd, L, _ref_draw_cols(cur, l))
+            Uts.append(Ut)
+            sigmas.append(sig)
+            S, cur = kernels.ttm(S, cur, l, Ut)
+    elif o.mlsvd_method == 'classic':
+        for l in range(L):
+            n = o.svd_n_components if o.svd_n_components is not None else min(R, shape[l])
+            Ut, sig, dim = _mode_svd(Td, shape, l, n, tol_mlsvd, L, _ref_draw_cols(shape, l))
+            Uts.append(Ut)
+            sigmas.append(sig)
+        S, cur = Td, list(shape)
+        for l in range(L):
+            S, cur = kernels.ttm(S, cur, l, Uts[l])
+    else:
+        raise NotImplementedError("mlsvd_method %r" % (o.mlsvd_method,))
+    if isinstance(o.trunc_dims, list):
+        sl = []
+        for l in range(L):
+            sl.append(slice(0, o.trunc_dims[l]))
+            Uts[l] = Uts[l][:min(o.trunc_dims[l], Uts[l].shape[0])].contiguous()
+        S = S[tuple(sl)].contiguous()
+        cur = list(S.shape)
+    return S.contiguous().view(*cur), Uts, sigmas, cur
+
+
+def mlsvd(T, Tsize, R, options=None):
+    """Drop-in for Compression.mlsvd: returns ``(S, U, T1, sigmas)`` as NumPy arrays.
+
+    ``T1`` is the first unfolding of ``T`` (a layout view, Conversion.py:231).
+    """
+    _dev.require_cuda()
+    o = make_options(options) if not hasattr(options, 'bi_method_parameters') else options
+    if isinstance(T, list):
+        from .sparse import mlsvd_sparse_device
+        data, idxs, dims = T
+        S, Uts, sigmas = mlsvd_sparse_device(data, idxs, dims, R, o)
+        from scipy.sparse import coo_matrix  # noqa: F401  (T1 is the sparse unfolding, built on request)
+        T1 = None
+    else:
+        prec = o.precision or ('fp64' if np.asarray(T).dtype == np.float64 else 'fp32')
+        Td = _dev.to_device(T, _dev.torch_dtype(prec))
+        S, Uts, sigmas, _ = mlsvd_device(Td, R, o)
+        T1 = np.moveaxis(np.asarray(T, dtype=np.float64), 0, 0).reshape(T.shape[0], -1, order='F')
+    U = [u.double().cpu().numpy().T.copy() for u in Uts]
+    return S.double().cpu().numpy(), U, T1, sigmas

@@ -1,0 +1,124 @@
+"""Thin wrappers over the C ABI entry points, taking CUDA torch tensors.
+
+Every function launches on the current torch stream and raises ``TfxError`` when
+the library reports a failure.  Shapes and strides follow the C ABI header.
+"""
+import ctypes
+
+import numpy as np
+import torch
+
+from . import _dev, _lib
+
+
+def _dt(t):
+    if t.dtype == torch.float64:
+        return _lib.F64
+    if t.dtype == torch.float32:
+        return _lib.F32
+    raise TypeError("tensors must be float32 or float64, got %s" % t.dtype)
+
+
+def _vp(t):
+    return ctypes.c_void_p(_dev.ptr(t))
+
+
+def _st():
+    return ctypes.c_void_p(_dev.stream())
+
+
+def mode_gram(S, shape, l):
+    """``S_(l) S_(l)^T`` (D x D) of a C-order tensor with the given shape."""
+    P = int(np.prod(shape[:l], dtype=np.int64))
+    D = int(shape[l])
+    Q = int(np.prod(shape[l + 1:], dtype=np.int64))
+    lib = _lib.load()
+    nb = lib.tfx_mode_gram_scratch_bytes(_dt(S), P, D, Q)
+    scratch = torch.empty(int(nb), dtype=torch.uint8, device=S.device)
+    G = torch.empty((D, D), dtype=S.dtype, device=S.device)
+    _lib.call("tfx_mode_gram", _dt(S), _vp(S), P, D, Q, _vp(G), _vp(scratch), nb, _st())
+    return G
+
+
+def gemm(A, B, C, M, N, K, batch, strides, alpha=1.0, beta=0.0):
+    arr = (ctypes.c_longlong * 9)(*[int(s) for s in strides])
+    _lib.call("tfx_gemm", _dt(A), _vp(A), _vp(B), _vp(C), int(M), int(N), int(K), int(batch), arr,
+              float(alpha), float(beta), _st())
+    return C
+
+
+def matmul(A, B, transA=False, transB=False):
+    """C = op(A) op(B) for 2-D row-major tensors (device GEMM)."""
+    M = A.shape[1] if transA else A.shape[0]
+    K = A.shape[0] if transA else A.shape[1]
+    N = B.shape[0] if transB else B.shape[1]
+    C = torch.empty((M, N), dtype=A.dtype, device=A.device)
+    sAm, sAk = (1, A.shape[1]) if transA else (A.shape[1], 1)
+    sBk, sBn = (1, B.shape[1]) if transB else (B.shape[1], 1)
+    A = A.contiguous()
+    B = B.contiguous()
+    return gemm(A, B, C, M, N, K, 1, [0, sAm, sAk, 0, sBk, sBn, 0, N, 1])
+
+
+def ttm(S, shape, l, Ut):
+    """Mode-l product with U^T: out[p, j, q] = sum_i U[i, j] S[p, i, q].
+
+    ``Ut`` is (n, D) row-major, i.e. U (D x n) column-major."""
+    P = int(np.prod(shape[:l], dtype=np.int64))
+    D = int(shape[l])
+    Q = int(np.prod(shape[l + 1:], dtype=np.int64))
+    n = int(Ut.shape[0])
+    out = torch.empty(P * n * Q, dtype=S.dtype, device=S.device)
+    Uc = Ut.contiguous()
+    if Q >= 16:
+        # batch over p: (n x D) (D x Q)
+        gemm(Uc, S, out, n, Q, D, P, [0, D, 1, D * Q, Q, 1, n * Q, Q, 1])
+    else:
+        # batch over q: (P x D) (D x n)
+        gemm(S, Uc, out, P, n, D, Q, [1, D * Q, Q, 0, 1, D, 1, n * Q, Q])
+    new_shape = list(shape)
+    new_shape[l] = n
+    return out.view(*new_shape), new_shape
+
+
+def orthonormalize(Y):
+    """CGS2 on the columns of Y given as a (k, D) row-major tensor (= D x k column-major)."""
+    k, D = Y.shape
+    _lib.call("tfx_orthonormalize", _dt(Y), _vp(Y), int(D), int(k), _st())
+    return Y
+
+
+def sym_eig(A, max_sweeps=40):
+    """Eigenvalues (descending) and eigenvectors (rows of the returned (n, n) tensor)."""
+    n = A.shape[0]
+    ev = torch.empty(n, dtype=A.dtype, device=A.device)
+    V = torch.empty((n, n), dtype=A.dtype, device=A.device)
+    _lib.call("tfx_sym_eig", _dt(A), _vp(A.contiguous()), int(n), _vp(ev), _vp(V), int(max_sweeps), None, _st())
+    return ev, V
+
+
+def flip_signs(Ut):
+    """Ut is (n, D) row-major = U (D x n) column-major."""
+    n, D = Ut.shape
+    _lib.call("tfx_flip_signs", _dt(Ut), _vp(Ut), int(D), int(n), _st())
+    return Ut
+
+
+def cp_residual_sq(T, dims, W_flat, R):
+    """||T - [[W]]||^2 on the device (float64 scalar tensor)."""
+    lib = _lib.load()
+    scratch = torch.empty(int(lib.tfx_cp_residual_scratch_bytes()), dtype=torch.uint8, device=T.device)
+    out = torch.empty(1, dtype=torch.float64, device=T.device)
+    L = len(dims)
+    cd = (ctypes.c_int * L)(*[int(d) for d in dims])
+    _lib.call("tfx_cp_residual", _dt(T), _vp(T), L, cd, int(R), _vp(W_flat), _vp(out), _vp(scratch), _st())
+    return out
+
+
+def tensor_norms(T):
+    """(sum t^2, sum |t|) as a float64 tensor of 2 entries."""
+    lib = _lib.load()
+    scratch = torch.empty(int(lib.tfx_cp_residual_scratch_bytes()), dtype=torch.uint8, device=T.device)
+    out = torch.empty(2, dtype=torch.float64, device=T.device)
+    _lib.call("tfx_tensor_norms", _dt(T), _vp(T), int(T.numel()), _vp(out), _vp(scratch), _st())
+    return out

@@ -1,0 +1,178 @@
+"""Dense device kernels (Gram, TTM, eigensolver, residual) and the full cpd vs the reference."""
+import numpy as np
+import pytest
+
+import tfx_oracle as orc
+from conftest import load_golden, split_x
+
+pytestmark = pytest.mark.gpu
+
+tfx = pytest.importorskip("tensorfox_gb300")
+torch = pytest.importorskip("torch")
+from tensorfox_gb300 import kernels  # noqa: E402
+
+
+def dev(a, dt=torch.float64):
+    return torch.from_numpy(np.ascontiguousarray(a)).to("cuda", dt)
+
+
+@pytest.mark.parametrize("shape,l", [((37, 23, 19), 0), ((37, 23, 19), 1), ((37, 23, 19), 2),
+                                     ((130, 70, 5), 0), ((9, 8, 7, 6), 2), ((300, 4, 3), 0)])
+@pytest.mark.parametrize("dt", [torch.float64, torch.float32])
+def test_mode_gram(shape, l, dt):
+    rng = np.random.default_rng(1)
+    T = rng.standard_normal(shape)
+    G = kernels.mode_gram(dev(T, dt), list(shape), l).double().cpu().numpy()
+    U = orc.unfold(T, l + 1)
+    ref = U @ U.T
+    tol = 1e-12 if dt == torch.float64 else 2e-5
+    np.testing.assert_allclose(G, ref, rtol=tol, atol=tol * np.abs(ref).max())
+
+
+@pytest.mark.parametrize("shape,l,n", [((37, 23, 19), 0, 5), ((37, 23, 19), 1, 7), ((37, 23, 19), 2, 19),
+                                       ((40, 30, 5), 2, 3), ((9, 8, 7, 6), 1, 4)])
+def test_ttm(shape, l, n):
+    rng = np.random.default_rng(2)
+    T = rng.standard_normal(shape)
+    U = np.linalg.qr(rng.standard_normal((shape[l], n)))[0]
+    out, new_shape = kernels.ttm(dev(T), list(shape), l, dev(U.T.copy()))
+    ref = np.moveaxis(np.tensordot(U.T, T, axes=(1, l)), 0, l)
+    np.testing.assert_allclose(out.cpu().numpy(), ref, rtol=1e-12, atol=1e-12)
+
+
+@pytest.mark.parametrize("n", [1, 2, 5, 16, 33, 64, 90])
+def test_sym_eig(n):
+    rng = np.random.default_rng(n)
+    A = rng.standard_normal((n, n))
+    A = A + A.T
+    ev, V = kernels.sym_eig(dev(A))
+    ev, V = ev.cpu().numpy(), V.cpu().numpy()
+    ref = np.sort(np.linalg.eigvalsh(A))[::-1]
+    np.testing.assert_allclose(ev, ref, rtol=1e-10, atol=1e-10)
+    # A v = lambda v for every returned pair, V orthonormal
+    np.testing.assert_allclose(A @ V.T, V.T * ev, atol=1e-9)
+    np.testing.assert_allclose(V @ V.T, np.eye(n), atol=1e-10)
+
+
+def test_orthonormalize():
+    rng = np.random.default_rng(3)
+    Y = rng.standard_normal((20, 500))
+    Yd = dev(Y)
+    kernels.orthonormalize(Yd)
+    Q = Yd.cpu().numpy()
+    np.testing.assert_allclose(Q @ Q.T, np.eye(20), atol=1e-12)
+    # same span
+    P = Q.T @ Q
+    np.testing.assert_allclose(P @ Y.T, Y.T, atol=1e-9)
+
+
+@pytest.mark.parametrize("dims,R", [((20, 15, 12), 4), ((9, 8, 7, 6), 3), ((70, 3, 66), 5)])
+@pytest.mark.parametrize("dt", [torch.float64, torch.float32])
+def test_cp_residual_and_norms(dims, R, dt):
+    rng = np.random.default_rng(4)
+    W = [rng.standard_normal((d, R)) for d in dims]
+    T = rng.standard_normal(dims)
+    x = np.concatenate([w.flatten('F') for w in W])
+    got = float(kernels.cp_residual_sq(dev(T, dt), dims, dev(x, dt), R).cpu().numpy()[0])
+    ref = orc.fastnorm(orc.unfold(T, 1), orc.cpd2unfold1(W)) ** 2
+    tol = 1e-12 if dt == torch.float64 else 1e-5
+    assert abs(got - ref) <= tol * ref
+    nrm = kernels.tensor_norms(dev(T, dt)).cpu().numpy()
+    assert abs(nrm[0] - np.sum(T ** 2)) <= tol * np.sum(T ** 2)
+    assert abs(nrm[1] - np.sum(np.abs(T))) <= tol * np.sum(np.abs(T))
+
+
+@pytest.mark.parametrize("name", ["mlsvd_seq", "mlsvd_classic", "mlsvd_seq_L4"])
+def test_mlsvd_matches_reference(name):
+    g = load_golden(name)
+    T, R = g["T"], int(g["R"])
+    o = tfx.make_options(None)
+    o.mlsvd_method = str(g["method"])
+    np.random.seed(int(g["seed"]))
+    S, U, T1, sig = tfx.mlsvd(T, np.linalg.norm(T), R, o)
+    assert [u.shape[1] for u in U] == list(g["ranks"])
+    np.testing.assert_allclose(np.concatenate(sig), g["sigmas"], rtol=1e-6)
+    Uref = np.concatenate([u.flatten('F') for u in U])
+    # same singular vectors (signs fixed by the shared convention)
+    np.testing.assert_allclose(Uref, g["U"], atol=1e-6)
+    np.testing.assert_allclose(S, g["S"], rtol=1e-5, atol=1e-6 * np.abs(g["S"]).max())
+
+
+def test_mlsvd_keeps_rng_in_step():
+    g = load_golden("mlsvd_seq")
+    np.random.seed(3)
+    orc.mlsvd(g["T"], 1.0, int(g["R"]), None)
+    want = np.random.rand()
+    np.random.seed(3)
+    tfx.mlsvd(g["T"], 1.0, int(g["R"]), None)
+    assert np.random.rand() == want
+
+
+def _congruence(A, B):
+    """Mean over columns of the product over modes of |cos| after best column matching."""
+    R = A[0].shape[1]
+    C = np.ones((R, R))
+    for a, b in zip(A, B):
+        an = a / np.linalg.norm(a, axis=0)
+        bn = b / np.linalg.norm(b, axis=0)
+        C *= np.abs(an.T @ bn)
+    from scipy.optimize import linear_sum_assignment
+    r, c = linear_sum_assignment(-C)
+    return C[r, c].min()
+
+
+def _opts(g):
+    o = tfx.Options()
+    for k, v in zip(g["opt_names"], g["opt_values"]):
+        setattr(o, str(k), eval(str(v)))
+    return o
+
+
+@pytest.mark.parametrize("name", ["cpd_c1_small", "cpd_L4", "cpd_refine"])
+def test_cpd_matches_reference(name):
+    g = load_golden(name)
+    T, R = g["T"], int(g["R"])
+    np.random.seed(int(g["seed"]))
+    f, out = tfx.cpd(T, R, _opts(g))
+    ref = float(g["rel_error"])
+    assert abs(out.rel_error - ref) <= 1e-2 * ref
+    dims = T.shape
+    fref = split_x(g["factors"], dims, R)
+    assert _congruence(f, fref) > 0.999
+    assert _congruence(f, split_x(g["planted"], dims, R)) > 0.999
+
+
+def test_reference_doctest_tensor():
+    """tests/simple_tensor_cpd_options.py:17-35 of the reference."""
+    g = load_golden("ref_tests_2x2x2")
+    errs = []
+    for seed in range(10):
+        np.random.seed(seed)
+        _, out = tfx.cpd(g["T"], 3)
+        errs.append(out.rel_error)
+    assert min(errs) < 1e-14
+    o = tfx.make_options(None)
+    o.initialization = [np.ones((2, 3))] * 3
+    _, out = tfx.cpd(g["T"], 3, o)
+    assert out.rel_error < 0.14
+    o.refine = True
+    _, out = tfx.cpd(g["T"], 3, o)
+    assert out.rel_error < 0.14
+    o.refine = False
+    o.inner_method = 'cg_static'
+    o.cg_maxiter = 3
+    o.cg_tol = 1e-7
+    _, out = tfx.cpd(g["T"], 3, o)
+    assert out.rel_error < 0.14
+
+
+def test_cpd_fp32_planted():
+    rng = np.random.default_rng(11)
+    dims, R = (60, 50, 40), 6
+    W = [rng.standard_normal((d, R)) for d in dims]
+    T = orc.cpd2tens(W)
+    T = (T + 1e-3 * np.linalg.norm(T) / np.sqrt(T.size) * rng.standard_normal(dims)).astype(np.float32)
+    np.random.seed(0)
+    f, out = tfx.cpd(T, R)
+    assert out.rel_error < 2e-3
+    assert _congruence(f, W) > 0.999
