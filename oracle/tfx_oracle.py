@@ -60,9 +60,15 @@ def make_options(options=None):
 # layout helpers (Conversion.py, Critical.py)
 # ----------------------------------------------------------------------------
 def unfold(T, mode):
-    """Mode-``mode`` (1-based) unfolding, Kolda order (Conversion.py:207-252)."""
-    d = T.shape[mode - 1]
-    return np.ascontiguousarray(np.moveaxis(T, mode - 1, 0).reshape(d, -1, order='F'), dtype=np.float64)
+    """Mode-``mode`` (1-based) unfolding, Kolda order (Conversion.py:207-252).
+
+    Column ``s = sum_{k != m} i_k prod_{j < k, j != m} d_j``: a C-order reshape of
+    the axes (m, last other, ..., first other), done as one transposing copy.
+    """
+    m = mode - 1
+    others = [k for k in range(T.ndim) if k != m]
+    perm = [m] + others[::-1]
+    return np.ascontiguousarray(np.transpose(T, perm), dtype=np.float64).reshape(T.shape[m], -1)
 
 
 def foldback(Tl, mode, dims):
@@ -680,12 +686,23 @@ class Output:
     pass
 
 
-def cpd(T, R, options=None):
+def cpd(T, R, options=None, timings=None):
     """``cpd`` → ``tricpd`` for method 'dGN' (TensorFox.py:69-255, 424-655).
 
     Returns ``(factors, output)`` where ``output`` carries num_steps, rel_error,
     accuracy, step_sizes, errors, improv, gradients and stop like the reference's.
+    ``timings`` (a dict) receives wall seconds of the 'mlsvd', 'dgn' and 'final'
+    phases when given.
     """
+    import time as _time
+    _t = [_time.perf_counter()]
+
+    def _mark(name):
+        now = _time.perf_counter()
+        if timings is not None:
+            timings[name] = timings.get(name, 0.0) + now - _t[0]
+        _t[0] = now
+
     o = make_options(options)
     sparse_in = isinstance(T, list)
     if sparse_in:
@@ -700,9 +717,12 @@ def cpd(T, R, options=None):
     else:
         Ts = np.asarray(Ts, dtype=np.float64)
         Tsize = norm(Ts)
+    _mark('prepare')
     S, U, T1, sigmas = mlsvd(Ts, Tsize, R, o)
+    _mark('mlsvd')
     init = starting_point(S, U, R, ordering, o)
     factors, ss, er, im, gr, st = dGN(S, init, R, o)
+    _mark('dgn')
     factors = [U[l] @ factors[l] for l in range(len(factors))]
     refine = o.refine and not sparse_in
     if refine:
@@ -726,4 +746,5 @@ def cpd(T, R, options=None):
     out.gradients = [gr, gr2]
     out.stop = [st, st2]
     out.options = o
+    _mark('final')
     return factors, out
