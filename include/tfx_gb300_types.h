@@ -31,7 +31,11 @@ enum tfx_dtype { TFX_F32 = 0, TFX_F64 = 1 };
  *   damp_sched: [maxiter] damping schedule when options.init_damp is a list, else NULL
  *   stats  : [4*maxiter] errors, step_sizes, improv, gradients (written)
  *   result : [4] stop code, iterations run, status, dogleg fallbacks (written)
- *   info   : [4] |T|, best error, final damping, mean|T| (written) */
+ *   info   : [4] |T|, best error, final damping, mean|T| (written)
+ *   prof   : optional [16] SM clock cycles per phase (gramians, gradient, CG,
+ *            update, residual, dogleg, control, total) and per CG step part
+ *            (publish+barrier, staging, A_k, Y_l, z_l, two reductions, update),
+ *            or NULL */
 typedef struct tfx_dgn_problem {
   int L;
   int R;
@@ -45,6 +49,7 @@ typedef struct tfx_dgn_problem {
   double* stats;
   int* result;
   double* info;
+  long long* prof;
 } tfx_dgn_problem;
 
 /* Solver options (Auxiliar.py:258-283 defaults; TensorFox.py:84-213 meaning). */

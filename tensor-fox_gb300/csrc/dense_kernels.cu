@@ -164,6 +164,56 @@ __global__ void __launch_bounds__(TFX_THREADS) k_gemm(const T* __restrict__ A, c
 // ---------------------------------------------------------------------------
 // CGS2 orthonormalisation of the k columns of Y (D x k, column-major), in place.
 // ---------------------------------------------------------------------------
+// Shared-memory variant: the whole D x k block lives in shared memory, so each
+// of the 4k dependent phases costs a barrier instead of an L2 round trip.
+template <class T>
+__global__ void __launch_bounds__(TFX_THREADS) k_orth_smem(T* Y, int D, int k) {
+  extern __shared__ __align__(16) char smem_o[];
+  T* Ys = (T*)smem_o;                          // k columns of length D
+  T* coef = Ys + (size_t)D * k;                // k coefficients
+  size_t roff = ((size_t)D * k + ((k + 1) & ~1) + 2) * sizeof(T);
+  roff = (roff + 15) & ~(size_t)15;
+  double* red = (double*)(smem_o + roff);
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  for (int e = tid; e < D * k; e += TFX_THREADS) Ys[e] = Y[e];
+  __syncthreads();
+  for (int j = 0; j < k; ++j) {
+    T* yj = Ys + (size_t)j * D;
+    for (int pass = 0; pass < 2; ++pass) {
+      for (int i = wid; i < j; i += TFX_THREADS / 32) {
+        const T* yi = Ys + (size_t)i * D;
+        T s = T(0);
+        for (int r = lane; r < D; r += 32) s = fma(yi[r], yj[r], s);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        if (lane == 0) coef[i] = s;
+      }
+      __syncthreads();
+      for (int r = tid; r < D; r += TFX_THREADS) {
+        T v = yj[r];
+        for (int i = 0; i < j; ++i) v = fma(-coef[i], Ys[(size_t)i * D + r], v);
+        yj[r] = v;
+      }
+      __syncthreads();
+    }
+    double sq = 0.0;
+    for (int r = tid; r < D; r += TFX_THREADS) sq += (double)yj[r] * (double)yj[r];
+    sq = warp_sum(sq);
+    if (lane == 0) red[wid] = sq;
+    __syncthreads();
+    double nrm = 0.0;
+    for (int w = 0; w < TFX_THREADS / 32; ++w) nrm += red[w];
+    const T inv = (T)(nrm > 0.0 ? 1.0 / sqrt(nrm) : 0.0);
+    for (int r = tid; r < D; r += TFX_THREADS) yj[r] = yj[r] * inv;
+    __syncthreads();
+  }
+  for (int e = tid; e < D * k; e += TFX_THREADS) Y[e] = Ys[e];
+}
+
+static size_t orth_smem_bytes(int D, int k, size_t es) {
+  return (size_t)D * k * es + (size_t)(((k + 1) & ~1) + 2) * es + 16 + (TFX_THREADS / 32) * sizeof(double) + 16;
+}
+
 template <class T>
 __global__ void __launch_bounds__(TFX_THREADS) k_orth(T* Y, int D, int k) {
   // arithmetic in the working precision T: GB300's FP64 rate is a small
@@ -260,16 +310,21 @@ __global__ void __launch_bounds__(TFX_THREADS) k_jacobi(const T* __restrict__ Ai
         const int p = a < b ? a : b, q = a < b ? b : a;
         pr[2 * kk] = p;
         pr[2 * kk + 1] = q;
-        const double apq = (double)A[p * m + q];
-        double c = 1.0, s = 0.0;
-        if (fabs(apq) > 1e-300) {
-          const double tau = ((double)A[q * m + q] - (double)A[p * m + p]) / (2.0 * apq);
-          const double t = (tau >= 0.0 ? 1.0 : -1.0) / (fabs(tau) + sqrt(1.0 + tau * tau));
-          c = 1.0 / sqrt(1.0 + t * t);
+        // rotation in the working precision (FP64 division and square root
+        // are slow on GB300; the FP64 path keeps them in FP64)
+        const T apq = A[p * m + q];
+        T c = T(1), s = T(0);
+        if (apq != T(0)) {
+          const T tau = (A[q * m + q] - A[p * m + p]) / (T(2) * apq);
+          const T at = fabs(tau);
+          // for huge |tau| use t ~ 1/(2 tau) to avoid overflow of tau*tau
+          const T t = (at > T(1e18)) ? T(1) / (T(2) * tau)
+                                      : (tau >= T(0) ? T(1) : T(-1)) / (at + sqrt(T(1) + tau * tau));
+          c = T(1) / sqrt(T(1) + t * t);
           s = t * c;
         }
-        cs[kk] = (T)c;
-        cs[m / 2 + kk] = (T)s;
+        cs[kk] = c;
+        cs[m / 2 + kk] = s;
       }
       __syncthreads();
       // columns: A <- A J, V <- V J
@@ -550,20 +605,48 @@ extern "C" int tfx_gemm(int dtype, const void* A, const void* B, void* C, long l
   g.alpha = alpha;
   g.beta = beta;
   cudaStream_t st = (cudaStream_t)stream;
-  const long long tiles = ((M + 63) / 64) * ((N + 63) / 64);
-  if (tiles > 0x7fffffffLL) return tfx_set_error(TFX_STATUS_ERR_ARG, "gemm too large");
+  // smaller tiles when the output is too small to fill the GPU with 64x64 tiles
+  int ts = 4;
   const long long by = std::min<long long>(batch, 65535);
+  while (ts > 1) {
+    const long long b = 16LL * ts;
+    if (((M + b - 1) / b) * ((N + b - 1) / b) * by >= 2LL * num_sms()) break;
+    ts >>= 1;
+  }
+  const long long bs = 16LL * ts;
+  const long long tiles = ((M + bs - 1) / bs) * ((N + bs - 1) / bs);
+  if (tiles > 0x7fffffffLL) return tfx_set_error(TFX_STATUS_ERR_ARG, "gemm too large");
   dim3 grid((unsigned)tiles, (unsigned)by);
-  if (dtype == TFX_F32)
-    k_gemm<float, 4><<<grid, TFX_THREADS, 0, st>>>((const float*)A, (const float*)B, (float*)C, g);
-  else
-    k_gemm<double, 4><<<grid, TFX_THREADS, 0, st>>>((const double*)A, (const double*)B, (double*)C, g);
+  if (dtype == TFX_F32) {
+    if (ts == 4) k_gemm<float, 4><<<grid, TFX_THREADS, 0, st>>>((const float*)A, (const float*)B, (float*)C, g);
+    else if (ts == 2) k_gemm<float, 2><<<grid, TFX_THREADS, 0, st>>>((const float*)A, (const float*)B, (float*)C, g);
+    else k_gemm<float, 1><<<grid, TFX_THREADS, 0, st>>>((const float*)A, (const float*)B, (float*)C, g);
+  } else {
+    if (ts == 4) k_gemm<double, 4><<<grid, TFX_THREADS, 0, st>>>((const double*)A, (const double*)B, (double*)C, g);
+    else if (ts == 2) k_gemm<double, 2><<<grid, TFX_THREADS, 0, st>>>((const double*)A, (const double*)B, (double*)C, g);
+    else k_gemm<double, 1><<<grid, TFX_THREADS, 0, st>>>((const double*)A, (const double*)B, (double*)C, g);
+  }
   return check_launch("gemm");
 }
 
 extern "C" int tfx_orthonormalize(int dtype, void* Y, int D, int k, void* stream) {
   if (!Y || D < 1 || k < 1 || k > 1024) return tfx_set_error(TFX_STATUS_ERR_ARG, "orthonormalize args");
   cudaStream_t st = (cudaStream_t)stream;
+  const size_t es = dtype == TFX_F64 ? 8 : 4;
+  const size_t sm = orth_smem_bytes(D, k, es);
+  if (sm <= 200 * 1024) {
+    cudaError_t e;
+    if (dtype == TFX_F32) {
+      e = cudaFuncSetAttribute(k_orth_smem<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+      if (e != cudaSuccess) return tfx_set_cuda_error(e, "orth attr");
+      k_orth_smem<float><<<1, TFX_THREADS, sm, st>>>((float*)Y, D, k);
+    } else {
+      e = cudaFuncSetAttribute(k_orth_smem<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+      if (e != cudaSuccess) return tfx_set_cuda_error(e, "orth attr");
+      k_orth_smem<double><<<1, TFX_THREADS, sm, st>>>((double*)Y, D, k);
+    }
+    return check_launch("orthonormalize");
+  }
   if (dtype == TFX_F32)
     k_orth<float><<<1, TFX_THREADS, 0, st>>>((float*)Y, D, k);
   else

@@ -14,8 +14,7 @@ extern "C" int tfx_dgn_solve(int dtype, const tfx_dgn_problem* h_probs, tfx_dgn_
                              const tfx_dgn_options* op, int cluster, void* stream) {
   if (h_probs == nullptr || d_probs == nullptr || op == nullptr || nprob < 1)
     return tfx_set_error(TFX_STATUS_ERR_ARG, "null argument");
-  if (cluster != 1 && cluster != 2 && cluster != 4 && cluster != 8 && cluster != 16)
-    return tfx_set_error(TFX_STATUS_ERR_ARG, "cluster must be 1, 2, 4, 8 or 16");
+  if (cluster < 1 || cluster > 16) return tfx_set_error(TFX_STATUS_ERR_ARG, "cluster must be in 1..16");
   if (op->maxiter < 1) return tfx_set_error(TFX_STATUS_ERR_ARG, "maxiter must be >= 1");
   int maxL = 0, maxR = 0, maxd = 0, maxdim_or_R = 0;
   for (int p = 0; p < nprob; ++p) {
@@ -44,7 +43,16 @@ extern "C" int tfx_dgn_solve(int dtype, const tfx_dgn_problem* h_probs, tfx_dgn_
   const int maxncol = (maxR + cluster - 1) / cluster;
   const size_t es = dtype == TFX_F64 ? 8 : 4;
   if (op->maxiter > 4096) return tfx_set_error(TFX_STATUS_ERR_UNSUPPORTED, "maxiter above 4096");
-  SmemPlan sp = smem_plan(TS, es, maxL, maxR, maxd, maxncol, op->maxiter);
+  int maxnx = 0, maxsumd = 0;
+  for (int p = 0; p < nprob; ++p) {
+    int sd = 0;
+    for (int l = 0; l < h_probs[p].L; ++l) sd += h_probs[p].dims[l];
+    maxnx = sd * h_probs[p].R > maxnx ? sd * h_probs[p].R : maxnx;
+    maxsumd = sd > maxsumd ? sd : maxsumd;
+  }
+  // stage the CG operands in shared memory when they fit, else read them from L2
+  SmemPlan sp = smem_plan(TS, es, maxL, maxR, maxd, maxncol, op->maxiter, maxnx, maxsumd, 1);
+  if (sp.total > 200 * 1024) sp = smem_plan(TS, es, maxL, maxR, maxd, maxncol, op->maxiter, maxnx, maxsumd, 0);
   if (sp.total > 220 * 1024) return tfx_set_error(TFX_STATUS_ERR_UNSUPPORTED, "problem too large for the engine's shared memory; use a larger cluster");
   cudaStream_t st = (cudaStream_t)stream;
   cudaError_t e = cudaMemcpyAsync(d_probs, h_probs, sizeof(tfx_dgn_problem) * nprob, cudaMemcpyHostToDevice, st);

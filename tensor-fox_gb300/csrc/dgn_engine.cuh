@@ -30,6 +30,7 @@
 #include "../../include/tfx_gb300_types.h"
 
 #include <math.h>
+#include <type_traits>
 #include <stdio.h>
 
 namespace tfx {
@@ -66,13 +67,16 @@ __host__ __device__ inline WsLayout ws_layout(int L, int R, int nx, size_t es) {
 }
 
 struct SmemPlan {
-  size_t sA, sB, sPart, sAk, sY, sM, sDG, sGam, sNorm, sBase, sIdx, rs4, rs12, misc, hist, total;
+  size_t sA, sB, sPart, sAk, sY, sM, sDG, sGam, sNorm, sBase, sIdx, rs4, rs12, misc, hist, rs1, rs1b, sScale;
+  size_t sQf, sWf, sP1o, sP2o, sVec;  // staged operands of the CG (valid when stage != 0)
+  int stage;
+  size_t total;
 };
 
 __host__ __device__ inline size_t al16(size_t v) { return (v + 15) & ~(size_t)15; }
 
 __host__ __device__ inline SmemPlan smem_plan(int TS, size_t es, int maxL, int maxR, int maxd, int maxncol,
-                                               int maxiter) {
+                                               int maxiter, int maxnx, int maxsumd, int stage) {
   SmemPlan p;
   const int BM = 16 * TS, BN = 16 * TS;
   size_t o = 0;
@@ -90,10 +94,324 @@ __host__ __device__ inline SmemPlan smem_plan(int TS, size_t es, int maxL, int m
   p.sIdx = o; o += al16((size_t)NB * maxL * sizeof(int));
   p.rs4 = o; o += al16(sizeof(RedScratch<4>));
   p.rs12 = o; o += al16(sizeof(RedScratch<TFX_MAX_ORDER>));
-  p.misc = o; o += 64;
+  p.misc = o; o += 64 + 16 * TFX_MAX_ORDER * 8;
   p.hist = o; o += al16((size_t)2 * maxiter * sizeof(double));
+  p.rs1 = o; o += al16(sizeof(RedScratch<1>));
+  p.rs1b = o; o += al16(sizeof(RedScratch<1>));
+  p.sScale = o; o += al16((size_t)maxL * maxncol * es);
+  p.stage = stage;
+  p.sQf = p.sWf = p.sP1o = p.sP2o = p.sVec = o;
+  if (stage) {
+    p.sQf = o; o += al16((size_t)maxnx * es);
+    p.sWf = o; o += al16((size_t)maxnx * es);
+    p.sP1o = o; o += al16((size_t)maxL * maxR * maxncol * es);
+    p.sP2o = o; o += al16((size_t)maxL * maxL * maxR * maxncol * es);
+    // the CTA's own slices of r, P, y, z and the expanded M, damp*Gamma
+    const size_t own = (size_t)maxncol * (size_t)maxsumd;
+    p.sVec = o; o += al16(6 * own * es);
+  }
   p.total = o;
   return p;
+}
+
+__device__ __forceinline__ char* dyn_smem() {
+  extern __shared__ __align__(16) char tfx_dsm[];
+  return tfx_dsm;
+}
+
+// ---------------------------------------------------------------------------
+// CG inner solve of one team, written with register-resident scalars and
+// shared-memory pointers derived from the dynamic shared-memory symbol, so
+// that its hot loops use direct shared-memory accesses.
+//
+// J^T J v for the owned columns (GaussNewton.py:371-377, 551-581):
+//   A_k = D_k^T W_k,  Y_l = sum_{k != l} P2[l][k] o A_k,  z_l = W_l Y_l + D_l P1_l
+// Preconditioned CG (GaussNewton.py:315-398), reference quirks included: the
+// first new direction is (1+beta) r because P aliases the residual array.
+// STAGED: the full input vector, the factors and the owned P1/P2 columns sit in
+// shared memory; otherwise they are read from global memory (L2).
+// ---------------------------------------------------------------------------
+struct CgOffsets {
+  size_t d, sQf, sWf, sP1o, sP2o, sAk, sY, sM, sDG, rs4, rs1, sVec;
+};
+
+// Copy n elements written by other CTAs of the team from global memory into
+// shared memory.  ld.global.cg reads at L2 (coherent across SMs) and lets the
+// loads of one thread overlap instead of queueing behind its shared stores.
+template <class T>
+__device__ __forceinline__ void stage_copy(T* sdst, const T* gsrc, int n) {
+  constexpr int V = 16 / sizeof(T);
+  using V4 = typename std::conditional<sizeof(T) == 4, float4, double2>::type;
+  const int nv = n / V;
+  const V4* src = reinterpret_cast<const V4*>(gsrc);
+  V4* dst = reinterpret_cast<V4*>(sdst);
+  int e = threadIdx.x;
+  for (; e + 3 * TFX_THREADS < nv; e += 4 * TFX_THREADS) {
+    const V4 a = __ldcg(src + e), b = __ldcg(src + e + TFX_THREADS);
+    const V4 c = __ldcg(src + e + 2 * TFX_THREADS), d4 = __ldcg(src + e + 3 * TFX_THREADS);
+    dst[e] = a;
+    dst[e + TFX_THREADS] = b;
+    dst[e + 2 * TFX_THREADS] = c;
+    dst[e + 3 * TFX_THREADS] = d4;
+  }
+  for (; e < nv; e += TFX_THREADS) dst[e] = __ldcg(src + e);
+  for (int t = nv * V + threadIdx.x; t < n; t += TFX_THREADS) sdst[t] = __ldcg(gsrc + t);
+}
+
+template <class T, bool STAGED>
+__device__ __forceinline__ void cg_matvec(const int L, const int R, const int nx, const int ncol, const int c0,
+                                          const CgOffsets so, const T* Dglob, T* zout, const T* Wg, const T* P1g,
+                                          const T* P2g, T* zloc = nullptr, long long* cprof = nullptr) {
+  // timers accumulate in registers of thread 0 (cprof points at its private array)
+  long long tc = cprof ? clock64() : 0;
+  auto ctick = [&](int ph) {
+    if (cprof) {
+      const long long now = clock64();
+      cprof[ph] += now - tc;
+      tc = now;
+    }
+  };
+  char* sm = dyn_smem();
+  const int* d = (const int*)(sm + so.d);
+  const int* off = d + TFX_MAX_ORDER;
+  T* sAk = (T*)(sm + so.sAk);
+  T* sY = (T*)(sm + so.sY);
+  const int tid = threadIdx.x;
+  const T* Din;
+  const T* Wr;
+  if (STAGED) {
+    T* sQf = (T*)(sm + so.sQf);
+    stage_copy(sQf, Dglob, nx);
+    __syncthreads();
+    ctick(1);
+    Din = sQf;
+    Wr = (const T*)(sm + so.sWf);
+  } else {
+    Din = Dglob;
+    Wr = Wg;
+  }
+  const T* sP1o = (const T*)(sm + so.sP1o);
+  const T* sP2o = (const T*)(sm + so.sP2o);
+  const int RN = R * ncol;
+  for (int e = tid; e < L * RN; e += TFX_THREADS) {
+    const int k = e / RN, q = e - k * RN, a = q / ncol, c = q - a * ncol;
+    const int dk = d[k];
+    const T* dv = Din + off[k] + a * dk;
+    const T* wv = Wr + off[k] + (c0 + c) * dk;
+    T acc = T(0);
+#pragma unroll 4
+    for (int i = 0; i < dk; ++i) acc = fma(dv[i], wv[i], acc);
+    sAk[e] = acc;
+  }
+  __syncthreads();
+  ctick(2);
+  for (int e = tid; e < L * RN; e += TFX_THREADS) {
+    const int l = e / RN, q = e - l * RN, a = q / ncol, c = q - a * ncol;
+    T acc = T(0);
+    for (int k = 0; k < L; ++k) {
+      if (k == l) continue;
+      const T p2 = STAGED ? sP2o[((size_t)(l * L + k) * R + a) * ncol + c]
+                          : P2g[((size_t)(l * L + k) * R + a) * R + c0 + c];
+      acc += p2 * sAk[(size_t)k * RN + q];
+    }
+    sY[e] = acc;
+  }
+  __syncthreads();
+  ctick(3);
+  // z_l = W_l Y_l + D_l P1_l over all owned outputs of all modes at once
+  const int ownn = ncol * (nx / R);
+  for (int e = tid; e < ownn; e += TFX_THREADS) {
+    int l = 0, rem = e;
+    while (rem >= ncol * d[l]) {
+      rem -= ncol * d[l];
+      ++l;
+    }
+    const int dl = d[l], ol = off[l];
+    const int c = rem / dl, i = rem - c * dl;
+    const T* wrow = Wr + ol + i;
+    const T* drow = Din + ol + i;
+    const T* yc = sY + (size_t)l * RN + c;
+    const T* p1c = STAGED ? sP1o + (size_t)l * R * ncol + c : P1g + (size_t)l * R * R + c0 + c;
+    const int p1s = STAGED ? ncol : R;
+    T a1 = T(0), a2 = T(0);
+#pragma unroll 4
+    for (int r = 0; r < R; ++r) {
+      a1 = fma(wrow[r * dl], yc[r * ncol], a1);
+      a2 = fma(drow[r * dl], p1c[r * p1s], a2);
+    }
+    if (zloc)
+      zloc[e] = a1 + a2;
+    else
+      zout[ol + (c0 + c) * dl + i] = a1 + a2;
+  }
+  __syncthreads();
+  ctick(4);
+}
+
+template <class T, bool STAGED>
+__device__ __forceinline__ int cg_team(const Team tm, const int L, const int R, const int nx, const int ncol,
+                                       const int c0, const CgOffsets so, T* grad, T* jtj, T* y, T* r, T* P, T* Q,
+                                       T* z, const T* Wg, const T* P1g, const T* P2g, const int budget,
+                                       const double cg_tol, double& rn_out, int& flip4, long long* cprof_g) {
+  long long lprof[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  long long* cprof = cprof_g ? lprof : nullptr;
+  long long tc = cprof ? clock64() : 0;
+  auto ctick = [&](int ph) {
+    if (cprof) {
+      const long long now = clock64();
+      cprof[ph] += now - tc;
+      tc = now;
+    }
+  };
+  char* sm = dyn_smem();
+  const int* d = (const int*)(sm + so.d);
+  const int* off = d + TFX_MAX_ORDER;
+  const T* sM = (const T*)(sm + so.sM);
+  const T* sDG = (const T*)(sm + so.sDG);
+  RedScratch<1>* rs1 = (RedScratch<1>*)(sm + so.rs1);
+  const int tid = threadIdx.x;
+  // own slice: element (l, c, i) lives at local index ncol*(off[l]/R) + c*d[l] + i
+  const int own = ncol * (nx / R);
+  T *vr, *vP, *vy, *vz, *vM, *vDG;
+  if (STAGED) {
+    vr = (T*)(sm + so.sVec);
+    vP = vr + own;
+    vy = vP + own;
+    vz = vy + own;
+    vM = vz + own;
+    vDG = vM + own;
+  }
+  cg_matvec<T, STAGED>(L, R, nx, ncol, c0, so, grad, jtj, Wg, P1g, P2g);
+  Acc<T> v[1];
+  double red[1];
+  for (int l = 0; l < L; ++l) {
+    const int dl = d[l], base = off[l] + c0 * dl, n = ncol * dl, lb = ncol * (off[l] / R);
+    for (int e = tid; e < n; e += TFX_THREADS) {
+      const int c = e / dl, g = base + e;
+      const T m = sM[l * ncol + c];
+      const T rr = m * __ldcg(grad + g);
+      if (STAGED) {
+        vM[lb + e] = m;
+        vDG[lb + e] = sDG[l * ncol + c];
+        vr[lb + e] = rr;
+        vP[lb + e] = rr;
+        vy[lb + e] = T(0);
+      } else {
+        r[g] = rr;
+        P[g] = rr;
+        y[g] = T(0);
+      }
+      v[0].fma_(rr, rr);
+    }
+  }
+  team_sum_acc<1, T>(tm, v, red, rs1, flip4);
+  double rn = red[0];
+  if (rn == 0.0) rn = 1e-6;
+  int maxit = budget;
+  double tol = cg_tol;
+  if (nx > 100) {
+    maxit = min(maxit, nx);
+  } else {
+    tol = 0.0;
+  }
+  int itn = 0;
+  bool broke = false;
+  for (itn = 0; itn < maxit; ++itn) {
+    // Q = M P (owned part, published through global memory)
+    for (int l = 0; l < L; ++l) {
+      const int dl = d[l], base = off[l] + c0 * dl, n = ncol * dl, lb = ncol * (off[l] / R);
+      for (int e = tid; e < n; e += TFX_THREADS) {
+        if (STAGED) {
+          Q[base + e] = vM[lb + e] * vP[lb + e];
+        } else {
+          const int c = e / dl;
+          Q[base + e] = sM[l * ncol + c] * P[base + e];
+        }
+      }
+    }
+    tm.sync();
+    ctick(0);
+    cg_matvec<T, STAGED>(L, R, nx, ncol, c0, so, Q, z, Wg, P1g, P2g, STAGED ? vz : nullptr, cprof);
+    if (cprof) tc = clock64();
+    Acc<T> w[1];
+    const T* Qs = STAGED ? (const T*)(sm + so.sQf) : Q;  // full Q, staged by the matvec
+    for (int l = 0; l < L; ++l) {
+      const int dl = d[l], base = off[l] + c0 * dl, n = ncol * dl, lb = ncol * (off[l] / R);
+      for (int e = tid; e < n; e += TFX_THREADS) {
+        if (STAGED) {
+          const T zz = vM[lb + e] * (vz[lb + e] + vDG[lb + e] * Qs[base + e]);
+          vz[lb + e] = zz;
+          w[0].fma_(vP[lb + e], zz);
+        } else {
+          const int c = e / dl, g = base + e;
+          const T zz = sM[l * ncol + c] * (z[g] + sDG[l * ncol + c] * Q[g]);
+          z[g] = zz;
+          w[0].fma_(P[g], zz);
+        }
+      }
+    }
+    team_sum_acc<1, T>(tm, w, red, rs1, flip4);
+    ctick(5);
+    double den = red[0];
+    if (den == 0.0) den = 1e-6;
+    const double alpha = rn / den;
+    const T ta = (T)alpha;
+    Acc<T> u[1];
+    if (STAGED) {
+      for (int e = tid; e < own; e += TFX_THREADS) {
+        vy[e] += ta * vP[e];
+        const T rr = vr[e] - ta * vz[e];
+        vr[e] = rr;
+        u[0].fma_(rr, rr);
+      }
+    } else {
+      for (int l = 0; l < L; ++l) {
+        const int dl = d[l], base = off[l] + c0 * dl, n = ncol * dl;
+        for (int e = tid; e < n; e += TFX_THREADS) {
+          const int g = base + e;
+          y[g] += ta * P[g];
+          const T rr = r[g] - ta * z[g];
+          r[g] = rr;
+          u[0].fma_(rr, rr);
+        }
+      }
+    }
+    team_sum_acc<1, T>(tm, u, red, rs1, flip4);
+    ctick(6);
+    const double rn_new = red[0];
+    const double beta = rn_new / rn;
+    rn = rn_new;
+    const T tb = (T)beta;
+    if (STAGED) {
+      for (int e = tid; e < own; e += TFX_THREADS) vP[e] = (itn == 0) ? vr[e] + tb * vr[e] : vr[e] + tb * vP[e];
+    } else {
+      for (int l = 0; l < L; ++l) {
+        const int dl = d[l], base = off[l] + c0 * dl, n = ncol * dl;
+        for (int e = tid; e < n; e += TFX_THREADS) {
+          const int g = base + e;
+          P[g] = (itn == 0) ? r[g] + tb * r[g] : r[g] + tb * P[g];
+        }
+      }
+    }
+    ctick(7);
+    if (rn <= tol) {
+      broke = true;
+      break;
+    }
+  }
+  if (STAGED) {
+    // the step leaves the team's shared memory for the update phase
+    __syncthreads();
+    for (int l = 0; l < L; ++l) {
+      const int dl = d[l], base = off[l] + c0 * dl, n = ncol * dl, lb = ncol * (off[l] / R);
+      for (int e = tid; e < n; e += TFX_THREADS) y[base + e] = vy[lb + e];
+    }
+  }
+  __syncthreads();
+  if (cprof_g)
+    for (int k = 0; k < 8; ++k) cprof_g[k] += lprof[k];
+  rn_out = rn;
+  return broke ? itn + 1 : maxit;
 }
 
 template <class T, int TS>
@@ -102,9 +420,10 @@ struct Engine {
   Team tm;
   int tid;
   int L, R, nx, ncol, c0, c1, maxd;
-  int d[TFX_MAX_ORDER];
-  int off[TFX_MAX_ORDER + 1];
-  long long st[TFX_MAX_ORDER];
+  // problem shape, kept in shared memory (dynamically indexed in hot loops)
+  int* d;
+  int* off;
+  long long* st;
   long long N;
   const T* Tt;
   T *xc, *xn, *W, *grad, *jtj, *y, *r, *P, *Q, *z, *bx, *by, *bW, *P1, *P2;
@@ -115,9 +434,33 @@ struct Engine {
   int* sIdx;
   RedScratch<4>* rs4;
   RedScratch<TFX_MAX_ORDER>* rs12;
-  int flip4, flip12;
+  int flip4, flip12, flip1, flip1b;
+  RedScratch<1>* rs1b;
+  T* sScale;
   double damp, Tsize;
   tfx_dgn_options op;
+  // staged operands: full search direction and factors, owned P1/P2 columns
+  int stage;
+  T *sQf, *sWf, *sP1o, *sP2o;
+  const T* Wr;  // factors to read: shared-memory copy when staged
+
+  __device__ __forceinline__ T& P1at(int l, int a, int c) {
+    return stage ? sP1o[((size_t)l * R + a) * ncol + c] : P1[((size_t)l * R + a) * R + c0 + c];
+  }
+  __device__ __forceinline__ T& P2at(int l, int k, int a, int c) {
+    return stage ? sP2o[((size_t)(l * L + k) * R + a) * ncol + c] : P2[((size_t)(l * L + k) * R + a) * R + c0 + c];
+  }
+
+  // copy the (complete, synchronised) global factors into shared memory
+  __device__ void stage_W() {
+    if (stage) {
+      stage_copy(sWf, W, nx);
+      __syncthreads();
+      Wr = sWf;
+    } else {
+      Wr = W;
+    }
+  }
 
   // -------------------------------------------------------------------------
   // generic small contraction: out(m, n) = sum_k A(m, k) B(k, n)
@@ -187,8 +530,8 @@ struct Engine {
     for (int u = tm.rank * TFX_THREADS + tid; u < L * RR; u += tm.size * TFX_THREADS) {
       const int l = u / RR, q = u - l * RR, a = q / R, b = q - a * R;
       if (a > b) continue;
-      const T* pa = W + off[l] + a * d[l];
-      const T* pb = W + off[l] + b * d[l];
+      const T* pa = Wr + off[l] + a * d[l];
+      const T* pb = Wr + off[l] + b * d[l];
       double acc = 0.0;
       for (int i0 = 0; i0 < d[l]; i0 += 16) {
         T p = T(0);
@@ -209,13 +552,13 @@ struct Engine {
       double p = 1.0;
       for (int m = 0; m < L; ++m)
         if (m != l && m != k) p *= G[(size_t)m * RR + a * R + b];
-      P2[((size_t)(l * L + k) * R + a) * R + b] = (T)p;
+      P2at(l, k, a, c) = (T)p;
     }
     // P1 with the reference's product order
     for (int e = tid; e < L * R * ncol; e += TFX_THREADS) {
       const int l = e / (R * ncol), q = e - l * (R * ncol), a = q / ncol, c = q - a * ncol;
       const int b = c0 + c;
-      P1[((size_t)l * R + a) * R + b] = (T)p1_value(l, a, b);
+      P1at(l, a, c) = (T)p1_value(l, a, b);
     }
     // tmp = max |P1[L-1]| over the whole matrix (every CTA computes it)
     double mx = 0.0;
@@ -285,7 +628,15 @@ struct Engine {
               sBase[tid] = base;
             }
             __syncthreads();
-            for (int e = tid; e < TFX_BK * TL::BM; e += TFX_THREADS) {
+            // all of this thread's tensor loads are issued before any shared
+            // store (read-only path: the tensor is constant during the solve)
+            constexpr int NPT = (TFX_BK * TL::BM + TFX_THREADS - 1) / TFX_THREADS;
+            T av[NPT];
+            const long long stl = st[l];
+            const int dl = d[l];
+#pragma unroll
+            for (int j = 0; j < NPT; ++j) {
+              const int e = tid + j * TFX_THREADS;
               int kk, mm;
               if (l == L - 1) {
                 kk = e / TL::BM;
@@ -294,9 +645,23 @@ struct Engine {
                 mm = e / TFX_BK;
                 kk = e - mm * TFX_BK;
               }
-              T v = T(0);
-              if (kk < kc && m0 + mm < d[l]) v = Tt[sBase[kk] + (long long)(m0 + mm) * st[l]];
-              sA[kk * TL::LDA + mm] = v;
+              av[j] = (e < TFX_BK * TL::BM && kk < kc && m0 + mm < dl) ? __ldg(Tt + sBase[kk] + (long long)(m0 + mm) * stl)
+                                                                     : T(0);
+            }
+#pragma unroll
+            for (int j = 0; j < NPT; ++j) {
+              const int e = tid + j * TFX_THREADS;
+              if (e < TFX_BK * TL::BM) {
+                int kk, mm;
+                if (l == L - 1) {
+                  kk = e / TL::BM;
+                  mm = e - kk * TL::BM;
+                } else {
+                  mm = e / TFX_BK;
+                  kk = e - mm * TFX_BK;
+                }
+                sA[kk * TL::LDA + mm] = av[j];
+              }
             }
             for (int e = tid; e < TFX_BK * TL::BN; e += TFX_THREADS) {
               const int kk = e / TL::BN, nn = e - kk * TL::BN;
@@ -304,7 +669,7 @@ struct Engine {
               if (kk < kc && n0 + nn < R) {
                 v = T(1);
                 for (int m = L - 1; m >= 0; --m)
-                  if (m != l) v *= W[off[m] + (n0 + nn) * d[m] + sIdx[kk * L + m]];
+                  if (m != l) v *= Wr[off[m] + (n0 + nn) * d[m] + sIdx[kk * L + m]];
               }
               sB[kk * TL::LDB + nn] = v;
             }
@@ -325,119 +690,31 @@ struct Engine {
       // reduce own columns and subtract W_l P1_l
       for (int e = tid; e < d[l] * ncol; e += TFX_THREADS) {
         const int c = e / d[l], i = e - c * d[l], b = c0 + c;
+        // issue every peer's load before summing (independent remote loads)
+        T pv[TFX_MAX_TEAM];
+#pragma unroll
+        for (int rr = 0; rr < TFX_MAX_TEAM; ++rr) pv[rr] = rr < tm.size ? tm.peer(sPart, rr)[i * R + b] : T(0);
         T mk = T(0);
-        for (int rr = 0; rr < tm.size; ++rr) mk += tm.peer(sPart, rr)[i * R + b];
+#pragma unroll
+        for (int rr = 0; rr < TFX_MAX_TEAM; ++rr)
+          if (rr < tm.size) mk += pv[rr];
         T wp = T(0);
-        for (int s = 0; s < R; ++s) wp = fma(W[off[l] + s * d[l] + i], P1[((size_t)l * R + s) * R + b], wp);
+        for (int s = 0; s < R; ++s) wp = fma(Wr[off[l] + s * d[l] + i], P1at(l, s, c), wp);
         grad[off[l] + b * d[l] + i] = mk - wp;
       }
       tm.sync();
     }
   }
 
-  // -------------------------------------------------------------------------
-  // J^T J v for the owned columns (GaussNewton.py:371-377, 551-581):
-  //   A_k = D_k^T W_k,  Y_l = sum_{k != l} P2[l][k] o A_k,
-  //   z_l = W_l Y_l + D_l P1_l.
-  // -------------------------------------------------------------------------
-  __device__ void matvec(const T* Din, T* zout) {
-    for (int k = 0; k < L; ++k) {
-      const int dk = d[k], ok = off[k];
-      T* dst = sAk + (size_t)k * R * ncol;
-      gemm(
-          R, ncol, dk, [&](int m, int kk) { return Din[ok + m * dk + kk]; },
-          [&](int kk, int n) { return W[ok + (c0 + n) * dk + kk]; },
-          [&](int m, int n, T v) { dst[m * ncol + n] = v; });
-    }
-    __syncthreads();
-    for (int e = tid; e < L * R * ncol; e += TFX_THREADS) {
-      const int l = e / (R * ncol), q = e - l * (R * ncol), a = q / ncol, c = q - a * ncol;
-      T acc = T(0);
-      for (int k = 0; k < L; ++k)
-        if (k != l) acc += P2[((size_t)(l * L + k) * R + a) * R + c0 + c] * sAk[((size_t)k * R + a) * ncol + c];
-      sY[e] = acc;
-    }
-    __syncthreads();
-    for (int l = 0; l < L; ++l) {
-      const int dl = d[l], ol = off[l];
-      const T* Yl = sY + (size_t)l * R * ncol;
-      const T* P1l = P1 + (size_t)l * R * R;
-      gemm(
-          dl, ncol, 2 * R,
-          [&](int m, int kk) { return kk < R ? W[ol + kk * dl + m] : Din[ol + (kk - R) * dl + m]; },
-          [&](int kk, int n) { return kk < R ? Yl[kk * ncol + n] : P1l[(kk - R) * R + c0 + n]; },
-          [&](int m, int n, T v) { zout[ol + (c0 + n) * dl + m] = v; });
-    }
-    __syncthreads();
-  }
-
-  // -------------------------------------------------------------------------
-  // Preconditioned CG (GaussNewton.py:315-398), reference quirks included:
-  // the first new direction is (1+beta) r because P aliases the residual.
-  // -------------------------------------------------------------------------
+  // CG inner solve (see cg_team above)
+  CgOffsets cgo;
+  long long* cprof;  // optional CG sub-phase timers (rank 0, thread 0)
   __device__ int cg(int budget, double& rn_out) {
-    matvec(grad, jtj);
-    double v[4] = {0.0, 0.0, 0.0, 0.0};
-    for_own([&](int e, int l, int c) {
-      const T rr = sM[l * ncol + c] * grad[e];
-      r[e] = rr;
-      P[e] = rr;
-      y[e] = T(0);
-      v[0] += (double)rr * (double)rr;
-    });
-    team_sum<4>(tm, v, rs4, flip4);
-    double rn = v[0];
-    if (rn == 0.0) rn = 1e-6;
-    int maxit = budget;
-    double tol = op.cg_tol;
-    if (nx > 100) {
-      maxit = min(maxit, nx);
-    } else {
-      tol = 0.0;
-    }
-    int itn = 0;
-    bool broke = false;
-    for (itn = 0; itn < maxit; ++itn) {
-      for_own([&](int e, int l, int c) { Q[e] = sM[l * ncol + c] * P[e]; });
-      tm.sync();
-      matvec(Q, z);
-      double w[4] = {0.0, 0.0, 0.0, 0.0};
-      for_own([&](int e, int l, int c) {
-        const T zz = sM[l * ncol + c] * (z[e] + sDG[l * ncol + c] * Q[e]);
-        z[e] = zz;
-        w[0] += (double)P[e] * (double)zz;
-      });
-      team_sum<4>(tm, w, rs4, flip4);
-      double den = w[0];
-      if (den == 0.0) den = 1e-6;
-      const double alpha = rn / den;
-      const T ta = (T)alpha;
-      double u[4] = {0.0, 0.0, 0.0, 0.0};
-      for_own([&](int e, int l, int c) {
-        y[e] += ta * P[e];
-        const T rr = r[e] - ta * z[e];
-        r[e] = rr;
-        u[0] += (double)rr * (double)rr;
-      });
-      team_sum<4>(tm, u, rs4, flip4);
-      const double rn_new = u[0];
-      const double beta = rn_new / rn;
-      rn = rn_new;
-      const T tb = (T)beta;
-      if (itn == 0) {
-        for_own([&](int e, int l, int c) { P[e] = r[e] + tb * r[e]; });
-      } else {
-        for_own([&](int e, int l, int c) { P[e] = r[e] + tb * P[e]; });
-      }
-      if (rn <= tol) {
-        broke = true;
-        break;
-      }
-    }
-    // make every owned entry written in this phase visible before the update
-    __syncthreads();
-    rn_out = rn;
-    return broke ? itn + 1 : maxit;
+    if (stage)
+      return cg_team<T, true>(tm, L, R, nx, ncol, c0, cgo, grad, jtj, y, r, P, Q, z, W, P1, P2, budget, op.cg_tol,
+                              rn_out, flip1, cprof);
+    return cg_team<T, false>(tm, L, R, nx, ncol, c0, cgo, grad, jtj, y, r, P, Q, z, W, P1, P2, budget, op.cg_tol,
+                             rn_out, flip1, cprof);
   }
 
   // Column balancing of x into the factor buffer (Conversion.py:361-387),
@@ -449,22 +726,25 @@ struct Engine {
       for (int p = wid; p < L * ncol; p += TFX_THREADS / 32) {
         const int l = p / ncol, c = p - l * ncol;
         const T* col = src + off[l] + (c0 + c) * d[l];
-        double s = 0.0;
-        for (int i = lane; i < d[l]; i += 32) s += (double)col[i] * (double)col[i];
-        s = warp_sum(s);
-        if (lane == 0) sNorm[p] = sqrt(s);
+        Acc<T> s;
+        for (int i = lane; i < d[l]; i += 32) s.fma_(col[i], col[i]);
+        s.warp_reduce();
+        if (lane == 0) sNorm[p] = sqrt(s.value());
       }
       __syncthreads();
-      for_own([&](int e, int l, int c) {
+      // one balancing factor per (mode, column): (prod_m n_m)^(1/L) / n_l
+      for (int c = tid; c < ncol; c += TFX_THREADS) {
         double prod = 1.0;
         for (int m = 0; m < L; ++m) prod *= sNorm[m * ncol + c];
         if (prod != 0.0) {
           const double num = pow(prod, 1.0 / (double)L);
-          dst[e] = (T)((num / sNorm[l * ncol + c]) * (double)src[e]);
+          for (int m = 0; m < L; ++m) sScale[m * ncol + c] = (T)(num / sNorm[m * ncol + c]);
         } else {
-          dst[e] = src[e];
+          for (int m = 0; m < L; ++m) sScale[m * ncol + c] = T(1);
         }
-      });
+      }
+      __syncthreads();
+      for_own([&](int e, int l, int c) { dst[e] = sScale[l * ncol + c] * src[e]; });
     } else {
       for_own([&](int e, int l, int c) { dst[e] = src[e]; });
     }
@@ -552,7 +832,7 @@ struct Engine {
           const int m = m0 + ty + 16 * u;
           const long long q = q0 + tx + 16 * v;
           if (m < d[0] && q < Q0) {
-            const T df = Tt[(long long)m * Q0 + q] - acc[u][v];
+            const T df = __ldg(Tt + (long long)m * Q0 + q) - acc[u][v];
             ps = fma(df, df, ps);
           }
         }
@@ -640,8 +920,9 @@ struct Engine {
       __syncthreads();
       to_factors(xn, W, false);
       tm.sync();
+      stage_W();
       team_sum<4>(tm, s, rs4, flip4);
-      error = rel_error(W);
+      error = rel_error(Wr);
       const double num = (Tsize * Tsize) * (old_error * old_error - error * error);
       if (s[0] != 0.0) {
         gain = num / s[0];
@@ -676,6 +957,7 @@ struct Engine {
     });
     __syncthreads();
     tm.sync();
+    stage_W();
     return best_error;
   }
 };
@@ -684,6 +966,9 @@ template <class T, int TS>
 __device__ void solve_problem(const tfx_dgn_problem& pb, const tfx_dgn_options& op, Team tm, char* smem,
                               const SmemPlan& sp) {
   Engine<T, TS> E;
+  E.d = (int*)(smem + sp.misc + 64);
+  E.off = E.d + TFX_MAX_ORDER;
+  E.st = (long long*)(smem + sp.misc + 64 + 4 * TFX_MAX_ORDER * 8);
   E.tm = tm;
   E.tid = threadIdx.x;
   E.op = op;
@@ -693,19 +978,24 @@ __device__ void solve_problem(const tfx_dgn_problem& pb, const tfx_dgn_options& 
   E.N = 1;
   E.maxd = 0;
   for (int l = 0; l < E.L; ++l) {
-    E.d[l] = pb.dims[l];
-    E.off[l] = E.R * sumd;
+    if (threadIdx.x == 0) {
+      E.d[l] = pb.dims[l];
+      E.off[l] = E.R * sumd;
+    }
     sumd += pb.dims[l];
     E.N *= pb.dims[l];
     E.maxd = max(E.maxd, pb.dims[l]);
   }
-  E.off[E.L] = E.R * sumd;
-  E.nx = E.R * sumd;
-  long long s = 1;
-  for (int l = E.L - 1; l >= 0; --l) {
-    E.st[l] = s;
-    s *= E.d[l];
+  if (threadIdx.x == 0) {
+    E.off[E.L] = E.R * sumd;
+    long long s = 1;
+    for (int l = E.L - 1; l >= 0; --l) {
+      E.st[l] = s;
+      s *= pb.dims[l];
+    }
   }
+  E.nx = E.R * sumd;
+  __syncthreads();
   E.c0 = (int)((long long)E.R * tm.rank / tm.size);
   E.c1 = (int)((long long)E.R * (tm.rank + 1) / tm.size);
   E.ncol = E.c1 - E.c0;
@@ -742,6 +1032,28 @@ __device__ void solve_problem(const tfx_dgn_problem& pb, const tfx_dgn_options& 
   E.rs4 = (RedScratch<4>*)(smem + sp.rs4);
   E.rs12 = (RedScratch<TFX_MAX_ORDER>*)(smem + sp.rs12);
   E.sMisc = (double*)(smem + sp.misc);
+  E.stage = sp.stage;
+  E.sQf = (T*)(smem + sp.sQf);
+  E.sWf = (T*)(smem + sp.sWf);
+  E.sP1o = (T*)(smem + sp.sP1o);
+  E.sP2o = (T*)(smem + sp.sP2o);
+  E.Wr = E.W;
+  E.cgo.d = sp.misc + 64;
+  E.cgo.sQf = sp.sQf;
+  E.cgo.sWf = sp.sWf;
+  E.cgo.sP1o = sp.sP1o;
+  E.cgo.sP2o = sp.sP2o;
+  E.cgo.sAk = sp.sAk;
+  E.cgo.sY = sp.sY;
+  E.cgo.sM = sp.sM;
+  E.cgo.sDG = sp.sDG;
+  E.cgo.rs4 = sp.rs4;
+  E.cgo.rs1 = sp.rs1;
+  E.cgo.sVec = sp.sVec;
+  E.rs1b = (RedScratch<1>*)(smem + sp.rs1b);
+  E.sScale = (T*)(smem + sp.sScale);
+  E.flip1 = 0;
+  E.flip1b = 0;
   E.flip4 = 0;
   E.flip12 = 0;
 
@@ -776,13 +1088,29 @@ __device__ void solve_problem(const tfx_dgn_problem& pb, const tfx_dgn_options& 
   double error = 1.0, best_error = INFINITY;
   int stop = 5, it = 0, n_dogleg = 0;
   E.tm.sync();
+  E.stage_W();
 
+  // optional phase timers (rank 0, thread 0): SM clock cycles per phase
+  long long* prof = (E.tm.rank == 0 && threadIdx.x == 0) ? pb.prof : nullptr;
+  E.cprof = prof ? prof + 8 : nullptr;
+  long long tclk = clock64(), t_start = tclk;
+  auto tick = [&](int ph) {
+    if (prof) {
+      const long long now = clock64();
+      prof[ph] += now - tclk;
+      tclk = now;
+    }
+  };
   for (it = 0; it < maxiter; ++it) {
     const double old_error = error;
+    tick(6);
     E.gramians_and_precond();
+    tick(0);
     E.gradient();
+    tick(1);
     double rn;
     E.cg(pb.budgets[it], rn);
+    tick(2);
     // y <- M y ; xn <- x + y ; W <- balanced(xn)
     E.for_own([&](int e, int l, int c) {
       const T yy = E.sM[l * E.ncol + c] * E.y[e];
@@ -792,24 +1120,29 @@ __device__ void solve_problem(const tfx_dgn_problem& pb, const tfx_dgn_options& 
     __syncthreads();
     E.to_factors(E.xn, E.W, true);
     E.tm.sync();
-    error = E.rel_error(E.W);
+    E.stage_W();
+    tick(3);
+    error = E.rel_error(E.Wr);
+    tick(4);
     if (it > 3 && error > op.tol_jump * old_error) {
       error = E.dogleg(error);
       ++n_dogleg;
     }
+    tick(5);
     // gain ratio, step size, gradient norm (x_new - x_old with the final x)
-    double v[4] = {0.0, 0.0, 0.0, 0.0};
-    double gm[4] = {0.0, 0.0, 0.0, 0.0};
-    const double dmp = E.damp;
+    Acc<T> va[4];
+    MaxAcc<T> ga[1];
+    double v[4], gm[1];
+    const T dmp = (T)E.damp;
     E.for_own([&](int e, int l, int c) {
-      const double dx = (double)E.xn[e] - (double)E.xc[e];
-      v[0] += dx * ((double)E.grad[e] + dmp * dx);
-      v[1] += dx * dx;
-      v[2] += (double)E.xc[e] * (double)E.xc[e];
-      gm[0] = fmax(gm[0], fabs((double)E.grad[e]));
+      const T dx = E.xn[e] - E.xc[e];
+      va[0].fma_(dx, E.grad[e] + dmp * dx);
+      va[1].fma_(dx, dx);
+      va[2].fma_(E.xc[e], E.xc[e]);
+      ga[0].v = fmax(ga[0].v, fabs(E.grad[e]));
     });
-    team_sum<4>(E.tm, v, E.rs4, E.flip4);
-    team_max<4>(E.tm, gm, E.rs4, E.flip4);
+    team_sum_acc<4, T>(E.tm, va, v, E.rs4, E.flip4);
+    team_reduce_acc<1, true>(E.tm, ga, gm, E.rs1b, E.flip1b);
     const double num = (Tsize * Tsize) * (old_error * old_error - error * error);
     double gain;
     if (v[0] != 0.0) {
@@ -871,6 +1204,8 @@ __device__ void solve_problem(const tfx_dgn_problem& pb, const tfx_dgn_options& 
     }
   }
   const int iters = (it < maxiter) ? it + 1 : maxiter;
+  tick(6);
+  if (prof) prof[7] += clock64() - t_start;
   E.tm.sync();
   if (E.tm.rank == 0 && threadIdx.x == 0) {
     pb.result[0] = stop;
@@ -912,6 +1247,7 @@ static int launch_dgn(const tfx_dgn_problem* d_probs, int nprob, const tfx_dgn_o
   cudaError_t e = cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sp.total);
   if (e != cudaSuccess) return tfx_set_cuda_error(e, "dgn smem attribute");
   if (cluster > 8) {
+    // clusters of 9..16 CTAs are beyond the portable size
     e = cudaFuncSetAttribute(kfn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
     if (e != cudaSuccess) return tfx_set_cuda_error(e, "dgn cluster attribute");
   }

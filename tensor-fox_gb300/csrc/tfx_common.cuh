@@ -58,65 +58,153 @@ __device__ __forceinline__ double warp_max(double v) {
   return v;
 }
 
-// Reduction scratch living in shared memory: per-warp partials and a
-// double-buffered per-CTA slot read by the peers of the team.
+// ---------------------------------------------------------------------------
+// Accumulators.  GB300 executes FP64 at a small fraction of its FP32 rate, so
+// the FP32 path accumulates sums in float-float form (an unevaluated pair
+// hi + lo with |lo| <= ulp(hi)/2, combined with Knuth's TwoSum and exact FMA
+// products: about 48 significant bits).  The FP64 path accumulates in double.
+// ---------------------------------------------------------------------------
+template <class T>
+struct Acc;
+
+template <>
+struct Acc<float> {
+  float hi, lo;
+  __device__ __forceinline__ Acc() : hi(0.f), lo(0.f) {}
+  __device__ __forceinline__ void add2(float bh, float bl) {
+    const float s = hi + bh;
+    const float bb = s - hi;
+    float err = (hi - (s - bb)) + (bh - bb);
+    err += lo + bl;
+    hi = s + err;
+    lo = err - (hi - s);
+  }
+  __device__ __forceinline__ void add(float x) { add2(x, 0.f); }
+  __device__ __forceinline__ void fma_(float x, float y) {
+    const float p = x * y;
+    add2(p, fmaf(x, y, -p));
+  }
+  __device__ __forceinline__ double value() const { return (double)hi + (double)lo; }
+  __device__ __forceinline__ void warp_reduce() {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const float oh = __shfl_xor_sync(0xffffffffu, hi, o);
+      const float ol = __shfl_xor_sync(0xffffffffu, lo, o);
+      add2(oh, ol);
+    }
+  }
+};
+
+template <>
+struct Acc<double> {
+  double v;
+  __device__ __forceinline__ Acc() : v(0.0) {}
+  __device__ __forceinline__ void add(double x) { v += x; }
+  __device__ __forceinline__ void fma_(double x, double y) { v = fma(x, y, v); }
+  __device__ __forceinline__ double value() const { return v; }
+  __device__ __forceinline__ void warp_reduce() { v = warp_sum(v); }
+};
+
+// Reduction scratch living in shared memory: per-warp partials, a
+// double-buffered per-CTA slot read by the peers of the team, and the team's
+// totals broadcast to the CTA.
+#define TFX_MAX_TEAM 16
 template <int NV>
 struct RedScratch {
   double warp[TFX_THREADS / 32][NV];
   double part[2][NV];
+  double tot[NV];
 };
 
-// Sums NV per-thread values over the whole team; every thread of every CTA
-// returns the same totals.  `flip` alternates the slot buffer so that only one
-// team barrier is needed per call.
-template <int NV>
-__device__ __forceinline__ void team_sum(const Team& tm, double (&v)[NV], RedScratch<NV>* rs, int& flip) {
+// Team-wide sum (or max) of NV per-thread values; every thread of every CTA
+// returns the same totals.  Warps reduce first, then one thread per value
+// combines the warps, the CTAs' partials are read from distributed shared
+// memory by one thread per value and summed in rank order.  `flip`
+// alternates the slot buffer so that one team barrier per call suffices.
+template <int NV, bool MAX, class A>
+__device__ __forceinline__ void team_reduce_acc(const Team& tm, A (&v)[NV], double (&out)[NV], RedScratch<NV>* rs,
+                                                int& flip) {
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
 #pragma unroll
   for (int j = 0; j < NV; ++j) {
-    double s = warp_sum(v[j]);
-    if (lane == 0) rs->warp[wid][j] = s;
-  }
-  __syncthreads();
-  if (threadIdx.x < NV) {
-    double s = 0.0;
-    for (int w = 0; w < TFX_THREADS / 32; ++w) s += rs->warp[w][threadIdx.x];
-    rs->part[flip][threadIdx.x] = s;
-  }
-  tm.sync();
-#pragma unroll
-  for (int j = 0; j < NV; ++j) {
-    double s = 0.0;
-    for (int r = 0; r < tm.size; ++r) s += tm.peer(&rs->part[flip][0], r)[j];
-    v[j] = s;
-  }
-  flip ^= 1;
-  __syncthreads();  // warp slots may be rewritten by the next call
-}
-
-template <int NV>
-__device__ __forceinline__ void team_max(const Team& tm, double (&v)[NV], RedScratch<NV>* rs, int& flip) {
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-#pragma unroll
-  for (int j = 0; j < NV; ++j) {
-    double s = warp_max(v[j]);
-    if (lane == 0) rs->warp[wid][j] = s;
+    v[j].warp_reduce();
+    if (lane == 0) rs->warp[wid][j] = v[j].value();
   }
   __syncthreads();
   if (threadIdx.x < NV) {
     double s = rs->warp[0][threadIdx.x];
-    for (int w = 1; w < TFX_THREADS / 32; ++w) s = fmax(s, rs->warp[w][threadIdx.x]);
+    for (int w = 1; w < TFX_THREADS / 32; ++w) s = MAX ? fmax(s, rs->warp[w][threadIdx.x]) : s + rs->warp[w][threadIdx.x];
     rs->part[flip][threadIdx.x] = s;
   }
   tm.sync();
+  if (threadIdx.x < NV) {
+    const int j = threadIdx.x;
+    double pv[TFX_MAX_TEAM];
 #pragma unroll
-  for (int j = 0; j < NV; ++j) {
-    double s = tm.peer(&rs->part[flip][0], 0)[j];
-    for (int r = 1; r < tm.size; ++r) s = fmax(s, tm.peer(&rs->part[flip][0], r)[j]);
-    v[j] = s;
+    for (int r = 0; r < TFX_MAX_TEAM; ++r) pv[r] = r < tm.size ? tm.peer(&rs->part[flip][0], r)[j] : 0.0;
+    double s = pv[0];
+#pragma unroll
+    for (int r = 1; r < TFX_MAX_TEAM; ++r)
+      if (r < tm.size) s = MAX ? fmax(s, pv[r]) : s + pv[r];
+    rs->tot[j] = s;
   }
-  flip ^= 1;
   __syncthreads();
+#pragma unroll
+  for (int j = 0; j < NV; ++j) out[j] = rs->tot[j];
+  flip ^= 1;
+  __syncthreads();  // tot and warp slots may be rewritten by the next call
+}
+
+struct DAcc {  // plain double accumulator used by the double-valued wrappers
+  double v;
+  __device__ __forceinline__ void warp_reduce() { v = warp_sum(v); }
+  __device__ __forceinline__ double value() const { return v; }
+};
+struct DMax {
+  double v;
+  __device__ __forceinline__ void warp_reduce() { v = warp_max(v); }
+  __device__ __forceinline__ double value() const { return v; }
+};
+template <class T>
+struct MaxAcc {  // running maximum in the working precision
+  T v;
+  __device__ __forceinline__ MaxAcc() : v(T(0)) {}
+  __device__ __forceinline__ void warp_reduce() {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+  }
+  __device__ __forceinline__ double value() const { return (double)v; }
+};
+
+template <int NV, bool MAX>
+__device__ __forceinline__ void team_reduce(const Team& tm, double (&v)[NV], RedScratch<NV>* rs, int& flip) {
+  if (MAX) {
+    DMax a[NV];
+#pragma unroll
+    for (int j = 0; j < NV; ++j) a[j].v = v[j];
+    team_reduce_acc<NV, true>(tm, a, v, rs, flip);
+  } else {
+    DAcc a[NV];
+#pragma unroll
+    for (int j = 0; j < NV; ++j) a[j].v = v[j];
+    team_reduce_acc<NV, false>(tm, a, v, rs, flip);
+  }
+}
+
+template <int NV, class T>
+__device__ __forceinline__ void team_sum_acc(const Team& tm, Acc<T> (&v)[NV], double (&out)[NV], RedScratch<NV>* rs,
+                                             int& flip) {
+  team_reduce_acc<NV, false>(tm, v, out, rs, flip);
+}
+
+template <int NV>
+__device__ __forceinline__ void team_sum(const Team& tm, double (&v)[NV], RedScratch<NV>* rs, int& flip) {
+  team_reduce<NV, false>(tm, v, rs, flip);
+}
+
+template <int NV>
+__device__ __forceinline__ void team_max(const Team& tm, double (&v)[NV], RedScratch<NV>* rs, int& flip) {
+  team_reduce<NV, true>(tm, v, rs, flip);
 }
 
 // ---------------------------------------------------------------------------
@@ -124,7 +212,7 @@ __device__ __forceinline__ void team_max(const Team& tm, double (&v)[NV], RedScr
 // block of a (16*TM) x (16*TN) output tile.  A chunk is staged k-major in shared
 // memory: sA[k][m] (ld = BM+1) and sB[k][n] (ld = BN+1).
 // ---------------------------------------------------------------------------
-#define TFX_BK 16
+#define TFX_BK 32
 
 template <int TM, int TN>
 struct Tile {

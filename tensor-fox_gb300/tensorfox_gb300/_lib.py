@@ -22,7 +22,7 @@ class DgnProblem(ctypes.Structure):
     _fields_ = [("L", c_int), ("R", c_int), ("dims", c_int * MAX_ORDER),
                 ("tensor", c_void_p), ("x", c_void_p), ("best", c_void_p), ("work", c_void_p),
                 ("budgets", c_void_p), ("damp_sched", c_void_p), ("stats", c_void_p),
-                ("result", c_void_p), ("info", c_void_p)]
+                ("result", c_void_p), ("info", c_void_p), ("prof", c_void_p)]
 
 
 class DgnOptions(ctypes.Structure):

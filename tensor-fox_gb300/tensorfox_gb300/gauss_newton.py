@@ -51,17 +51,18 @@ def advance_rng(options, iterations):
 
 
 def auto_cluster(dims, R):
+    """CTAs per problem (one thread-block cluster): about one CTA per 1.2 million
+    multiply-adds of per-iteration MTTKRP work, at most 16 and at most R (every
+    CTA owns whole factor columns).  Measured on the 50^3, R=50 core of a
+    512^3 problem: 16 CTAs beat 10 and 8 despite the uneven column split."""
     n = int(np.prod(dims))
     work = n * R * len(dims)
-    for c, lim in ((1, 2e6), (2, 8e6), (4, 3e7), (8, 1e8)):
-        if work < lim:
-            return max(1, min(c, R))
-    return max(1, min(16, R))
+    return int(max(1, min(16, R, work // 1200000)))
 
 
 def _cluster_candidates(c, R):
-    cands = [x for x in (1, 2, 4, 8, 16) if x >= c and x <= max(R, 1)]
-    return cands or [1]
+    cands = [c] + [x for x in (1, 2, 4, 8, 12, 16) if x > c and x <= max(R, 1)]
+    return [x for x in cands if x <= max(R, 1)] or [1]
 
 
 class _Batch:
@@ -94,6 +95,7 @@ class _Batch:
         self.stats = torch.zeros((self.n, 4 * self.maxiter), dtype=torch.float64, device=tensors[0].device)
         self.result = torch.zeros((self.n, 4), dtype=torch.int32, device=tensors[0].device)
         self.info = torch.zeros((self.n, 4), dtype=torch.float64, device=tensors[0].device)
+        self.prof = torch.zeros((self.n, 16), dtype=torch.int64, device=tensors[0].device)
         self.desc = (_lib.DgnProblem * self.n)()
         for p in range(self.n):
             d = self.desc[p]
@@ -110,6 +112,7 @@ class _Batch:
             d.stats = _dev.ptr(self.stats[p])
             d.result = _dev.ptr(self.result[p])
             d.info = _dev.ptr(self.info[p])
+            d.prof = _dev.ptr(self.prof[p])
         self.d_desc = torch.empty(ctypes.sizeof(_lib.DgnProblem) * self.n, dtype=torch.uint8,
                                   device=tensors[0].device)
         o = _lib.DgnOptions()
