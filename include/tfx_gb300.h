@@ -1,0 +1,106 @@
+/* C ABI of libtfx_gb300.so: Tensor Fox's damped Gauss-Newton CPD path on GB300.
+ *
+ * Every pointer argument is a device pointer owned by the caller unless stated
+ * otherwise; every function enqueues work on `stream` (a cudaStream_t, NULL for
+ * the legacy stream) and returns a tfx_status.  No function throws; on failure
+ * tfx_last_error() returns a message for the calling thread.  Tensors are dense
+ * C-order arrays; factor matrices use the reference's flat layout
+ * concat_l vec_F(W_l) unless a function says "row-major".  dtype is TFX_F32 or
+ * TFX_F64.  Scratch buffers are caller-owned; *_scratch_bytes() give their size.
+ *
+ * Reference interfaces (Tensor Fox 1.2.1, modules/TensorFox/) replaced here are
+ * named beside each entry point.
+ */
+#ifndef TFX_GB300_H
+#define TFX_GB300_H
+
+#include <stddef.h>
+
+#include "tfx_gb300_types.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- library ------------------------------------------------------------ */
+const char* tfx_last_error(void);
+long long tfx_launch_count(void); /* kernels enqueued by this library so far */
+int tfx_version(void);
+
+/* ---- damped Gauss-Newton ------------------------------------------------
+ * GaussNewton.py:29 dGN(T, factors, R, options) -> (best_factors, step_sizes,
+ * errors, improv, gradients, stop), for a batch of independent problems: one
+ * thread-block cluster of `cluster` CTAs (1..16) per problem runs every
+ * iteration on the device (GaussNewton.py:254-398, 472-517, 713-795).
+ * h_probs: host array; d_probs: device buffer of nprob descriptors. */
+size_t tfx_dgn_workspace_bytes(int dtype, int L, const int* dims, int R);
+int tfx_dgn_solve(int dtype, const tfx_dgn_problem* h_probs, tfx_dgn_problem* d_probs, int nprob,
+                  const tfx_dgn_options* options, int cluster, void* stream);
+
+/* ---- compression (MLSVD) --------------------------------------------------
+ * Compression.py:192-237 compute_svd / 400-518 randomized_svd: the unfolding's
+ * Gram S_(l) S_(l)^T (D x D) of a C-order tensor viewed as (P, D, Q). */
+size_t tfx_mode_gram_scratch_bytes(int dtype, long long P, int D, long long Q);
+int tfx_mode_gram(int dtype, const void* S, long long P, int D, long long Q, void* G, void* scratch,
+                  size_t scratch_bytes, void* stream);
+/* Strided batched C = alpha*A*B + beta*C (mode products of Compression.py:153-156
+ * and MultilinearAlgebra.py:72-105, TensorFox.py:573-574 U_l W_l).
+ * strides = {sAb, sAm, sAk, sBb, sBk, sBn, sCb, sCm, sCn} (elements). */
+int tfx_gemm(int dtype, const void* A, const void* B, void* C, long long M, long long N, long long K, long long batch,
+             const long long* strides, double alpha, double beta, void* stream);
+/* Orthonormal basis of the k columns of Y (D x k column-major), in place
+ * (scipy qr in Compression.py:392). */
+int tfx_orthonormalize(int dtype, void* Y, int D, int k, void* stream);
+/* Eigen-decomposition of a symmetric n x n matrix: eigenvalues descending,
+ * eigenvectors as rows of V (scipy svd of Compression.py:501). */
+size_t tfx_sym_eig_smem_bytes(int dtype, int n);
+int tfx_sym_eig(int dtype, const void* A, int n, void* evals, void* V, int max_sweeps, int* sweeps, void* stream);
+/* svd_flip (Compression.py:521-564): the largest |entry| of every column of
+ * U (D x n column-major) becomes positive. */
+int tfx_flip_signs(int dtype, void* U, int D, int n, void* stream);
+
+/* ---- full-tensor residual ------------------------------------------------
+ * Critical.py:14-22 fastnorm(T1, cpd2unfold1(factors))^2 (Conversion.py:117-141),
+ * fused: *out = ||T - [[W]]||^2 (double). */
+size_t tfx_cp_residual_scratch_bytes(void);
+int tfx_cp_residual(int dtype, const void* T, int L, const int* dims, int R, const void* W, double* out, void* scratch,
+                    void* stream);
+/* norm(T)^2 and sum|T| (TensorFox.py:503, GaussNewton.py:113) into out2[0..1]. */
+int tfx_tensor_norms(int dtype, const void* T, long long N, double* out2, void* scratch, void* stream);
+
+/* ---- sparse (COO) ----------------------------------------------------------
+ * TensorFox.py:476-481: int64 (nnz x L) coordinates -> int32 L x nnz; *err = 1
+ * when a coordinate is out of range. */
+int tfx_coo_encode(const long long* idx64, long long nnz, int L, const int* dims, int* idx32, int* err, void* stream);
+/* Conversion.py:255-302 sparse_unfold: entries grouped by their mode-`mode`
+ * index (rowptr[d+1], permuted copies).  counts_scratch: 2*d ints. */
+int tfx_coo_sort_mode(int dtype, const int* idx32, const void* vals, long long nnz, int L, const int* dims, int mode,
+                      int* counts_scratch, long long* rowptr, int* sidx, void* svals, void* stream);
+/* COO MTTKRP T_(l) (KR of the other factors) -> out (d_mode x R row-major);
+ * Wrow_dev: device array of L pointers to row-major (d_m x R) factors.  The
+ * reference forms this product only through dense unfoldings
+ * (GaussNewton.py:401-427 on sparse2dense, Conversion.py:144-164). */
+int tfx_coo_mttkrp(int dtype, const int* sidx, const void* svals, long long nnz, const long long* rowptr, int L,
+                   const int* dims, int R, int mode, const void* const* Wrow_dev, void* out, void* stream);
+/* Critical.py:25-53 sparse_fastnorm^2: *out = sum over stored entries of
+ * (value - model)^2. */
+size_t tfx_sparse_residual_scratch_bytes(void);
+int tfx_sparse_residual(int dtype, const int* idx32, const void* vals, long long nnz, int L, const int* dims, int R,
+                        const void* const* Wrow_dev, double* out, void* scratch, void* stream);
+/* Compression.py:211-215 with 240-258 (dot_product_mkl(Tl, Tl.T)): dense
+ * T_(l) T_(l)^T from COO; *err = 2 if the fibre hash table overflows. */
+size_t tfx_coo_gram_scratch_bytes(long long nnz, int d);
+int tfx_coo_gram(int dtype, const int* idx32, const void* vals, long long nnz, const void* svals_sorted,
+                 const long long* rowptr, int L, const int* dims, int mode, void* G, void* scratch, size_t scratch_bytes,
+                 int* err, void* stream);
+/* MultilinearAlgebra.py:145-190 sparse_multilin_mult (Critical.py:2703-2720):
+ * dense core S (n_0 x ... x n_{L-1}) = T x_1 U_1^T ... ; U_dev: device array of
+ * L pointers to row-major (d_l x n_l) matrices. */
+size_t tfx_sparse_ttmc_scratch_bytes(int dtype, long long nnz, int L, const int* n);
+int tfx_sparse_ttmc(int dtype, const int* idx32, const void* vals, long long nnz, int L, const int* dims, const int* n,
+                    const void* const* U_dev, void* S, void* scratch, size_t scratch_bytes, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -134,10 +134,11 @@ def mlsvd(T, Tsize, R, options=None):
     _dev.require_cuda()
     o = make_options(options) if not hasattr(options, 'bi_method_parameters') else options
     if isinstance(T, list):
-        from .sparse import mlsvd_sparse_device
+        from .sparse import DeviceCOO, mlsvd_sparse_device
         data, idxs, dims = T
-        S, Uts, sigmas = mlsvd_sparse_device(data, idxs, dims, R, o)
-        from scipy.sparse import coo_matrix  # noqa: F401  (T1 is the sparse unfolding, built on request)
+        prec = o.precision if o.precision in ('fp64', 'fp32') else 'fp64'
+        X = DeviceCOO(data, idxs, dims, _dev.torch_dtype(prec))
+        S, Uts, sigmas = mlsvd_sparse_device(X, R, o)
         T1 = None
     else:
         prec = o.precision or ('fp64' if np.asarray(T).dtype == np.float64 else 'fp32')

@@ -1,0 +1,205 @@
+"""Sparse (COO) tensors on the device (TensorFox.py:476-481, Compression.py:123-137,
+Critical.py:25-53, MultilinearAlgebra.py:145-190).
+
+A sparse tensor is given as ``[data, idxs, dims]`` like in Tensor Fox.  On the
+device the coordinates are re-encoded once to int32 structure-of-arrays
+(``tfx_coo_encode``, bounds-checked) and per-mode row-sorted copies are built on
+demand (``tfx_coo_sort_mode``).
+
+``tricpd_sparse`` follows the reference's semantics exactly: absent entries are
+zeros of the data, the MLSVD works on the dense Gram ``T_(l) T_(l)^T`` of every
+unfolding, the core is the sparse multilinear product, dGN runs on the dense
+core and the final error counts the stored entries only.
+"""
+import ctypes
+
+import numpy as np
+import torch
+
+from . import _dev, _lib, kernels
+from .compression import clean_compression, top_eig, _draw_omega
+from .gauss_newton import _Batch, advance_rng, auto_cluster
+from .options import make_options
+
+
+def _vp(t):
+    return ctypes.c_void_p(_dev.ptr(t))
+
+
+def _st():
+    return ctypes.c_void_p(_dev.stream())
+
+
+def _cint(vals):
+    vals = [int(v) for v in vals]
+    return (ctypes.c_int * len(vals))(*vals)
+
+
+class DeviceCOO:
+    """COO tensor resident on the device: int32 SoA coordinates and values."""
+
+    def __init__(self, data, idxs, dims, dtype):
+        dims = [int(d) for d in dims]
+        self.dims = dims
+        self.L = len(dims)
+        if max(dims) >= 2 ** 31:
+            raise ValueError("dimensions must be below 2^31")
+        dev = _dev.device()
+        idx = torch.as_tensor(np.ascontiguousarray(np.asarray(idxs, dtype=np.int64).reshape(-1, self.L)),
+                              device=dev)
+        self.nnz = int(idx.shape[0])
+        self.vals = torch.as_tensor(np.asarray(data, dtype=np.float64), device=dev).to(dtype).contiguous()
+        self.idx32 = torch.empty((self.L, max(self.nnz, 1)), dtype=torch.int32, device=dev)
+        err = torch.zeros(1, dtype=torch.int32, device=dev)
+        _lib.call("tfx_coo_encode", _vp(idx), self.nnz, self.L, _cint(dims), _vp(self.idx32), _vp(err), _st())
+        if int(err.item()) != 0:
+            raise ValueError("sparse index out of range")
+        self.sorted = {}
+
+    def dt(self):
+        return _lib.F64 if self.vals.dtype == torch.float64 else _lib.F32
+
+    def sort_mode(self, mode):
+        """(rowptr, sorted int32 SoA coordinates, sorted values) for ``mode``."""
+        if mode not in self.sorted:
+            d = self.dims[mode]
+            dev = self.vals.device
+            counts = torch.empty(2 * d, dtype=torch.int32, device=dev)
+            rowptr = torch.empty(d + 1, dtype=torch.int64, device=dev)
+            sidx = torch.empty_like(self.idx32)
+            svals = torch.empty_like(self.vals)
+            _lib.call("tfx_coo_sort_mode", self.dt(), _vp(self.idx32), _vp(self.vals), self.nnz, self.L,
+                      _cint(self.dims), int(mode), _vp(counts), _vp(rowptr), _vp(sidx), _vp(svals), _st())
+            self.sorted[mode] = (rowptr, sidx, svals)
+        return self.sorted[mode]
+
+    def gram(self, mode):
+        """Dense T_(l) T_(l)^T (d_l x d_l) on the device."""
+        rowptr, sidx, svals = self.sort_mode(mode)
+        d = self.dims[mode]
+        lib = _lib.load()
+        nb = int(lib.tfx_coo_gram_scratch_bytes(self.nnz, d))
+        scratch = torch.empty(nb, dtype=torch.uint8, device=self.vals.device)
+        G = torch.empty((d, d), dtype=self.vals.dtype, device=self.vals.device)
+        err = torch.zeros(1, dtype=torch.int32, device=self.vals.device)
+        _lib.call("tfx_coo_gram", self.dt(), _vp(self.idx32), _vp(self.vals), self.nnz, _vp(svals), _vp(rowptr),
+                  self.L, _cint(self.dims), int(mode), _vp(G), _vp(scratch), nb, _vp(err), _st())
+        if int(err.item()) != 0:
+            raise RuntimeError("fibre hash table overflow in the sparse Gram")
+        return G
+
+
+def _row_major_ptrs(factors_rm):
+    arr = torch.tensor([_dev.ptr(w) for w in factors_rm], dtype=torch.int64, device=factors_rm[0].device)
+    return arr
+
+
+def coo_mttkrp(X, factors_rm, mode):
+    """Sparse MTTKRP ``T_(l) (KR of the other factors)`` as a (d_l, R) row-major tensor.
+
+    ``factors_rm`` are the (d_m, R) row-major device factor matrices."""
+    rowptr, sidx, svals = X.sort_mode(mode)
+    R = int(factors_rm[0].shape[1])
+    out = torch.empty((X.dims[mode], R), dtype=X.vals.dtype, device=X.vals.device)
+    ptrs = _row_major_ptrs(factors_rm)
+    _lib.call("tfx_coo_mttkrp", X.dt(), _vp(sidx), _vp(svals), X.nnz, _vp(rowptr), X.L, _cint(X.dims), R, int(mode),
+              _vp(ptrs), _vp(out), _st())
+    return out
+
+
+def sparse_residual_sq(X, factors_rm):
+    """sum over stored entries of (value - model)^2 (float64 device scalar)."""
+    R = int(factors_rm[0].shape[1])
+    lib = _lib.load()
+    scratch = torch.empty(int(lib.tfx_sparse_residual_scratch_bytes()), dtype=torch.uint8, device=X.vals.device)
+    out = torch.empty(1, dtype=torch.float64, device=X.vals.device)
+    ptrs = _row_major_ptrs(factors_rm)
+    _lib.call("tfx_sparse_residual", X.dt(), _vp(X.idx32), _vp(X.vals), X.nnz, X.L, _cint(X.dims), R, _vp(ptrs),
+              _vp(out), _vp(scratch), _st())
+    return out
+
+
+def sparse_ttmc(X, Uts):
+    """Dense core S = T x_1 U_1^T ... from COO; Uts[l] is (n_l, d_l) row-major."""
+    U_rm = [u.t().contiguous() for u in Uts]        # (d_l, n_l) row-major
+    n = [int(u.shape[0]) for u in Uts]
+    lib = _lib.load()
+    nb = int(lib.tfx_sparse_ttmc_scratch_bytes(X.dt(), X.nnz, X.L, _cint(n)))
+    scratch = torch.empty(max(nb, 16), dtype=torch.uint8, device=X.vals.device)
+    S = torch.empty(n, dtype=X.vals.dtype, device=X.vals.device)
+    ptrs = _row_major_ptrs(U_rm)
+    _lib.call("tfx_sparse_ttmc", X.dt(), _vp(X.idx32), _vp(X.vals), X.nnz, X.L, _cint(X.dims), _cint(n), _vp(ptrs),
+              _vp(S), _vp(scratch), nb, _st())
+    return S
+
+
+def mlsvd_sparse_device(X, R, options):
+    """Reference sparse MLSVD (Compression.py:123-137, 211-222) on a DeviceCOO."""
+    o = options
+    L = X.L
+    tol = o.tol_mlsvd
+    if isinstance(tol, list):
+        tol = tol[0] if L > 3 else tol[1]
+    if tol < 0:
+        tol = 1e-16
+    Uts, sigmas = [], []
+    for l in range(L):
+        d = X.dims[l]
+        low = min(R, d)
+        n = o.svd_n_components if o.svd_n_components is not None else int(max(L, np.log10(d * d * L)) * low)
+        omega = _draw_omega(d, n + 10)
+        G = X.gram(l)
+        Ut, lam = top_eig(G, n, omega)
+        # the reference takes sqrt of the Gram's singular values (Compression.py:222)
+        sig = np.sqrt(np.maximum(lam, 0.0))
+        dim = clean_compression(sig, tol, L)
+        Uts.append(Ut[:dim].contiguous())
+        sigmas.append(sig[:dim])
+    S = sparse_ttmc(X, Uts)
+    return S, Uts, sigmas
+
+
+def tricpd_sparse(T, R, options):
+    """``tricpd`` for ``[data, idxs, dims]`` (TensorFox.py:424-655, sparse branches)."""
+    from .api import Output, starting_point_random, _decompress, _run_dgn, unsort_dims
+    o = options
+    if o.method != 'dGN':
+        raise NotImplementedError("method %r is outside the damped Gauss-Newton path" % (o.method,))
+    data, idxs, dims = T
+    data = np.asarray(data, dtype=np.float64)
+    idxs = np.asarray(idxs, dtype=np.int64).reshape(len(data), -1)
+    dims = np.asarray(dims)
+    prec = o.precision if o.precision in ('fp64', 'fp32') else 'fp64'
+    dt = _dev.torch_dtype(prec)
+    ordering = np.argsort(-dims)
+    sdims = dims[ordering]
+    X = DeviceCOO(data, idxs[:, ordering], sdims, dt)
+    Tsize = float(np.linalg.norm(data))
+    S, Uts, sigmas = mlsvd_sparse_device(X, R, o)
+    core = [int(u.shape[0]) for u in Uts]
+    if isinstance(o.initialization, list):
+        init = []
+        for l in range(len(core)):
+            W = torch.from_numpy(np.asarray(o.initialization[ordering[l]], dtype=np.float64)).to(S.device, dt)
+            init.append(kernels.matmul(Uts[l], W).double().cpu().numpy())
+    else:
+        init = starting_point_random(core, R, o)
+    x0 = torch.from_numpy(_dev.flat_factors(init)).to(device=S.device, dtype=dt)
+    best, ss, er, im, gr, st = _run_dgn(S, x0, R, o, prec)
+    Wf = _decompress(Uts, best, core, R)
+    factors = _dev.unflat(Wf.double().cpu().numpy(), [int(d) for d in sdims], R)
+    # final error on the stored entries (Auxiliar.py:155-159), sorted order
+    frm = [torch.from_numpy(np.ascontiguousarray(f)).to(S.device, dt) for f in factors]
+    res = float(sparse_residual_sq(X, frm).cpu().numpy()[0])
+    factors = unsort_dims(factors, ordering)
+    out = Output()
+    out.num_steps = len(ss)
+    out.rel_error = float(np.sqrt(res)) / Tsize
+    out.accuracy = max(0, 100 * (1 - out.rel_error))
+    out.step_sizes = [ss, np.array([0])]
+    out.errors = [er, np.array([0])]
+    out.improv = [im, np.array([0])]
+    out.gradients = [gr, np.array([0])]
+    out.stop = [st, 8]
+    out.options = o
+    return factors, out

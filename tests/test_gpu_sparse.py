@@ -1,0 +1,124 @@
+"""Sparse (COO) device path vs the reference's golden vectors and the oracle."""
+import numpy as np
+import pytest
+
+import tfx_oracle as orc
+from conftest import load_golden, split_x
+
+pytestmark = pytest.mark.gpu
+
+tfx = pytest.importorskip("tensorfox_gb300")
+torch = pytest.importorskip("torch")
+from tensorfox_gb300 import sparse  # noqa: E402
+
+
+def coo(dims, R, nnz, seed, noise=0.01):
+    rng = np.random.default_rng(seed)
+    lin = rng.choice(int(np.prod(dims)), size=nnz, replace=False)
+    idxs = np.stack(np.unravel_index(lin, dims), axis=1).astype(np.int64)
+    W = [rng.standard_normal((d, R)) for d in dims]
+    model = np.ones((nnz, R))
+    for l in range(len(dims)):
+        model *= W[l][idxs[:, l]]
+    return model.sum(1) + noise * rng.standard_normal(nnz), idxs, W
+
+
+def dense_of(data, idxs, dims):
+    T = np.zeros(dims)
+    np.add.at(T, tuple(idxs.T), data)
+    return T
+
+
+def rm(W, dt):
+    return [torch.from_numpy(np.ascontiguousarray(w)).to("cuda", dt) for w in W]
+
+
+@pytest.mark.parametrize("dims,R,nnz", [((10, 9, 8), 3, 60), ((30, 20, 25), 7, 900), ((6, 5, 4, 3), 4, 200),
+                                        ((40, 30, 20), 20, 3000)])
+@pytest.mark.parametrize("dt", [torch.float64, torch.float32])
+def test_coo_mttkrp_vs_dense(dims, R, nnz, dt):
+    data, idxs, W = coo(dims, R, nnz, 1)
+    X = sparse.DeviceCOO(data, idxs, dims, dt)
+    T = dense_of(data, idxs, dims)
+    Tl = [orc.unfold(T, l + 1) for l in range(len(dims))]
+    for l in range(len(dims)):
+        got = sparse.coo_mttkrp(X, rm(W, dt), l).double().cpu().numpy()
+        ref = orc.mttkrp(Tl, W, l)
+        tol = 1e-12 if dt == torch.float64 else 1e-5
+        np.testing.assert_allclose(got, ref, rtol=tol, atol=tol * np.abs(ref).max())
+
+
+@pytest.mark.parametrize("dt", [torch.float64, torch.float32])
+def test_sparse_units_vs_reference(dt):
+    g = load_golden("sparse_L3")
+    dims, R = [int(d) for d in g["dims"]], int(g["R"])
+    X = sparse.DeviceCOO(g["data"], g["idxs"], dims, dt)
+    W = split_x(g["W"], dims, R)
+    res = float(sparse.sparse_residual_sq(X, rm(W, dt)).cpu().numpy()[0])
+    tol = 1e-12 if dt == torch.float64 else 1e-5
+    assert abs(np.sqrt(res) - float(g["sparse_fastnorm"])) <= tol * float(g["sparse_fastnorm"])
+    s = 0
+    for l in range(3):
+        G = X.gram(l).double().cpu().numpy().flatten()
+        ref = g["grams"][s:s + dims[l] ** 2]
+        s += dims[l] ** 2
+        np.testing.assert_allclose(G, ref, rtol=tol, atol=tol * np.abs(ref).max())
+    UT, s = [], 0
+    for l, n in enumerate(g["UT_rows"]):
+        UT.append(g["UT"][s:s + n * dims[l]].reshape(n, dims[l]))
+        s += n * dims[l]
+    S = sparse.sparse_ttmc(X, [torch.from_numpy(u).to("cuda", dt) for u in UT]).double().cpu().numpy()
+    np.testing.assert_allclose(S, g["S"], rtol=tol, atol=tol * np.abs(g["S"]).max())
+
+
+def test_coo_gram_with_shared_fibres():
+    """Entries that share a fibre produce off-diagonal Gram terms; duplicates add up."""
+    rng = np.random.default_rng(5)
+    dims = (7, 3, 2)
+    idxs = np.array([[i, j, k] for i in range(7) for j in range(3) for k in range(2) if rng.random() < 0.5])
+    idxs = np.concatenate([idxs, idxs[:5]])            # duplicated coordinates
+    data = rng.standard_normal(len(idxs))
+    X = sparse.DeviceCOO(data, idxs, dims, torch.float64)
+    T = dense_of(data, idxs, dims)
+    for l in range(3):
+        U = orc.unfold(T, l + 1)
+        np.testing.assert_allclose(X.gram(l).cpu().numpy(), U @ U.T, rtol=1e-12, atol=1e-12)
+
+
+def test_coo_encode_rejects_out_of_range():
+    with pytest.raises(ValueError):
+        sparse.DeviceCOO(np.ones(2), np.array([[0, 0, 0], [0, 5, 0]]), (3, 3, 3), torch.float64)
+
+
+def test_sparse_cpd_vs_reference():
+    g = load_golden("sparse_L3")
+    dims, R = [int(d) for d in g["dims"]], int(g["R"])
+    np.random.seed(41)
+    f, out = tfx.cpd([g["data"], g["idxs"], np.array(dims)], R)
+    ref = float(g["cpd_rel_error"])
+    # same semantics (absent entries are zeros); trajectories differ by rounding only
+    assert abs(out.rel_error - ref) <= 0.05 * ref + 1e-3
+    assert out.stop[1] == 8
+
+
+def test_reference_sparse_doctest():
+    """tests/sparse_tensors.py:8-30 of the reference: an exactly low-rank sparse
+    tensor (sparse factors), best of 10, dense relative error < 1e-4."""
+    rng = np.random.default_rng(9)
+    dims, R = [10, 10, 10, 10], 5
+    W = []
+    for d in dims:
+        M = np.zeros((d, R))
+        for _ in range(10):
+            M[rng.integers(d), rng.integers(R)] = rng.standard_normal()
+        W.append(M)
+    T = orc.cpd2tens(W)
+    idxs = np.argwhere(T != 0)
+    data = T[tuple(idxs.T)]
+    best = 1.0
+    for seed in range(10):
+        np.random.seed(seed)
+        f, out = tfx.cpd([data, idxs, dims], R)
+        err = np.linalg.norm(T - orc.cpd2tens(f)) / np.linalg.norm(T)
+        best = min(best, err)
+    assert best < 1e-4
