@@ -48,6 +48,18 @@ int tfx_mode_gram(int dtype, const void* S, long long P, int D, long long Q, voi
  * strides = {sAb, sAm, sAk, sBb, sBk, sBn, sCb, sCm, sCn} (elements). */
 int tfx_gemm(int dtype, const void* A, const void* B, void* C, long long M, long long N, long long K, long long batch,
              const long long* strides, double alpha, double beta, void* stream);
+/* Allocation-free variant of tfx_mode_gram, for callers that cannot allocate
+ * device memory when they call (their host's memory pool owns the device, the
+ * call sits on a latency-critical path, or allocation is forbidden after
+ * start-up).  No counterpart in the reference.  The split-K scratch comes from a
+ * 32 MiB array built into the library (held by every GPU that loads it until
+ * exit; tfx_mode_gram_noalloc_capacity_bytes() returns its size), so
+ * D*D*element size must not exceed 32 MiB (D <= 2896 in float32, 2048 in
+ * float64); larger D is refused with TFX_STATUS_ERR_ARG.  The first call on a
+ * device looks the array's address up and should come before any stream
+ * capture.  Calls share the array: calls that overlap on the GPU race. */
+size_t tfx_mode_gram_noalloc_capacity_bytes(void);
+int tfx_mode_gram_noalloc(int dtype, const void* S, long long P, int D, long long Q, void* G, void* stream);
 /* Orthonormal basis of the k columns of Y (D x k column-major), in place
  * (scipy qr in Compression.py:392). */
 int tfx_orthonormalize(int dtype, void* Y, int D, int k, void* stream);

@@ -737,3 +737,69 @@ extern "C" int tfx_tensor_norms(int dtype, const void* T, long long N, double* o
   k_sum_partials<<<1, 32, 0, st>>>(partial, blocks, 2, out2);
   return check_launch("sum_partials");
 }
+
+// ============================================================================
+// Allocation-free mode Gram.
+//
+// Some callers cannot allocate device memory when they call us: a host that
+// lets another framework own all device memory through its own pool (a
+// cudaMalloc from us would fail or fragment that pool), code on a
+// latency-critical path that cannot afford cudaMalloc's implicit
+// synchronisation, or services that forbid any allocation after start-up.
+// For them tfx_mode_gram_noalloc takes its split-K scratch from a fixed array
+// compiled into this library instead of from a caller buffer.
+//
+// * The array has TFX_NOALLOC_SCRATCH_BYTES (32 MiB).  Every GPU that loads the
+//   library holds it until the process exits.
+// * The first call on each device looks up the array's device address with
+//   cudaGetSymbolAddress while that device is current (the symbol's host-side
+//   name is not a device address).  That first call on a device should come
+//   before any stream capture.
+// * Every call shares the one array: calls that overlap on the GPU (other
+//   streams, other host threads) race on it.  The kernels overwrite every
+//   scratch entry they later read, so nothing needs clearing between calls.
+// ============================================================================
+#include <mutex>
+
+#define TFX_NOALLOC_SCRATCH_BYTES (32u << 20)
+#define TFX_NOALLOC_MAX_DEVICES 64
+
+static __device__ __align__(256) unsigned char g_noalloc_gram_scratch[TFX_NOALLOC_SCRATCH_BYTES];
+
+static std::mutex g_noalloc_mu;
+static void* g_noalloc_addr[TFX_NOALLOC_MAX_DEVICES] = {nullptr};
+
+static int noalloc_scratch_address(void** out) {
+  int dev = -1;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return tfx_set_cuda_error(e, "mode_gram_noalloc: current device");
+  if (dev < 0 || dev >= TFX_NOALLOC_MAX_DEVICES)
+    return tfx_set_error(TFX_STATUS_ERR_UNSUPPORTED, "mode_gram_noalloc: device ordinal above 63");
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);
+  if (g_noalloc_addr[dev] == nullptr) {
+    void* p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_noalloc_gram_scratch);
+    if (e != cudaSuccess || p == nullptr)
+      return tfx_set_cuda_error(e == cudaSuccess ? cudaErrorInvalidSymbol : e, "mode_gram_noalloc: scratch address");
+    g_noalloc_addr[dev] = p;
+  }
+  *out = g_noalloc_addr[dev];
+  return TFX_STATUS_OK;
+}
+
+extern "C" size_t tfx_mode_gram_noalloc_capacity_bytes(void) { return TFX_NOALLOC_SCRATCH_BYTES; }
+
+extern "C" int tfx_mode_gram_noalloc(int dtype, const void* S, long long P, int D, long long Q, void* G, void* stream) {
+  if (!S || !G || P < 1 || D < 1 || Q < 1) return tfx_set_error(TFX_STATUS_ERR_ARG, "mode_gram_noalloc args");
+  if (dtype != TFX_F32 && dtype != TFX_F64) return tfx_set_error(TFX_STATUS_ERR_ARG, "mode_gram_noalloc dtype");
+  const size_t es = dtype == TFX_F64 ? 8 : 4;
+  // one D x D partial must fit: D <= 2896 in float32, D <= 2048 in float64
+  if ((size_t)D * (size_t)D * es > (size_t)TFX_NOALLOC_SCRATCH_BYTES)
+    return tfx_set_error(TFX_STATUS_ERR_ARG,
+                         "mode_gram_noalloc: D*D*element size exceeds the 32 MiB built-in scratch "
+                         "(D <= 2896 for float32, D <= 2048 for float64); use tfx_mode_gram with a caller buffer");
+  void* scratch = nullptr;
+  const int s = noalloc_scratch_address(&scratch);
+  if (s) return s;
+  return tfx_mode_gram(dtype, S, P, D, Q, G, scratch, TFX_NOALLOC_SCRATCH_BYTES, stream);
+}
