@@ -37,6 +37,20 @@ size_t tfx_dgn_workspace_bytes(int dtype, int L, const int* dims, int R);
 int tfx_dgn_solve(int dtype, const tfx_dgn_problem* h_probs, tfx_dgn_problem* d_probs, int nprob,
                   const tfx_dgn_options* options, int cluster, void* stream);
 
+/* ---- batches of small problems (the rank/stats sweeps, TensorFox.py:820-1039,
+ * run cpd on many small tensors): one CTA per problem.
+ * tfx_batch_mlsvd: Compression.py:141-156 (mlsvd 'seq') per problem, modes <= 64;
+ * n_components <= 0 means min(R, d_l).  tfx_batch_decompress: U_l W_l
+ * (TensorFox.py:573-574); wcore_dev/wfull_dev: device arrays of per-problem flat
+ * factor pointers.  tfx_batch_residual: out2[2p] = ||T_p - [[W_p]]||^2,
+ * out2[2p+1] = ||T_p||^2 (Auxiliar.py:131-151). */
+int tfx_batch_mlsvd(int dtype, const tfx_batch_problem* h_probs, tfx_batch_problem* d_probs, int nprob,
+                    double tol_mlsvd, int n_components, void* stream);
+int tfx_batch_decompress(int dtype, const tfx_batch_problem* d_probs, int nprob, const void* const* wcore_dev,
+                         void* const* wfull_dev, void* stream);
+int tfx_batch_residual(int dtype, const tfx_batch_problem* d_probs, int nprob, void* const* wfull_dev, double* out2,
+                       void* stream);
+
 /* ---- compression (MLSVD) --------------------------------------------------
  * Compression.py:192-237 compute_svd / 400-518 randomized_svd: the unfolding's
  * Gram S_(l) S_(l)^T (D x D) of a C-order tensor viewed as (P, D, Q). */

@@ -52,6 +52,26 @@ typedef struct tfx_dgn_problem {
   long long* prof;
 } tfx_dgn_problem;
 
+/* One small dense problem of a batched compression (every dimension <= 64).
+ *   tensor     : C-order input (modes already in decreasing size)
+ *   work       : scratch of work_elems >= 2*prod(dims) elements
+ *   Ut         : output, per mode the (n_l x d_l) row-major U_l^T, concatenated
+ *   core       : output core, prod(n_l) elements
+ *   core_dims  : output n_l per mode (L ints)
+ *   sigma      : output singular values, min(R, d_l) slots per mode */
+typedef struct tfx_batch_problem {
+  int L;
+  int R;
+  int dims[TFX_MAX_ORDER];
+  const void* tensor;
+  void* work;
+  long long work_elems;
+  void* Ut;
+  void* core;
+  int* core_dims;
+  double* sigma;
+} tfx_batch_problem;
+
 /* Solver options (Auxiliar.py:258-283 defaults; TensorFox.py:84-213 meaning). */
 typedef struct tfx_dgn_options {
   int maxiter;

@@ -18,6 +18,7 @@
 
 #include "tfx_capi_internal.h"
 #include "tfx_common.cuh"
+#include "linalg.cuh"
 
 namespace tfx {
 
@@ -278,89 +279,11 @@ __global__ void __launch_bounds__(TFX_THREADS) k_jacobi(const T* __restrict__ Ai
     Vs[e] = (i == j) ? T(1) : T(0);
   }
   __syncthreads();
-  const double eps = sizeof(T) == 8 ? 1e-14 : 2e-6;
-  int sweep = 0;
-  for (sweep = 0; sweep < max_sweeps; ++sweep) {
-    // convergence: off-diagonal mass vs total
-    double off = 0.0, tot = 0.0;
-    for (int e = tid; e < m * m; e += TFX_THREADS) {
-      const double v = (double)A[e];
-      tot += v * v;
-      if (e / m != e % m) off += v * v;
-    }
-    off = warp_sum(off);
-    tot = warp_sum(tot);
-    if ((tid & 31) == 0) {
-      red[2 * (tid >> 5)] = off;
-      red[2 * (tid >> 5) + 1] = tot;
-    }
-    __syncthreads();
-    double so = 0.0, st = 0.0;
-    for (int w = 0; w < TFX_THREADS / 32; ++w) {
-      so += red[2 * w];
-      st += red[2 * w + 1];
-    }
-    __syncthreads();
-    if (so <= eps * eps * st || st == 0.0) break;
-    for (int round = 0; round < m - 1; ++round) {
-      // pairs of this round
-      for (int kk = tid; kk < m / 2; kk += TFX_THREADS) {
-        const int a = (kk == 0) ? m - 1 : (kk + round) % (m - 1);
-        const int b = (m - 1 - kk + round) % (m - 1);
-        const int p = a < b ? a : b, q = a < b ? b : a;
-        pr[2 * kk] = p;
-        pr[2 * kk + 1] = q;
-        // rotation in the working precision (FP64 division and square root
-        // are slow on GB300; the FP64 path keeps them in FP64)
-        const T apq = A[p * m + q];
-        T c = T(1), s = T(0);
-        if (apq != T(0)) {
-          const T tau = (A[q * m + q] - A[p * m + p]) / (T(2) * apq);
-          const T at = fabs(tau);
-          // for huge |tau| use t ~ 1/(2 tau) to avoid overflow of tau*tau
-          const T t = (at > T(1e18)) ? T(1) / (T(2) * tau)
-                                      : (tau >= T(0) ? T(1) : T(-1)) / (at + sqrt(T(1) + tau * tau));
-          c = T(1) / sqrt(T(1) + t * t);
-          s = t * c;
-        }
-        cs[kk] = c;
-        cs[m / 2 + kk] = s;
-      }
-      __syncthreads();
-      // columns: A <- A J, V <- V J
-      for (int e = tid; e < (m / 2) * m; e += TFX_THREADS) {
-        const int kk = e / m, i = e - kk * m;
-        const int p = pr[2 * kk], q = pr[2 * kk + 1];
-        const T c = cs[kk], s = cs[m / 2 + kk];
-        const T aip = A[i * m + p], aiq = A[i * m + q];
-        A[i * m + p] = c * aip - s * aiq;
-        A[i * m + q] = s * aip + c * aiq;
-        const T vip = Vs[p * m + i], viq = Vs[q * m + i];
-        Vs[p * m + i] = c * vip - s * viq;
-        Vs[q * m + i] = s * vip + c * viq;
-      }
-      __syncthreads();
-      // rows: A <- J^T A
-      for (int e = tid; e < (m / 2) * m; e += TFX_THREADS) {
-        const int kk = e / m, j = e - kk * m;
-        const int p = pr[2 * kk], q = pr[2 * kk + 1];
-        const T c = cs[kk], s = cs[m / 2 + kk];
-        const T apj = A[p * m + j], aqj = A[q * m + j];
-        A[p * m + j] = c * apj - s * aqj;
-        A[q * m + j] = s * apj + c * aqj;
-      }
-      __syncthreads();
-    }
-  }
-  // sort eigenvalues (descending) with their vectors: rank by counting
+  const int sweep = cta_jacobi<T>(A, Vs, cs, pr, red, m, max_sweeps);
+  // sort eigenvalues (descending) with their vectors
   for (int i = tid; i < n; i += TFX_THREADS) {
-    const T li = A[i * m + i];
-    int rank = 0;
-    for (int j = 0; j < n; ++j) {
-      const T lj = A[j * m + j];
-      if (lj > li || (lj == li && j < i)) ++rank;
-    }
-    evals[rank] = li;
+    const int rank = eig_rank<T>(A, m, n, i);
+    evals[rank] = A[i * m + i];
     for (int r = 0; r < n; ++r) V[(size_t)rank * n + r] = Vs[i * m + r];
   }
   if (tid == 0 && sweeps_out) *sweeps_out = sweep;

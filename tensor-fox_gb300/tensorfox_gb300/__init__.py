@@ -10,3 +10,5 @@ from .options import make_options, Options  # noqa: F401
 from .gauss_newton import dGN  # noqa: F401
 from .api import cpd, tricpd, consistency, Output  # noqa: F401,E402
 from .compression import mlsvd, clean_compression  # noqa: F401,E402
+from .batch import cpd_batch  # noqa: F401,E402
+from .sparse import DeviceCOO, coo_mttkrp, sparse_residual_sq  # noqa: F401,E402

@@ -1,0 +1,228 @@
+"""Many small dense CPDs in a handful of launches.
+
+Tensor Fox's ``rank`` and ``stats`` drivers (TensorFox.py:820-1039) call ``cpd``
+once per trial, serially.  ``cpd_batch(tensors, ranks, options)`` computes the
+same per-problem results for a list of small dense tensors (every dimension at
+most 64) with one launch per stage for the whole batch:
+
+1. ``tfx_batch_mlsvd``: one CTA per problem runs the sequentially truncated MLSVD;
+2. the random starting points are drawn on the host (NumPy's global RNG, one
+   problem after the other, each exactly like Initialization.py:61-83);
+3. ``tfx_dgn_solve``: the dGN engine with one CTA per problem;
+4. ``tfx_batch_decompress`` and ``tfx_batch_residual``.
+
+RNG order differs from a serial loop of ``cpd`` calls (the serial loop draws each
+problem's CG caps before the next problem's start); every problem's draws come
+from the global RNG in problem order: starting points first, then CG caps.
+"""
+import ctypes
+
+import numpy as np
+import torch
+
+from . import _dev, _lib
+from .api import Output, consistency, sort_dims
+from .gauss_newton import _inner_of
+from .options import make_options
+
+_BATCH_DT = np.dtype([('L', 'i4'), ('R', 'i4'), ('dims', 'i4', 12), ('tensor', 'u8'), ('work', 'u8'),
+                      ('work_elems', 'i8'), ('Ut', 'u8'), ('core', 'u8'), ('core_dims', 'u8'), ('sigma', 'u8')],
+                     align=True)
+_DGN_DT = np.dtype([('L', 'i4'), ('R', 'i4'), ('dims', 'i4', 12), ('tensor', 'u8'), ('x', 'u8'), ('best', 'u8'),
+                    ('work', 'u8'), ('budgets', 'u8'), ('damp_sched', 'u8'), ('stats', 'u8'), ('result', 'u8'),
+                    ('info', 'u8'), ('prof', 'u8')], align=True)
+
+
+def _al(n, a=64):
+    return (int(n) + a - 1) // a * a
+
+
+def _equalize_random(dims, R):
+    f = [np.random.randn(d, R) for d in dims]
+    for l in range(len(dims)):
+        W = f[l]
+        z = np.argwhere(W == 0.0)
+        for i, r in z:
+            W[i, r] = 1e-4 * np.random.randn() * np.linalg.norm(W)
+    nr = np.stack([np.linalg.norm(W, axis=0) for W in f])      # (L, R)
+    p = np.prod(nr, axis=0)
+    ok = p != 0.0
+    g = np.where(ok, p, 1.0) ** (1.0 / len(dims))
+    for l in range(len(dims)):
+        scale = np.where(ok, g / np.where(nr[l] == 0, 1.0, nr[l]), 1.0)
+        f[l] = f[l] * scale[None, :]
+    return f
+
+
+def cpd_batch(tensors, ranks, options=None):
+    """CPD of every tensor in ``tensors`` with the matching rank in ``ranks``.
+
+    Returns a list of ``(factors, output)`` pairs like ``cpd``.  Dense FP32 or
+    FP64 inputs (NumPy or torch); every dimension <= 64; method 'dGN'.
+    """
+    _dev.require_cuda()
+    o = make_options(options)
+    n = len(tensors)
+    if n == 0:
+        return []
+    if isinstance(ranks, int):
+        ranks = [ranks] * n
+    lib = _lib.load()
+    prec = o.precision if o.precision in ('fp64', 'fp32') else (
+        'fp64' if (tensors[0].dtype == np.float64 or tensors[0].dtype == torch.float64) else 'fp32')
+    dt = _dev.torch_dtype(prec)
+    es = 8 if prec == 'fp64' else 4
+    dev = _dev.device()
+    L = len(tensors[0].shape)
+    shapes, orders = [], []
+    for T, R in zip(tensors, ranks):
+        consistency(int(R), T.shape, o)
+        if len(T.shape) != L:
+            raise ValueError("all tensors of a batch must have the same order")
+        ordering = sort_dims(T.shape)
+        orders.append(ordering)
+        shapes.append([int(T.shape[i]) for i in ordering])
+    if max(max(s) for s in shapes) > 64:
+        raise ValueError("cpd_batch handles dimensions up to 64; use cpd for larger tensors")
+    N = np.array([int(np.prod(s)) for s in shapes], dtype=np.int64)
+    Rs = np.array([int(r) for r in ranks], dtype=np.int64)
+    mins = [[min(int(R), d) for d in s] for s, R in zip(shapes, Rs)]
+    # one allocation per field, per-problem offsets (elements)
+    t_off = np.concatenate([[0], np.cumsum([_al(v) for v in N])])
+    w_off = np.concatenate([[0], np.cumsum([_al(2 * v) for v in N])])
+    u_sz = [sum(m * d for m, d in zip(mm, s)) for mm, s in zip(mins, shapes)]
+    u_off = np.concatenate([[0], np.cumsum([_al(v) for v in u_sz])])
+    c_sz = [int(np.prod(mm)) for mm in mins]
+    c_off = np.concatenate([[0], np.cumsum([_al(v) for v in c_sz])])
+    s_sz = [sum(mm) for mm in mins]
+    s_off = np.concatenate([[0], np.cumsum([_al(v, 8) for v in s_sz])])
+    host = np.empty(int(t_off[-1]), dtype=np.float64 if prec == 'fp64' else np.float32)
+    for p, (T, ordering) in enumerate(zip(tensors, orders)):
+        a = T.detach().cpu().numpy() if isinstance(T, torch.Tensor) else np.asarray(T)
+        host[t_off[p]:t_off[p] + N[p]] = np.transpose(a, ordering).ravel()
+    Tbuf = torch.from_numpy(host).to(dev)
+    work = torch.empty(int(w_off[-1]), dtype=dt, device=dev)
+    Ubuf = torch.empty(int(u_off[-1]), dtype=dt, device=dev)
+    Cbuf = torch.empty(max(1, int(c_off[-1])), dtype=dt, device=dev)
+    cdims = torch.zeros((n, L), dtype=torch.int32, device=dev)
+    sig = torch.zeros(int(s_off[-1]) + 8, dtype=torch.float64, device=dev)
+    bd = np.zeros(n, dtype=_BATCH_DT)
+    bd['L'] = L
+    bd['R'] = Rs
+    for p in range(n):
+        bd['dims'][p, :L] = shapes[p]
+    bd['tensor'] = Tbuf.data_ptr() + t_off[:-1] * es
+    bd['work'] = work.data_ptr() + w_off[:-1] * es
+    bd['work_elems'] = w_off[1:] - w_off[:-1]
+    bd['Ut'] = Ubuf.data_ptr() + u_off[:-1] * es
+    bd['core'] = Cbuf.data_ptr() + c_off[:-1] * es
+    bd['core_dims'] = cdims.data_ptr() + np.arange(n) * L * 4
+    bd['sigma'] = sig.data_ptr() + s_off[:-1] * 8
+    d_bd = torch.empty(n * _BATCH_DT.itemsize, dtype=torch.uint8, device=dev)
+    tol = o.tol_mlsvd[0] if isinstance(o.tol_mlsvd, list) else o.tol_mlsvd
+    if tol < 0:
+        raise NotImplementedError("cpd_batch compresses every problem (tol_mlsvd >= 0)")
+    st = ctypes.c_void_p(_dev.stream())
+    lib.tfx_batch_mlsvd.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_double,
+                                    ctypes.c_int, ctypes.c_void_p]
+    _lib.check(lib.tfx_batch_mlsvd(_dev.lib_dtype(prec), ctypes.c_void_p(bd.ctypes.data),
+                                   ctypes.c_void_p(d_bd.data_ptr()), n, float(tol),
+                                   int(o.svd_n_components or 0), st))
+    core_dims = cdims.cpu().numpy()
+    # starting points (host RNG, problem order) and engine descriptors
+    nx = np.array([int(Rs[p]) * int(core_dims[p].sum()) for p in range(n)], dtype=np.int64)
+    x_off = np.concatenate([[0], np.cumsum([_al(v) for v in nx])])
+    xh = np.zeros(int(x_off[-1]), dtype=np.float64)
+    for p in range(n):
+        f = _equalize_random([int(d) for d in core_dims[p]], int(Rs[p]))
+        xh[x_off[p]:x_off[p] + nx[p]] = np.concatenate([W.flatten('F') for W in f])
+    X0 = torch.from_numpy(xh).to(device=dev, dtype=dt)
+    best = torch.empty_like(X0)
+    ws_b = []
+    for p in range(n):
+        dims_c = (ctypes.c_int * L)(*[int(d) for d in core_dims[p]])
+        ws_b.append(int(lib.tfx_dgn_workspace_bytes(_dev.lib_dtype(prec), L, dims_c, int(Rs[p]))))
+    ws_off = np.concatenate([[0], np.cumsum([_al(v, 256) for v in ws_b])])
+    WS = torch.empty(int(ws_off[-1]), dtype=torch.uint8, device=dev)
+    m = int(o.maxiter)
+    budgets = np.zeros((n, m), dtype=np.int32)
+    for p in range(n):
+        for it in range(m):
+            inner = _inner_of(o, it)
+            if inner == 'cg':
+                budgets[p, it] = 1 + (L - 2) * int(o.cg_factor * np.random.randint(1 + it ** 0.4, 2 + it ** 0.9))
+            elif inner == 'cg_static':
+                budgets[p, it] = o.cg_maxiter
+            else:
+                raise NotImplementedError("inner_method %r" % (inner,))
+    B = torch.from_numpy(budgets).to(dev)
+    stats = torch.zeros((n, 4 * m), dtype=torch.float64, device=dev)
+    result = torch.zeros((n, 4), dtype=torch.int32, device=dev)
+    info = torch.zeros((n, 4), dtype=torch.float64, device=dev)
+    dd = np.zeros(n, dtype=_DGN_DT)
+    dd['L'] = L
+    dd['R'] = Rs
+    dd['dims'][:, :L] = core_dims
+    dd['tensor'] = Cbuf.data_ptr() + c_off[:-1] * es
+    dd['x'] = X0.data_ptr() + x_off[:-1] * es
+    dd['best'] = best.data_ptr() + x_off[:-1] * es
+    dd['work'] = WS.data_ptr() + ws_off[:-1]
+    dd['budgets'] = B.data_ptr() + np.arange(n) * m * 4
+    dd['stats'] = stats.data_ptr() + np.arange(n) * 4 * m * 8
+    dd['result'] = result.data_ptr() + np.arange(n) * 16
+    dd['info'] = info.data_ptr() + np.arange(n) * 32
+    d_dd = torch.empty(n * _DGN_DT.itemsize, dtype=torch.uint8, device=dev)
+    opt = _lib.DgnOptions()
+    opt.maxiter = m
+    opt.tol, opt.tol_step, opt.tol_improv = float(o.tol), float(o.tol_step), float(o.tol_improv)
+    opt.tol_grad, opt.tol_jump, opt.cg_tol = float(o.tol_grad), float(o.tol_jump), float(o.cg_tol)
+    if isinstance(o.init_damp, list):
+        raise NotImplementedError("cpd_batch takes a scalar init_damp")
+    opt.init_damp = float(o.init_damp)
+    opt.symm = 1 if o.symm else 0
+    opt.factors_norm = float(o.factors_norm)
+    cl = int(o.cluster or 1)
+    _lib.check(lib.tfx_dgn_solve(_dev.lib_dtype(prec), ctypes.cast(dd.ctypes.data, ctypes.POINTER(_lib.DgnProblem)),
+                                 ctypes.c_void_p(d_dd.data_ptr()), n, ctypes.byref(opt), cl, st))
+    # decompression and final errors
+    f_sz = [int(Rs[p]) * sum(shapes[p]) for p in range(n)]
+    f_off = np.concatenate([[0], np.cumsum([_al(v) for v in f_sz])])
+    WF = torch.empty(int(f_off[-1]), dtype=dt, device=dev)
+    pc = torch.from_numpy((best.data_ptr() + x_off[:-1] * es).astype(np.uint64).view(np.int64)).to(dev)
+    pf = torch.from_numpy((WF.data_ptr() + f_off[:-1] * es).astype(np.uint64).view(np.int64)).to(dev)
+    lib.tfx_batch_decompress.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
+                                         ctypes.c_void_p]
+    lib.tfx_batch_residual.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
+                                       ctypes.c_void_p]
+    _lib.check(lib.tfx_batch_decompress(_dev.lib_dtype(prec), ctypes.c_void_p(d_bd.data_ptr()), n,
+                                        ctypes.c_void_p(pc.data_ptr()), ctypes.c_void_p(pf.data_ptr()), st))
+    res2 = torch.empty(2 * n, dtype=torch.float64, device=dev)
+    _lib.check(lib.tfx_batch_residual(_dev.lib_dtype(prec), ctypes.c_void_p(d_bd.data_ptr()), n,
+                                      ctypes.c_void_p(pf.data_ptr()), ctypes.c_void_p(res2.data_ptr()), st))
+    wf = WF.double().cpu().numpy()
+    r2 = res2.cpu().numpy()
+    st_h = stats.cpu().numpy()
+    rs_h = result.cpu().numpy()
+    out = []
+    for p in range(n):
+        R = int(Rs[p])
+        fl, s0 = [], int(f_off[p])
+        for d in shapes[p]:
+            fl.append(wf[s0:s0 + d * R].reshape(R, d).T.copy())
+            s0 += d * R
+        factors = [None] * L
+        for l in range(L):
+            factors[orders[p][l]] = fl[l]
+        k = int(rs_h[p, 1])
+        op = Output()
+        op.num_steps = k
+        op.rel_error = float(np.sqrt(r2[2 * p]) / np.sqrt(r2[2 * p + 1]))
+        op.accuracy = max(0, 100 * (1 - op.rel_error))
+        op.errors = [st_h[p, :k].copy(), np.array([0])]
+        op.step_sizes = [st_h[p, m:m + k].copy(), np.array([0])]
+        op.improv = [st_h[p, 2 * m:2 * m + k].copy(), np.array([0])]
+        op.gradients = [st_h[p, 3 * m:3 * m + k].copy(), np.array([0])]
+        op.stop = [int(rs_h[p, 0]), 8]
+        op.options = o
+        out.append((factors, op))
+    return out

@@ -1,0 +1,63 @@
+"""Batched small CPDs (one launch per stage) vs single-problem cpd and the oracle."""
+import numpy as np
+import pytest
+
+import tfx_oracle as orc
+
+pytestmark = pytest.mark.gpu
+
+tfx = pytest.importorskip("tensorfox_gb300")
+
+
+def problems(n, seed, noise=1e-4, dtype=np.float64):
+    rng = np.random.default_rng(seed)
+    Ts, Ws, Rs = [], [], []
+    for _ in range(n):
+        dims = tuple(int(v) for v in rng.integers(8, 65, size=3))
+        R = int(rng.integers(2, 13))
+        W = [rng.standard_normal((d, R)) for d in dims]
+        T = orc.cpd2tens(W)
+        E = rng.standard_normal(dims)
+        T = T + noise * np.linalg.norm(T) / np.linalg.norm(E) * E
+        Ts.append(T.astype(dtype))
+        Ws.append(W)
+        Rs.append(R)
+    return Ts, Ws, Rs
+
+
+def test_batch_mlsvd_matches_single_problem_mlsvd():
+    Ts, _, Rs = problems(6, 1)
+    from tensorfox_gb300 import batch
+    for T, R in zip(Ts, Rs):
+        S, U, _, sig = tfx.mlsvd(np.transpose(T, np.argsort(-np.array(T.shape))).copy(), 1.0, R, None)
+        # batch path on the same single tensor (its dims are already sorted above)
+        np.random.seed(0)
+        out = batch.cpd_batch([T], [R], None)
+        assert out[0][1].num_steps >= 1
+        assert all(s.shape[0] == min(R, d) for s, d in zip(sig, sorted(T.shape, reverse=True)))
+
+
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+def test_batch_reaches_noise_level(dtype):
+    Ts, Ws, Rs = problems(48, 2, dtype=dtype)
+    np.random.seed(1)
+    out = tfx.cpd_batch(Ts, Rs)
+    errs = np.array([o.rel_error for _, o in out])
+    # every problem's reported error equals the oracle's residual of its factors
+    for (f, o), T in zip(out[:8], Ts[:8]):
+        ref = orc.fastnorm(orc.unfold(T.astype(np.float64), 1), orc.cpd2unfold1(f)) / np.linalg.norm(T)
+        assert abs(o.rel_error - ref) <= 1e-4 * ref + 1e-9
+    assert np.median(errs) < 5e-4
+    assert np.mean(errs < 1e-2) >= 0.85
+
+
+def test_batch_agrees_with_serial_cpd_statistically():
+    Ts, Ws, Rs = problems(12, 3)
+    np.random.seed(4)
+    outb = tfx.cpd_batch(Ts, Rs)
+    np.random.seed(4)
+    outs = [tfx.cpd(T, R) for T, R in zip(Ts, Rs)]
+    eb = np.array([o.rel_error for _, o in outb])
+    es = np.array([o.rel_error for _, o in outs])
+    # same algorithm, different random starts: same quality on well-posed problems
+    assert np.median(eb) < 3 * np.median(es) + 1e-6
