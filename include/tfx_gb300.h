@@ -94,6 +94,18 @@ int tfx_cp_residual(int dtype, const void* T, int L, const int* dims, int R, con
 /* norm(T)^2 and sum|T| (TensorFox.py:503, GaussNewton.py:113) into out2[0..1]. */
 int tfx_tensor_norms(int dtype, const void* T, long long N, double* out2, void* scratch, void* stream);
 
+/* ---- differentiable CP layer (forward / backward kernels) -------------------
+ * tfx_mttkrp: T_(l) (W_{L-1} o ... o W_{l+1} o W_{l-1} o ... o W_0), the product
+ * in GaussNewton.py:411-423, out (d_l x R column-major).  tfx_cp_full: the dense
+ * tensor of a CPD (Conversion.py:52-79 cpd2tens).  tfx_cp_wp1: W_l P1_l for every
+ * mode, P1_l = o_{m != l} W_m^T W_m (GaussNewton.py:520-548, :424), flat layout. */
+size_t tfx_mttkrp_scratch_bytes(int dtype, int L, const int* dims, int R, int mode);
+int tfx_mttkrp(int dtype, const void* T, int L, const int* dims, int R, const void* W, int mode, void* out, void* scratch,
+               size_t scratch_bytes, void* stream);
+int tfx_cp_full(int dtype, int L, const int* dims, int R, const void* W, void* out, void* stream);
+size_t tfx_cp_wp1_scratch_bytes(int L, int R);
+int tfx_cp_wp1(int dtype, int L, const int* dims, int R, const void* W, void* out, void* scratch, void* stream);
+
 /* ---- sparse (COO) ----------------------------------------------------------
  * TensorFox.py:476-481: int64 (nnz x L) coordinates -> int32 L x nnz; *err = 1
  * when a coordinate is out of range. */
