@@ -62,6 +62,13 @@ int tfx_mode_gram(int dtype, const void* S, long long P, int D, long long Q, voi
  * strides = {sAb, sAm, sAk, sBb, sBk, sBn, sCb, sCm, sCn} (elements). */
 int tfx_gemm(int dtype, const void* A, const void* B, void* C, long long M, long long N, long long K, long long batch,
              const long long* strides, double alpha, double beta, void* stream);
+/* The same Gram on the 5th-generation tensor cores: TMA-fed SWIZZLE_128B tiles,
+ * tcgen05.mma kind::tf32 into TMEM, FP32 accumulation, split-K partials summed
+ * in FP64.  FP32 input only; Q >= 32 and Q % 4 == 0; S 16-byte aligned.  *err
+ * (device int) receives a non-zero code if a bounded wait expired. */
+size_t tfx_mode_gram_tc_scratch_bytes(long long P, int D, long long Q);
+int tfx_mode_gram_tc(const float* S, long long P, int D, long long Q, float* G, void* scratch, size_t scratch_bytes,
+                     int* err, void* stream);
 /* Allocation-free variant of tfx_mode_gram, for callers that cannot allocate
  * device memory when they call (their host's memory pool owns the device, the
  * call sits on a latency-critical path, or allocation is forbidden after

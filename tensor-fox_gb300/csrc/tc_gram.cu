@@ -1,0 +1,343 @@
+// Mode Gram S_(l) S_(l)^T on the 5th-generation tensor cores (tcgen05, TF32).
+//
+// The unfolding is read straight from the C-order tensor through a 3-D TMA
+// tensor map over (q, i, p) -- the tensor viewed as (P, D, Q) with q contiguous
+// -- so both MMA operands are K-major SWIZZLE_128B tiles of 128 rows x 32 fp32.
+// One CTA computes a 128 x 128 block (bi, bj), bi <= bj, of the Gram over a
+// slice of the contraction index k = (p, q); the FP32 accumulator lives in
+// TMEM.  Warp 0 issues TMA loads into a ring of shared-memory stages, warp 1
+// issues tcgen05.mma (kind::tf32, M = N = 128, K = 8, four per stage), and all
+// four warps read the accumulator back with tcgen05.ld for the epilogue.
+// Split-K partials are summed by k_gram_reduce-like code in FP64.
+//
+// Replaces the streaming passes of the randomized SVD (Compression.py:337-518)
+// for dense modes with Q a multiple of 4 (TMA row pitch) and Q >= 32.
+//
+// Every mbarrier wait is bounded: on timeout the kernel records an error code,
+// skips its epilogue, waits (bounded) for copies it issued and frees its TMEM.
+#include <cuda.h>
+#include <math.h>
+
+#include <algorithm>
+
+#include "tfx_capi_internal.h"
+#include "tfx_common.cuh"
+
+namespace tfx {
+
+#define TCG_STAGES 5
+#define TCG_BM 128
+#define TCG_BK 32  // fp32 elements per 128-byte swizzled row
+#define TCG_TILE_BYTES (TCG_BM * TCG_BK * 4)
+#define TCG_SPIN_LIMIT (1u << 26)
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+
+// bounded wait for phase `parity`; returns false on timeout
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+  const uint32_t a = smem_u32(bar);
+  for (uint32_t it = 0; it < TCG_SPIN_LIMIT; ++it) {
+    uint32_t done;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(done)
+        : "r"(a), "r"(parity)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+
+__device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, uint64_t* bar, int x, int y, int z) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(
+          smem_u32(dst)),
+      "l"(map), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
+      : "memory");
+}
+
+// shared-memory matrix descriptor: K-major, SWIZZLE_128B, 8-row groups 1024 B apart
+__device__ __forceinline__ uint64_t sw128_desc(const void* tile) {
+  const uint64_t addr = smem_u32(tile);
+  uint64_t d = 0;
+  d |= (addr >> 4) & 0x3FFFull;          // start address
+  d |= (uint64_t)1 << 16;                // leading byte offset (unused for swizzled K-major)
+  d |= (uint64_t)(1024 >> 4) << 32;      // stride byte offset
+  d |= (uint64_t)1 << 46;                // descriptor version
+  d |= (uint64_t)2 << 61;                // SWIZZLE_128B
+  return d;
+}
+
+// instruction descriptor: D = F32, A = B = TF32, both K-major, M = 128, N = 128
+__host__ __device__ constexpr uint32_t tf32_idesc() {
+  return (1u << 4) | (2u << 7) | (2u << 10) | ((128u >> 3) << 17) | ((128u >> 4) << 24);
+}
+
+__device__ __forceinline__ void mma_tf32(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                         uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem_d),
+      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+
+__device__ __forceinline__ void mma_commit(uint64_t* bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+               : "memory");
+}
+
+struct TcGramSmem {
+  alignas(1024) unsigned char a[TCG_STAGES][TCG_TILE_BYTES];
+  alignas(1024) unsigned char b[TCG_STAGES][TCG_TILE_BYTES];
+  alignas(8) uint64_t full[TCG_STAGES];
+  alignas(8) uint64_t empty[TCG_STAGES];
+  alignas(8) uint64_t done;
+  uint32_t tmem_base;
+  int abort;
+};
+
+__global__ void __launch_bounds__(128, 1)
+    k_gram_tc(const __grid_constant__ CUtensorMap tmap, int D, long long P, int qchunks, int ksplit, float* part,
+              int* err) {
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  // align the carve-out to 1024 bytes (SWIZZLE_128B atoms)
+  TcGramSmem& S = *reinterpret_cast<TcGramSmem*>((((uintptr_t)smem_raw) + 1023) & ~(uintptr_t)1023);
+  const int nt = (D + TCG_BM - 1) / TCG_BM;
+  int t = blockIdx.x, bi = 0;
+  while (t >= nt - bi) {
+    t -= nt - bi;
+    ++bi;
+  }
+  const int bj = bi + t;
+  const bool diag = bi == bj;
+  const long long nchunk = P * qchunks;
+  const long long c0 = nchunk * blockIdx.y / ksplit, c1 = nchunk * (blockIdx.y + 1) / ksplit;
+  const int nit = (int)(c1 - c0);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < TCG_STAGES; ++s) {
+      mbar_init(&S.full[s], 1);
+      mbar_init(&S.empty[s], 1);
+    }
+    mbar_init(&S.done, 1);
+    S.abort = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 128;" ::"r"(smem_u32(&S.tmem_base))
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = S.tmem_base;
+  const uint32_t tx = diag ? TCG_TILE_BYTES : 2 * TCG_TILE_BYTES;
+
+  if (warp == 0 && lane == 0) {
+    // producer: TMA loads into the ring
+    int issued = 0;
+    for (int it = 0; it < nit; ++it) {
+      const int s = it % TCG_STAGES;
+      if (it >= TCG_STAGES) {
+        if (!mbar_wait(&S.empty[s], ((it / TCG_STAGES) - 1) & 1)) {
+          atomicExch(err, 1);
+          S.abort = 1;
+          break;
+        }
+      }
+      if (*(volatile int*)&S.abort) break;
+      const long long c = c0 + it;
+      const int p = (int)(c / qchunks);
+      const int q = (int)(c - (long long)p * qchunks) * TCG_BK;
+      mbar_expect_tx(&S.full[s], tx);
+      tma_load_3d(S.a[s], &tmap, &S.full[s], q, bi * TCG_BM, p);
+      if (!diag) tma_load_3d(S.b[s], &tmap, &S.full[s], q, bj * TCG_BM, p);
+      ++issued;
+    }
+    // on abort: wait (bounded) for the copies already issued to land
+    if (*(volatile int*)&S.abort) {
+      for (int it = (issued > TCG_STAGES ? issued - TCG_STAGES : 0); it < issued; ++it)
+        mbar_wait(&S.full[it % TCG_STAGES], (it / TCG_STAGES) & 1);
+    }
+  } else if (warp == 1 && lane == 0) {
+    // MMA issuer
+    constexpr uint32_t idesc = tf32_idesc();
+    for (int it = 0; it < nit; ++it) {
+      const int s = it % TCG_STAGES;
+      if (!mbar_wait(&S.full[s], (it / TCG_STAGES) & 1)) {
+        atomicExch(err, 2);
+        S.abort = 1;
+        break;
+      }
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const uint64_t da = sw128_desc(S.a[s]);
+      const uint64_t db = sw128_desc(diag ? S.a[s] : S.b[s]);
+#pragma unroll
+      for (int kk = 0; kk < TCG_BK / 8; ++kk) {
+        // advance 8 tf32 (32 bytes) along K inside the swizzle atom
+        mma_tf32(tmem, da + (uint64_t)(kk * 2), db + (uint64_t)(kk * 2), idesc, (it > 0 || kk > 0) ? 1u : 0u);
+      }
+      mma_commit(&S.empty[s]);
+    }
+    mma_commit(&S.done);
+  }
+  __syncwarp();
+  // epilogue: one thread waits for the accumulator, the outcome is shared so
+  // that the warp-collective TMEM loads below run uniformly
+  if (threadIdx.x == 0) {
+    if (!mbar_wait(&S.done, 0)) {
+      atomicExch(err, 3);
+      S.abort = 1;
+    }
+  }
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const bool ok_all = !*(volatile int*)&S.abort;
+  if (ok_all && nit > 0) {
+    float* out = part + (size_t)blockIdx.y * D * D;
+    const int row = bi * TCG_BM + warp * 32 + lane;
+#pragma unroll 1
+    for (int cc = 0; cc < TCG_BM; cc += 32) {
+      uint32_t v[32];
+      const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)cc;
+      asm volatile(
+          "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+          "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+          : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+            "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15]),
+            "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]), "=r"(v[22]), "=r"(v[23]),
+            "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
+          : "r"(taddr));
+      asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+      if (row < D) {
+        const int col0 = bj * TCG_BM + cc;
+        float* o = out + (size_t)row * D + col0;
+        for (int j = 0; j < 32; ++j)
+          if (col0 + j < D) o[j] = __uint_as_float(v[j]);
+      }
+    }
+  } else if (ok_all && nit == 0) {
+    // empty contraction slice: the partial block is zero
+    float* out = part + (size_t)blockIdx.y * D * D;
+    for (int e = threadIdx.x; e < TCG_BM * TCG_BM; e += blockDim.x) {
+      const int r = bi * TCG_BM + e / TCG_BM, c = bj * TCG_BM + e % TCG_BM;
+      if (r < D && c < D) out[(size_t)r * D + c] = 0.f;
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 0) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 128;" ::"r"(tmem) : "memory");
+  }
+}
+
+__global__ void k_gram_tc_reduce(const float* __restrict__ part, int D, int ksplit, float* __restrict__ G) {
+  const long long n = (long long)D * D;
+  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(e / D), j = (int)(e - (long long)i * D);
+    const long long src = (i / TCG_BM <= j / TCG_BM) ? e : (long long)j * D + i;
+    double s = 0.0;
+    for (int k = 0; k < ksplit; ++k) s += (double)part[(size_t)k * n + src];
+    G[e] = (float)s;
+  }
+}
+
+}  // namespace tfx
+
+using namespace tfx;
+
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+static EncodeTiledFn encode_fn() {
+  static EncodeTiledFn fn = nullptr;
+  if (!fn) {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = (EncodeTiledFn)p;
+  }
+  return fn;
+}
+
+static int sm_count() {
+  static int n = 0;
+  if (!n) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    if (n < 1) n = 1;
+  }
+  return n;
+}
+
+static int tc_splits(long long P, int D, long long Q) {
+  const int nt = (D + TCG_BM - 1) / TCG_BM;
+  const long long tiles = (long long)nt * (nt + 1) / 2;
+  const long long chunks = P * ((Q + TCG_BK - 1) / TCG_BK);
+  long long ks = (sm_count() + tiles - 1) / tiles;
+  ks = std::min<long long>(ks, std::max<long long>(1, chunks / 8));
+  return (int)std::max<long long>(1, std::min<long long>(ks, 64));
+}
+
+extern "C" size_t tfx_mode_gram_tc_scratch_bytes(long long P, int D, long long Q) {
+  return (size_t)tc_splits(P, D, Q) * D * D * 4 + 16;
+}
+
+extern "C" int tfx_mode_gram_tc(const float* S, long long P, int D, long long Q, float* G, void* scratch,
+                                size_t scratch_bytes, int* err, void* stream) {
+  if (!S || !G || !scratch || !err || P < 1 || D < 1 || Q < TCG_BK)
+    return tfx_set_error(TFX_STATUS_ERR_ARG, "mode_gram_tc args");
+  if ((Q % 4) != 0 || ((uintptr_t)S & 15) != 0)
+    return tfx_set_error(TFX_STATUS_ERR_ARG, "mode_gram_tc needs Q % 4 == 0 and a 16-byte aligned tensor");
+  if (P > 0x7fffffffLL || Q > 0x7fffffffLL) return tfx_set_error(TFX_STATUS_ERR_ARG, "mode_gram_tc extent");
+  EncodeTiledFn enc = encode_fn();
+  if (!enc) return tfx_set_error(TFX_STATUS_ERR_UNSUPPORTED, "cuTensorMapEncodeTiled unavailable");
+  int ks = tc_splits(P, D, Q);
+  const size_t per = (size_t)D * D * 4;
+  if (scratch_bytes < per) return tfx_set_error(TFX_STATUS_ERR_ARG, "mode_gram_tc scratch too small");
+  ks = (int)std::min<size_t>((size_t)ks, scratch_bytes / per);
+  CUtensorMap map;
+  const cuuint64_t gdim[3] = {(cuuint64_t)Q, (cuuint64_t)D, (cuuint64_t)P};
+  const cuuint64_t gstride[2] = {(cuuint64_t)Q * 4, (cuuint64_t)Q * D * 4};
+  const cuuint32_t box[3] = {TCG_BK, TCG_BM, 1};
+  const cuuint32_t estr[3] = {1, 1, 1};
+  CUresult r = enc(&map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, (void*)S, gdim, gstride, box, estr,
+                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return tfx_set_error(TFX_STATUS_ERR_ARG, "tensor map encoding failed");
+  const int nt = (D + TCG_BM - 1) / TCG_BM;
+  const int tiles = nt * (nt + 1) / 2;
+  const int qchunks = (int)((Q + TCG_BK - 1) / TCG_BK);
+  const size_t sm = sizeof(TcGramSmem) + 1024;
+  cudaStream_t st = (cudaStream_t)stream;
+  cudaError_t e = cudaFuncSetAttribute(k_gram_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  if (e != cudaSuccess) return tfx_set_cuda_error(e, "mode_gram_tc smem");
+  k_gram_tc<<<dim3(tiles, ks), 128, sm, st>>>(map, D, P, qchunks, ks, (float*)scratch, err);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return tfx_set_cuda_error(e, "mode_gram_tc launch");
+  tfx_count_launch(1);
+  const long long n = (long long)D * D;
+  const int rb = (int)std::max<long long>(1, std::min<long long>((n + 255) / 256, 4LL * sm_count()));
+  k_gram_tc_reduce<<<rb, 256, 0, st>>>((const float*)scratch, D, ks, G);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return tfx_set_cuda_error(e, "mode_gram_tc reduce");
+  tfx_count_launch(1);
+  return TFX_STATUS_OK;
+}

@@ -94,6 +94,7 @@ _EXTRA_SIGNATURES = {
     "tfx_cp_residual": [_I, _P, _I, POINTER(c_int), _I, _P, _P, _P, _P],
     "tfx_tensor_norms": [_I, _P, _LL, _P, _P, _P],
     "tfx_coo_encode": [_P, _LL, _I, POINTER(c_int), _P, _P, _P],
+    "tfx_mode_gram_tc": [_P, _LL, _I, _LL, _P, _P, _SZ, _P, _P],
     "tfx_coo_sort_mode": [_I, _P, _P, _LL, _I, POINTER(c_int), _I, _P, _P, _P, _P, _P],
     "tfx_coo_mttkrp": [_I, _P, _P, _LL, _P, _I, POINTER(c_int), _I, _I, _P, _P, _P],
     "tfx_sparse_residual": [_I, _P, _P, _LL, _I, POINTER(c_int), _I, _P, _P, _P, _P],
@@ -103,6 +104,7 @@ _EXTRA_SIGNATURES = {
 _SIZE_FUNCS = {
     "tfx_mode_gram_scratch_bytes": [_I, _LL, _I, _LL],
     "tfx_sym_eig_smem_bytes": [_I, _I],
+    "tfx_mode_gram_tc_scratch_bytes": [_LL, _I, _LL],
     "tfx_cp_residual_scratch_bytes": [],
     "tfx_sparse_residual_scratch_bytes": [],
     "tfx_coo_gram_scratch_bytes": [_LL, _I],

@@ -76,6 +76,8 @@ def _precision(T, options):
     p = options.precision
     if p in ('fp64', 'fp32'):
         return p
+    if p == 'mixed':
+        return 'fp32'
     if isinstance(T, torch.Tensor):
         return 'fp64' if T.dtype == torch.float64 else 'fp32'
     if isinstance(T, list):

@@ -67,11 +67,15 @@ def top_eig(G, n, omega=None):
     return Ut, lam
 
 
-def _mode_svd(S, shape, l, n, tol_mlsvd, L, draw_cols):
-    """One mode: Gram, eigenpairs, signs, truncation. Returns (Ut, sigma, dim)."""
-    D = int(shape[l])
+def _mode_svd(S, shape, l, n, tol_mlsvd, L, draw_cols, tensor_cores=False):
+    """One mode: Gram, eigenpairs, signs, truncation. Returns (Ut, sigma, dim).
+
+    ``tensor_cores`` selects the TF32 tcgen05 Gram when the mode allows it."""
     omega = _draw_omega(draw_cols, n + 10)
-    G = kernels.mode_gram(S, shape, l)
+    if tensor_cores and kernels.tc_gram_supported(S, shape, l):
+        G = kernels.mode_gram_tc(S, shape, l)
+    else:
+        G = kernels.mode_gram(S, shape, l)
     Ut, lam = top_eig(G, n, omega)
     sigma = np.sqrt(np.maximum(lam, 0.0))
     dim = clean_compression(sigma, tol_mlsvd, L)
@@ -97,18 +101,19 @@ def mlsvd_device(Td, R, options):
         eye = [torch.eye(d, dtype=Td.dtype, device=Td.device) for d in shape]
         return Td, eye, [np.ones(d) for d in shape], shape
     Uts, sigmas = [], []
+    tc = getattr(o, 'precision', None) == 'mixed'
     if o.mlsvd_method in ('seq', 'gpu'):
         S, cur = Td, list(shape)
         for l in range(L):
             n = o.svd_n_components if o.svd_n_components is not None else min(R, shape[l])
-            Ut, sig, dim = _mode_svd(S, cur, l, n, tol_mlsvd, L, _ref_draw_cols(cur, l))
+            Ut, sig, dim = _mode_svd(S, cur, l, n, tol_mlsvd, L, _ref_draw_cols(cur, l), tc)
             Uts.append(Ut)
             sigmas.append(sig)
             S, cur = kernels.ttm(S, cur, l, Ut)
     elif o.mlsvd_method == 'classic':
         for l in range(L):
             n = o.svd_n_components if o.svd_n_components is not None else min(R, shape[l])
-            Ut, sig, dim = _mode_svd(Td, shape, l, n, tol_mlsvd, L, _ref_draw_cols(shape, l))
+            Ut, sig, dim = _mode_svd(Td, shape, l, n, tol_mlsvd, L, _ref_draw_cols(shape, l), tc)
             Uts.append(Ut)
             sigmas.append(sig)
         S, cur = Td, list(shape)

@@ -145,8 +145,10 @@ def _precision_of(T, options):
     p = getattr(options, 'precision', None)
     if p in ('fp64', 'fp32'):
         return p
+    if p == 'mixed':
+        return 'fp32'
     if p not in (None, 'auto'):
-        raise ValueError("precision must be 'fp64', 'fp32' or None")
+        raise ValueError("precision must be 'fp64', 'fp32', 'mixed' or None")
     if isinstance(T, torch.Tensor):
         return 'fp64' if T.dtype == torch.float64 else 'fp32'
     return 'fp64' if np.asarray(T).dtype == np.float64 else 'fp32'

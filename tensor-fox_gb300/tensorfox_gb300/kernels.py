@@ -40,6 +40,29 @@ def mode_gram(S, shape, l):
     return G
 
 
+def tc_gram_supported(S, shape, l):
+    """The tensor-core Gram needs FP32, Q = prod(shape[l+1:]) >= 32 with Q % 4 == 0."""
+    Q = int(np.prod(shape[l + 1:], dtype=np.int64))
+    return S.dtype == torch.float32 and Q >= 32 and Q % 4 == 0 and S.data_ptr() % 16 == 0
+
+
+def mode_gram_tc(S, shape, l):
+    """``S_(l) S_(l)^T`` on the tensor cores (tcgen05 kind::tf32, FP32 accumulation)."""
+    P = int(np.prod(shape[:l], dtype=np.int64))
+    D = int(shape[l])
+    Q = int(np.prod(shape[l + 1:], dtype=np.int64))
+    lib = _lib.load()
+    nb = int(lib.tfx_mode_gram_tc_scratch_bytes(P, D, Q))
+    scratch = torch.empty(nb, dtype=torch.uint8, device=S.device)
+    err = torch.zeros(1, dtype=torch.int32, device=S.device)
+    G = torch.empty((D, D), dtype=torch.float32, device=S.device)
+    _lib.call("tfx_mode_gram_tc", _vp(S), P, D, Q, _vp(G), _vp(scratch), nb, _vp(err), _st())
+    e = int(err.item())
+    if e != 0:
+        raise _lib.TfxError("tensor-core Gram: bounded wait expired (code %d)" % e)
+    return G
+
+
 def gemm(A, B, C, M, N, K, batch, strides, alpha=1.0, beta=0.0):
     arr = (ctypes.c_longlong * 9)(*[int(s) for s in strides])
     _lib.call("tfx_gemm", _dt(A), _vp(A), _vp(B), _vp(C), int(M), int(N), int(K), int(batch), arr,

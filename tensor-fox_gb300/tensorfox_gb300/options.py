@@ -3,7 +3,8 @@
 ``make_options`` copies every attribute the caller's object defines over the
 defaults, exactly like the reference.  Two fields are added by this package and
 ignored by the reference: ``precision`` ('fp64', 'fp32' or None for the input's
-own type) and ``cluster`` (CTAs per problem in the device engine, None = auto).
+own type, 'mixed' = FP32 data with TF32 tensor-core contractions for the
+compression) and ``cluster`` (CTAs per problem in the device engine, None = auto).
 """
 
 _DEFAULTS = dict(maxiter=200, tol=1e-16, tol_step=1e-6, tol_improv=1e-6, tol_grad=1e-6, tol_jump=10,
