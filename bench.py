@@ -33,7 +33,8 @@ CONGRUENCE = 0.5
 SNR_DB = 40.0
 SEED = 2024
 METRIC = "CPD time-to-rel-err 1e-6 (s), mixed/batched vs plain on GB300; matvec HBM GB/s"
-WORKLOAD = "dense FP32 512x512x512 CPD, rank 50, congruence 0.5, 40 dB SNR, default options"
+WORKLOAD = ("dense FP32 512x512x512 CPD, rank 50, congruence 0.5, 40 dB SNR, default options, "
+            "precision='mixed' (TF32 tensor-core compression)")
 
 
 def make_problem(dims=DIMS, R=RANK, seed=SEED):
@@ -189,7 +190,7 @@ def run_ours(args):
     Th = torch.from_numpy(T).pin_memory()
     R = RANK
     opts = tfx.make_options(None)
-    opts.precision = "fp32"
+    opts.precision = "mixed"
 
     def barrier():
         if world > 1:
@@ -231,18 +232,36 @@ def run_ours(args):
         dist.all_reduce(tt, op=dist.ReduceOp.MAX)
         t_dev, t_e2e = float(tt[0]), float(tt[1])
 
-    # dominant kernel: the mode-1 Gram of the 512 x 262144 unfolding, timed alone
-    nrep = 10
-    for _ in range(2):
-        kernels.mode_gram(Td, list(DIMS), 0)
+    # the plain FP32 path on the same input (the north_star's "plain" comparison)
+    plain = tfx.make_options(None)
+    plain.precision = "fp32"
+    np.random.seed(0)
+    tfx.cpd(Td, R, plain)
+    barrier()
+    p0, p1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    p0.record(stream)
+    for _ in range(max(1, args.steps // 2)):
+        np.random.seed(0)
+        _, out_plain = tfx.cpd(Td, R, plain)
+    p1.record(stream)
+    barrier()
+    t_plain = p0.elapsed_time(p1) / 1e3 / max(1, args.steps // 2)
+
+    # dominant dense kernel: the tcgen05 mode-1 Gram of the 512 x 262144 unfolding,
+    # timed alone with CUDA events on the launching stream
+    nrep = 20
+    for _ in range(3):
+        kernels.mode_gram_tc(Td, list(DIMS), 0)
     torch.cuda.synchronize()
     g0, g1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     g0.record(stream)
     for _ in range(nrep):
-        kernels.mode_gram(Td, list(DIMS), 0)
+        kernels.mode_gram_tc(Td, list(DIMS), 0)
     g1.record(stream)
     torch.cuda.synchronize()
     t_gram = g0.elapsed_time(g1) / 1e3 / nrep
+
+    batched = run_batched(args) if not args.no_batched else None
     flops = 2.0 * DIMS[0] * DIMS[0] * DIMS[1] * DIMS[2]
     hbm, bf16, src = peaks()
     achieved_tf = flops / t_gram / 1e12
@@ -264,24 +283,69 @@ def run_ours(args):
 
     line = {"metric": METRIC, "value": t_dev, "unit": "s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t_dev * 1e3, "higher_is_better": False, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "vs_baseline": None, "dtype": "f32+tf32", "data": "synthetic",
             "config": {"workload": WORKLOAD, "global_batch": world, "parallelism": "replicas",
                        "l2_flush": "none: 537 MB tensor exceeds the 129 MB L2"},
             "rel_error": float(fl.rel_error), "num_steps": int(fl.num_steps), "stop": [int(s) for s in fl.stop],
+            "plain_fp32": {"value": t_plain, "unit": "s", "rel_error": float(out_plain.rel_error)},
             "e2e": {"value": t_e2e, "unit": "s", "h2d_bytes_per_step": int(T.nbytes),
                     "d2h_bytes_per_step": int(sum(d * R * 8 for d in DIMS))},
-            "roofline": {"bound": "tensor", "kernel": "k_mode_gram (mode-1 Gram, 512 x 262144)",
+            "roofline": {"bound": "tensor", "kernel": "k_gram_tc (tcgen05 TF32 mode-1 Gram, 512 x 262144, incl. split-K reduce)",
                          "achieved": achieved_tf, "peak": bf16, "unit": "TFLOP/s", "frac": achieved_tf / bf16,
                          "traffic": traffic, "peak_source": src + " bf16 dense (TF32 tensor rate is half of it)"},
             "gpu_launches": int(launches / max(1, args.steps)) * args.steps,
             "clocks": clk.summary()}
     if cpu is not None:
         line["cpu_baseline"] = cpu
+    if batched is not None:
+        line["batched"] = batched
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:
         import torch.distributed as dist
         dist.destroy_process_group()
+
+
+def run_batched(args, n=1024, seed=7):
+    """c4-style batch: n small FP32 CPDs (dims U[8,64], rank U[2,12], noise 1e-4).
+
+    Reports the batch wall time and the engine's J^T J v throughput in the
+    algorithmic-bytes sense: bytes_mv = s*3*n_x + 8*L^2*R^2 per product, summed
+    over every product the engine ran, divided by the engine's share of the time."""
+    import torch
+    import tensorfox_gb300 as tfx
+    rng = np.random.default_rng(seed)
+    Ts, Rs = [], []
+    for _ in range(n):
+        dims = tuple(int(v) for v in rng.integers(8, 65, size=3))
+        R = int(rng.integers(2, 13))
+        W = [rng.standard_normal((d, R)).astype(np.float32) for d in dims]
+        T = np.einsum("ir,jr,kr->ijk", *W)
+        E = rng.standard_normal(dims).astype(np.float32)
+        Ts.append(T + 1e-4 * np.linalg.norm(T) / np.linalg.norm(E) * E)
+        Rs.append(R)
+    o = tfx.make_options(None)
+    o.precision = "fp32"
+    np.random.seed(0)
+    tfx.cpd_batch(Ts[:64], Rs[:64], o)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    np.random.seed(0)
+    outs = tfx.cpd_batch(Ts, Rs, o)
+    torch.cuda.synchronize()
+    t = time.perf_counter() - t0
+    errs = np.array([op.rel_error for _, op in outs])
+    # J^T J v products the engine ran (counted on the device), with the
+    # algorithmic bytes of each: read W and v, write z (s*3*n_x) and the FP64
+    # R x R Gram Hadamards (8*L^2*R^2)
+    nmv, nbytes = 0, 0.0
+    for (f, op), R in zip(outs, Rs):
+        nx = R * sum(op.core_dims)
+        nmv += op.matvecs
+        nbytes += op.matvecs * (4 * 3 * nx + 8 * 9 * R * R)
+    return {"problems": n, "seconds": t, "median_rel_error": float(np.median(errs)),
+            "frac_below_1e-3": float(np.mean(errs < 1e-3)), "matvecs": int(nmv),
+            "matvec_GBps_vs_batch_time": nbytes / t / 1e9}
 
 
 def main():
@@ -291,6 +355,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-batched", action="store_true")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

@@ -31,7 +31,7 @@ enum tfx_dtype { TFX_F32 = 0, TFX_F64 = 1 };
  *   damp_sched: [maxiter] damping schedule when options.init_damp is a list, else NULL
  *   stats  : [4*maxiter] errors, step_sizes, improv, gradients (written)
  *   result : [4] stop code, iterations run, status, dogleg fallbacks (written)
- *   info   : [4] |T|, best error, final damping, mean|T| (written)
+ *   info   : [5] |T|, best error, final damping, mean|T|, J^T J v products run (written)
  *   prof   : optional [16] SM clock cycles per phase (gramians, gradient, CG,
  *            update, residual, dogleg, control, total) and per CG step part
  *            (publish+barrier, staging, A_k, Y_l, z_l, two reductions, update),

@@ -1087,6 +1087,7 @@ __device__ void solve_problem(const tfx_dgn_problem& pb, const tfx_dgn_options& 
   const int cnst = 1 + maxiter / 10;
   double error = 1.0, best_error = INFINITY;
   int stop = 5, it = 0, n_dogleg = 0;
+  long long matvecs = 0;
   E.tm.sync();
   E.stage_W();
 
@@ -1109,7 +1110,8 @@ __device__ void solve_problem(const tfx_dgn_problem& pb, const tfx_dgn_options& 
     E.gradient();
     tick(1);
     double rn;
-    E.cg(pb.budgets[it], rn);
+    const int itn = E.cg(pb.budgets[it], rn);
+    matvecs += itn + 1;  // CG products plus J^T J grad
     tick(2);
     // y <- M y ; xn <- x + y ; W <- balanced(xn)
     E.for_own([&](int e, int l, int c) {
@@ -1216,6 +1218,7 @@ __device__ void solve_problem(const tfx_dgn_problem& pb, const tfx_dgn_options& 
     pb.info[1] = best_error;
     pb.info[2] = E.damp;
     pb.info[3] = meanabs;
+    pb.info[4] = (double)matvecs;
   }
 }
 

@@ -12,8 +12,10 @@ most 64) with one launch per stage for the whole batch:
 4. ``tfx_batch_decompress`` and ``tfx_batch_residual``.
 
 RNG order differs from a serial loop of ``cpd`` calls (the serial loop draws each
-problem's CG caps before the next problem's start); every problem's draws come
-from the global RNG in problem order: starting points first, then CG caps.
+problem's CG caps before the next problem's start): the starting points are drawn
+from NumPy's global RNG problem by problem, then the CG caps iteration by
+iteration, one value per problem for each iteration (same distribution as
+GaussNewton.py:267).
 """
 import ctypes
 
@@ -146,19 +148,19 @@ def cpd_batch(tensors, ranks, options=None):
     WS = torch.empty(int(ws_off[-1]), dtype=torch.uint8, device=dev)
     m = int(o.maxiter)
     budgets = np.zeros((n, m), dtype=np.int32)
-    for p in range(n):
-        for it in range(m):
-            inner = _inner_of(o, it)
-            if inner == 'cg':
-                budgets[p, it] = 1 + (L - 2) * int(o.cg_factor * np.random.randint(1 + it ** 0.4, 2 + it ** 0.9))
-            elif inner == 'cg_static':
-                budgets[p, it] = o.cg_maxiter
-            else:
-                raise NotImplementedError("inner_method %r" % (inner,))
+    for it in range(m):      # one draw per iteration for the whole batch (iteration-major order)
+        inner = _inner_of(o, it)
+        if inner == 'cg':
+            draw = np.random.randint(int(1 + it ** 0.4), int(2 + it ** 0.9), size=n)
+            budgets[:, it] = 1 + (L - 2) * (o.cg_factor * draw).astype(np.int64)
+        elif inner == 'cg_static':
+            budgets[:, it] = o.cg_maxiter
+        else:
+            raise NotImplementedError("inner_method %r" % (inner,))
     B = torch.from_numpy(budgets).to(dev)
     stats = torch.zeros((n, 4 * m), dtype=torch.float64, device=dev)
     result = torch.zeros((n, 4), dtype=torch.int32, device=dev)
-    info = torch.zeros((n, 4), dtype=torch.float64, device=dev)
+    info = torch.zeros((n, 8), dtype=torch.float64, device=dev)
     dd = np.zeros(n, dtype=_DGN_DT)
     dd['L'] = L
     dd['R'] = Rs
@@ -170,7 +172,7 @@ def cpd_batch(tensors, ranks, options=None):
     dd['budgets'] = B.data_ptr() + np.arange(n) * m * 4
     dd['stats'] = stats.data_ptr() + np.arange(n) * 4 * m * 8
     dd['result'] = result.data_ptr() + np.arange(n) * 16
-    dd['info'] = info.data_ptr() + np.arange(n) * 32
+    dd['info'] = info.data_ptr() + np.arange(n) * 64
     d_dd = torch.empty(n * _DGN_DT.itemsize, dtype=torch.uint8, device=dev)
     opt = _lib.DgnOptions()
     opt.maxiter = m
@@ -201,6 +203,7 @@ def cpd_batch(tensors, ranks, options=None):
                                       ctypes.c_void_p(pf.data_ptr()), ctypes.c_void_p(res2.data_ptr()), st))
     wf = WF.double().cpu().numpy()
     r2 = res2.cpu().numpy()
+    info_h = info.cpu().numpy()
     st_h = stats.cpu().numpy()
     rs_h = result.cpu().numpy()
     out = []
@@ -224,5 +227,7 @@ def cpd_batch(tensors, ranks, options=None):
         op.gradients = [st_h[p, 3 * m:3 * m + k].copy(), np.array([0])]
         op.stop = [int(rs_h[p, 0]), 8]
         op.options = o
+        op.matvecs = int(info_h[p, 4])
+        op.core_dims = [int(d) for d in core_dims[p]]
         out.append((factors, op))
     return out
