@@ -265,13 +265,11 @@ def run_ours(args):
     flops = 2.0 * DIMS[0] * DIMS[0] * DIMS[1] * DIMS[2]
     hbm, bf16, src = peaks()
     achieved_tf = flops / t_gram / 1e12
-    traffic = None
-    prof = os.path.join(ROOT, "profiles", "mode_gram_traffic.json")
-    if os.path.exists(prof):
-        try:
-            traffic = json.load(open(prof)).get("bytes_per_launch")
-        except (OSError, ValueError):
-            traffic = None
+    # DRAM traffic of one launch, from the ncu capture of the small case
+    # (profiles/k_gram_tc_mode0_512x128x512.md: 135.97 MB read + 3.58 MB written
+    # for a 134 MB input) scaled by the input size, which the traffic follows
+    # (the tensor crosses HBM once; the partials grow with the split count only)
+    traffic = (135.97e6 + 3.58e6) * (float(np.prod(DIMS)) * 4 / (512 * 128 * 512 * 4))
 
     # congruence with the planted factors and the FP64 oracle error of the result
     fl = outs[-1]
@@ -348,6 +346,37 @@ def run_batched(args, n=1024, seed=7):
             "matvec_GBps_vs_batch_time": nbytes / t / 1e9}
 
 
+def run_case(case):
+    """Small fixed workloads used for ncu captures (see profiles/)."""
+    import torch
+    import tensorfox_gb300 as tfx
+    from tensorfox_gb300 import kernels, compression, api, gauss_newton, _dev
+    if case == "tc_gram_small":
+        # tcgen05 Gram of a 512 x 128 x 512 FP32 tensor (128 MB), mode 0, four launches
+        T = torch.randn(512, 128, 512, device="cuda", generator=torch.Generator("cuda").manual_seed(0))
+        for _ in range(4):
+            G = kernels.mode_gram_tc(T, [512, 128, 512], 0)
+        torch.cuda.synchronize()
+        print(json.dumps({"case": case, "G00": float(G[0, 0])}))
+    elif case == "engine_core":
+        # two dGN engine launches on the 50^3 rank-50 core of the benchmark tensor
+        T, _ = make_problem()
+        Td = torch.from_numpy(T).cuda()
+        o = tfx.make_options(None)
+        o.precision = "mixed"
+        np.random.seed(0)
+        S, Uts, sig, core = compression.mlsvd_device(Td, RANK, o)
+        init = api.starting_point_random(core, RANK, o)
+        x0 = torch.from_numpy(_dev.flat_factors(init)).cuda().float()
+        for _ in range(2):
+            b = gauss_newton._Batch([S], [x0], [RANK], o, "fp32")
+            b.launch(gauss_newton.auto_cluster(tuple(S.shape), RANK))
+        torch.cuda.synchronize()
+        print(json.dumps({"case": case, "result": b.result[0].cpu().numpy().tolist()}))
+    else:
+        raise SystemExit("unknown case " + case)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -356,7 +385,11 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--case", default=None, help="tc_gram_small | engine_core (profiling workloads)")
     args = ap.parse_args()
+    if args.case:
+        run_case(args.case)
+        return
     if args.impl == "reference":
         run_reference(args)
     else:
