@@ -62,6 +62,13 @@ int tfx_mode_gram(int dtype, const void* S, long long P, int D, long long Q, voi
  * strides = {sAb, sAm, sAk, sBb, sBk, sBn, sCb, sCm, sCn} (elements). */
 int tfx_gemm(int dtype, const void* A, const void* B, void* C, long long M, long long N, long long K, long long batch,
              const long long* strides, double alpha, double beta, void* stream);
+/* Mode-l product with a truncated factor, out[p] (n x Q) = Ut (n x D) S[p] (D x Q)
+ * for S of shape (P, D, Q) and Ut (n x D), all row-major (Compression.py:153-156,
+ * the multilin_mult of MultilinearAlgebra.py:72-105 with U_l^T).  FP32 with
+ * D, Q multiples of 4 runs a dedicated register-tiled kernel; other shapes use
+ * tfx_gemm. */
+int tfx_ttm(int dtype, const void* S, long long P, int D, long long Q, const void* Ut, int n, void* out,
+            void* stream);
 /* The same Gram on the 5th-generation tensor cores: TMA-fed SWIZZLE_128B tiles,
  * tcgen05.mma kind::tf32 into TMEM, FP32 accumulation, split-K partials summed
  * in FP64.  FP32 input only; Q >= 32 and Q % 4 == 0; S 16-byte aligned.  *err

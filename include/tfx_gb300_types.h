@@ -32,10 +32,11 @@ enum tfx_dtype { TFX_F32 = 0, TFX_F64 = 1 };
  *   stats  : [4*maxiter] errors, step_sizes, improv, gradients (written)
  *   result : [4] stop code, iterations run, status, dogleg fallbacks (written)
  *   info   : [5] |T|, best error, final damping, mean|T|, J^T J v products run (written)
- *   prof   : optional [16] SM clock cycles per phase (gramians, gradient, CG,
- *            update, residual, dogleg, control, total) and per CG step part
- *            (publish+barrier, staging, A_k, Y_l, z_l, two reductions, update),
- *            or NULL */
+ *   prof   : optional [24] SM clock cycles per phase (gramians, gradient, CG,
+ *            update, residual, dogleg, control, total), per CG step part
+ *            (publish+barrier, staging, A_k, Y_l, z_l, two reductions, update)
+ *            and per third-order gradient part (setup, chunk issue, chunk wait,
+ *            Y and M2, barrier, M0 and M1, finish, team barrier), or NULL */
 typedef struct tfx_dgn_problem {
   int L;
   int R;

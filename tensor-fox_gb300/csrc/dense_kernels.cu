@@ -163,6 +163,116 @@ __global__ void __launch_bounds__(TFX_THREADS) k_gemm(const T* __restrict__ A, c
 }
 
 // ---------------------------------------------------------------------------
+// Mode product for FP32 with a short left factor: out[p] (n x Q) = Ut (n x D)
+// times S[p] (D x Q), all row-major.  One warp owns 8 rows of the output tile
+// and each lane 8 x TN outputs; per 4 k steps a lane reads 8 broadcast float4
+// of Ut and TN float4 of S for 32*TN FMAs.  The (BK x BN) slab of S and the
+// (BM x BK) slab of Ut are double-buffered in shared memory and filled with
+// cp.async (16-byte copies, zero-filled past the edges), so the next slab
+// streams in while the current one is multiplied.  The block has
+// 32 * ceil(rows/8) threads (at most 8 warps): a 50-row factor wastes 6 rows
+// instead of 14.  Needs D % 4 == 0, Q % 4 == 0 and 16-byte aligned pointers.
+// ---------------------------------------------------------------------------
+constexpr int TTM_BK = 16;
+
+__device__ __forceinline__ void cp_async16(void* sdst, const void* gsrc, int src_bytes) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(sdst);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(sa), "l"(gsrc), "r"(src_bytes) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+
+template <int TN>
+__global__ void __launch_bounds__(256, 2) k_ttm_f32(const float* __restrict__ Ut, const float* __restrict__ S,
+                                                    float* __restrict__ out, int n, int D, long long Q, long long P) {
+  constexpr int BN = 32 * TN;
+  constexpr int AKS = TTM_BK + 4;  // padded row stride of the Ut slab
+  __shared__ __align__(16) float sA[2][64][AKS];
+  __shared__ __align__(16) float sB[2][TTM_BK][BN];
+  const int nw = blockDim.x >> 5, nt = blockDim.x;
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  const int BM = 8 * nw;
+  const int m0 = blockIdx.z * BM;
+  const long long q0 = (long long)blockIdx.x * BN;
+  const int nk = (D + TTM_BK - 1) / TTM_BK;
+  for (long long p = blockIdx.y; p < P; p += gridDim.y) {
+    const float* Sp = S + p * (long long)D * Q;
+    auto issue = [&](int t, int b) {
+      const int k0 = t * TTM_BK;
+      for (int e = tid; e < BM * (TTM_BK / 4); e += nt) {
+        const int m = e >> 2, k4 = (e & 3) * 4;
+        const bool ok = m0 + m < n && k0 + k4 < D;
+        cp_async16(&sA[b][m][k4], ok ? (const void*)(Ut + (long long)(m0 + m) * D + k0 + k4) : (const void*)Ut,
+                   ok ? 16 : 0);
+      }
+      for (int e = tid; e < TTM_BK * (BN / 4); e += nt) {
+        const int kk = e / (BN / 4), c4 = (e - kk * (BN / 4)) * 4;
+        const bool ok = k0 + kk < D && q0 + c4 < Q;
+        cp_async16(&sB[b][kk][c4], ok ? (const void*)(Sp + (long long)(k0 + kk) * Q + q0 + c4) : (const void*)Sp,
+                   ok ? 16 : 0);
+      }
+      cp_async_commit();
+    };
+    float acc[8][TN];
+#pragma unroll
+    for (int i = 0; i < 8; ++i)
+#pragma unroll
+      for (int j = 0; j < TN; ++j) acc[i][j] = 0.f;
+    __syncthreads();  // the previous p's readers are done with both buffers
+    issue(0, 0);
+    for (int t = 0; t < nk; ++t) {
+      const int b = t & 1;
+      if (t + 1 < nk) {
+        issue(t + 1, b ^ 1);
+        cp_async_wait<1>();
+      } else {
+        cp_async_wait<0>();
+      }
+      __syncthreads();
+#pragma unroll
+      for (int k4 = 0; k4 < TTM_BK; k4 += 4) {
+        float4 a[8];
+#pragma unroll
+        for (int i = 0; i < 8; ++i) a[i] = *(const float4*)&sA[b][wid * 8 + i][k4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          float bv[TN];
+#pragma unroll
+          for (int j4 = 0; j4 < TN / 4; ++j4) {
+            const float4 v = *(const float4*)&sB[b][k4 + u][j4 * 128 + lane * 4];
+            bv[4 * j4 + 0] = v.x;
+            bv[4 * j4 + 1] = v.y;
+            bv[4 * j4 + 2] = v.z;
+            bv[4 * j4 + 3] = v.w;
+          }
+#pragma unroll
+          for (int i = 0; i < 8; ++i) {
+            const float ai = u == 0 ? a[i].x : u == 1 ? a[i].y : u == 2 ? a[i].z : a[i].w;
+#pragma unroll
+            for (int j = 0; j < TN; ++j) acc[i][j] = fmaf(ai, bv[j], acc[i][j]);
+          }
+        }
+      }
+      __syncthreads();  // slab b is free for the copy issued next iteration
+    }
+    float* op = out + p * (long long)n * Q;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      const int m = m0 + wid * 8 + i;
+      if (m >= n) continue;
+#pragma unroll
+      for (int j4 = 0; j4 < TN / 4; ++j4) {
+        const long long q = q0 + j4 * 128 + lane * 4;
+        if (q < Q)
+          *(float4*)(op + (long long)m * Q + q) =
+              make_float4(acc[i][4 * j4], acc[i][4 * j4 + 1], acc[i][4 * j4 + 2], acc[i][4 * j4 + 3]);
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
 // CGS2 orthonormalisation of the k columns of Y (D x k, column-major), in place.
 // ---------------------------------------------------------------------------
 // Shared-memory variant: the whole D x k block lives in shared memory, so each
@@ -209,6 +319,251 @@ __global__ void __launch_bounds__(TFX_THREADS) k_orth_smem(T* Y, int D, int k) {
     __syncthreads();
   }
   for (int e = tid; e < D * k; e += TFX_THREADS) Y[e] = Ys[e];
+}
+
+// Blocked CGS2 (BCGS2): panels of ORTH_B columns are projected against the
+// finished columns twice with two matrix products (coefficients C = Q^T P,
+// then P -= Q C), and orthonormalised inside the panel by column CGS2 with
+// thread-private rows.  The serial chain is k / ORTH_B panel steps instead of
+// k column steps, and each finished column is read once per panel instead of
+// once per later column.  Y (D x k, column-major) is staged in shared memory
+// with a column stride ldy = D rounded up to 1 mod 32 elements, so that lanes
+// reading the same row of 32 different columns hit 32 different banks.
+constexpr int ORTH_NT = 256, ORTH_NW = ORTH_NT / 32, ORTH_B = 8;
+
+__host__ __device__ inline int orth_ldy(int D) { return D + ((33 - (D & 31)) & 31); }
+
+__host__ __device__ inline size_t orth_align16(size_t b) { return (b + 15) & ~(size_t)15; }
+
+template <class T>
+__device__ __forceinline__ void load_row8(const T* p, T (&v)[ORTH_B]) {
+#pragma unroll
+  for (int c = 0; c < ORTH_B; ++c) v[c] = p[c];
+}
+template <>
+__device__ __forceinline__ void load_row8<float>(const float* p, float (&v)[ORTH_B]) {
+  const float4 a = *(const float4*)p, b = *(const float4*)(p + 4);
+  v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
+  v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
+}
+template <>
+__device__ __forceinline__ void load_row8<double>(const double* p, double (&v)[ORTH_B]) {
+#pragma unroll
+  for (int c = 0; c < ORTH_B; c += 2) {
+    const double2 a = *(const double2*)(p + c);
+    v[c] = a.x;
+    v[c + 1] = a.y;
+  }
+}
+
+template <class T>
+static __host__ __device__ size_t orth_bcgs_offsets(int D, int k, size_t* oP, size_t* oPart, size_t* oC,
+                                                    size_t* oRed) {
+  size_t o = orth_align16((size_t)k * orth_ldy(D) * sizeof(T));
+  *oP = o;
+  o = orth_align16(o + (size_t)D * ORTH_B * sizeof(T));
+  *oPart = o;
+  o = orth_align16(o + (size_t)ORTH_NW * 32 * ORTH_B * sizeof(T));
+  *oC = o;
+  o = orth_align16(o + (size_t)k * ORTH_B * sizeof(T));
+  *oRed = o;
+  return o;
+}
+
+// Column CGS2 of the (D x cb) panel by one warp with the panel in registers:
+// lane l holds rows l, l + 32, ... (RPL of them).  Every loop is unrolled
+// over compile-time column indices, so the dots, shuffles and updates of a
+// column are independent instructions rather than a chain of shared-memory
+// round trips.
+template <class T, int RPL>
+__device__ __forceinline__ void panel_cgs2_warp(T* Pb, int D, int cb) {
+  const int lane = threadIdx.x & 31;
+  T v[RPL][ORTH_B];
+#pragma unroll
+  for (int t = 0; t < RPL; ++t) {
+    const int r = lane + 32 * t;
+    if (r < D) {
+      load_row8<T>(Pb + (size_t)r * ORTH_B, v[t]);
+    } else {
+#pragma unroll
+      for (int c = 0; c < ORTH_B; ++c) v[t][c] = T(0);
+    }
+  }
+#pragma unroll
+  for (int c = 0; c < ORTH_B; ++c) {
+    if (c < cb) {
+#pragma unroll
+      for (int pass = 0; pass < 2; ++pass) {
+        if (c > 0) {
+          T d[ORTH_B];
+#pragma unroll
+          for (int c2 = 0; c2 < c; ++c2) {
+            d[c2] = T(0);
+#pragma unroll
+            for (int t = 0; t < RPL; ++t) d[c2] = fma(v[t][c2], v[t][c], d[c2]);
+          }
+#pragma unroll
+          for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+            for (int c2 = 0; c2 < c; ++c2) d[c2] += __shfl_xor_sync(0xffffffffu, d[c2], o);
+#pragma unroll
+          for (int t = 0; t < RPL; ++t)
+#pragma unroll
+            for (int c2 = 0; c2 < c; ++c2) v[t][c] = fma(-d[c2], v[t][c2], v[t][c]);
+        }
+      }
+      T nq = T(0);
+#pragma unroll
+      for (int t = 0; t < RPL; ++t) nq = fma(v[t][c], v[t][c], nq);
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) nq += __shfl_xor_sync(0xffffffffu, nq, o);
+      const T inv = nq > T(0) ? T(1) / sqrt(nq) : T(0);
+#pragma unroll
+      for (int t = 0; t < RPL; ++t) v[t][c] *= inv;
+    }
+  }
+#pragma unroll
+  for (int t = 0; t < RPL; ++t) {
+    const int r = lane + 32 * t;
+    if (r < D)
+#pragma unroll
+      for (int c = 0; c < ORTH_B; ++c) Pb[(size_t)r * ORTH_B + c] = v[t][c];
+  }
+}
+
+template <class T, int RPL>
+__global__ void __launch_bounds__(ORTH_NT) k_orth_bcgs(T* Y, int D, int k) {
+  extern __shared__ __align__(16) char smem_b[];
+  size_t oP, oPart, oC, oRed;
+  orth_bcgs_offsets<T>(D, k, &oP, &oPart, &oC, &oRed);
+  const int ldy = orth_ldy(D);
+  T* Ys = (T*)smem_b;               // column j at Ys[j * ldy]
+  T* Pb = (T*)(smem_b + oP);        // panel, row r at Pb[r * ORTH_B]
+  T* part = (T*)(smem_b + oPart);   // partial coefficients [slice][i][c]
+  T* C = (T*)(smem_b + oC);         // coefficients [i][c]
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  for (int e = tid; e < D * k; e += ORTH_NT) {
+    const int j = e / D, r = e - j * D;
+    Ys[(size_t)j * ldy + r] = Y[e];
+  }
+  for (int j0 = 0; j0 < k; j0 += ORTH_B) {
+    const int cb = min(ORTH_B, k - j0);
+    __syncthreads();
+    for (int e = tid; e < D * ORTH_B; e += ORTH_NT) {
+      const int r = e / ORTH_B, c = e - r * ORTH_B;
+      Pb[e] = c < cb ? Ys[(size_t)(j0 + c) * ldy + r] : T(0);
+    }
+    __syncthreads();
+    if (j0 > 0) {
+      const int g = (j0 + 31) >> 5;        // groups of 32 finished columns
+      const int S = ORTH_NW / g;           // row slices
+      const int rows = (D + S - 1) / S;
+      for (int pass = 0; pass < 2; ++pass) {
+        // C = Q^T P: warp (grp, slice) forms 32 columns x ORTH_B partial dots
+        const int grp = wid % g, slice = wid / g;
+        const int i = grp * 32 + lane;
+        if (slice < S && i < j0) {
+          T acc[ORTH_B];
+#pragma unroll
+          for (int c = 0; c < ORTH_B; ++c) acc[c] = T(0);
+          const int r0 = slice * rows, r1 = min(D, r0 + rows);
+          const T* yi = Ys + (size_t)i * ldy;
+#pragma unroll 4
+          for (int r = r0; r < r1; ++r) {
+            const T y = yi[r];
+            T pv[ORTH_B];
+            load_row8<T>(Pb + (size_t)r * ORTH_B, pv);
+#pragma unroll
+            for (int c = 0; c < ORTH_B; ++c) acc[c] = fma(y, pv[c], acc[c]);
+          }
+#pragma unroll
+          for (int c = 0; c < ORTH_B; ++c) part[((size_t)slice * g * 32 + i) * ORTH_B + c] = acc[c];
+        }
+        __syncthreads();
+        for (int e = tid; e < j0 * ORTH_B; e += ORTH_NT) {
+          const int ii = e / ORTH_B, c = e - ii * ORTH_B;
+          T x = T(0);
+          for (int sl = 0; sl < S; ++sl) x += part[((size_t)sl * g * 32 + ii) * ORTH_B + c];
+          C[e] = x;
+        }
+        __syncthreads();
+        // P -= Q C, one row per thread
+        for (int r = tid; r < D; r += ORTH_NT) {
+          T v[ORTH_B];
+          load_row8<T>(Pb + (size_t)r * ORTH_B, v);
+#pragma unroll 4
+          for (int ii = 0; ii < j0; ++ii) {
+            const T y = Ys[(size_t)ii * ldy + r];
+            T cc[ORTH_B];
+            load_row8<T>(C + (size_t)ii * ORTH_B, cc);
+#pragma unroll
+            for (int c = 0; c < ORTH_B; ++c) v[c] = fma(-y, cc[c], v[c]);
+          }
+#pragma unroll
+          for (int c = 0; c < ORTH_B; ++c) Pb[(size_t)r * ORTH_B + c] = v[c];
+        }
+        __syncthreads();
+      }
+    }
+    // column CGS2 inside the panel by warp 0 alone: its sums are warp
+    // shuffles, so the 2 * ORTH_B - 1 dependent reductions of a panel cost no
+    // block barrier.  RPL > 0: the panel sits in registers (D <= 32 * RPL).
+    if (RPL > 0) {
+      if (wid == 0) panel_cgs2_warp<T, (RPL > 0 ? RPL : 1)>(Pb, D, cb);
+    } else if (wid == 0) {
+      for (int c = 0; c < cb; ++c) {
+        for (int pass = 0; pass < 2 && c > 0; ++pass) {
+          T d[ORTH_B];
+#pragma unroll
+          for (int c2 = 0; c2 < ORTH_B; ++c2) d[c2] = T(0);
+          for (int r = lane; r < D; r += 32) {
+            T v[ORTH_B];
+            load_row8<T>(Pb + (size_t)r * ORTH_B, v);
+            const T vc = Pb[(size_t)r * ORTH_B + c];
+#pragma unroll
+            for (int c2 = 0; c2 < ORTH_B; ++c2)
+              if (c2 < c) d[c2] = fma(v[c2], vc, d[c2]);
+          }
+#pragma unroll
+          for (int c2 = 0; c2 < ORTH_B; ++c2)
+            if (c2 < c)
+#pragma unroll
+              for (int o = 16; o > 0; o >>= 1) d[c2] += __shfl_xor_sync(0xffffffffu, d[c2], o);
+          for (int r = lane; r < D; r += 32) {
+            T v[ORTH_B];
+            load_row8<T>(Pb + (size_t)r * ORTH_B, v);
+            T x = Pb[(size_t)r * ORTH_B + c];
+#pragma unroll
+            for (int c2 = 0; c2 < ORTH_B; ++c2)
+              if (c2 < c) x = fma(-d[c2], v[c2], x);
+            Pb[(size_t)r * ORTH_B + c] = x;
+          }
+          __syncwarp();
+        }
+        T nq = T(0);
+        for (int r = lane; r < D; r += 32) {
+          const T x = Pb[(size_t)r * ORTH_B + c];
+          nq = fma(x, x, nq);
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) nq += __shfl_xor_sync(0xffffffffu, nq, o);
+        const T inv = nq > T(0) ? T(1) / sqrt(nq) : T(0);
+        for (int r = lane; r < D; r += 32) Pb[(size_t)r * ORTH_B + c] *= inv;
+        __syncwarp();
+      }
+    }
+    __syncthreads();
+    // finished panel back into Ys (fenced by the next barrier)
+    for (int e = tid; e < D * cb; e += ORTH_NT) {
+      const int c = e / D, r = e - c * D;
+      Ys[(size_t)(j0 + c) * ldy + r] = Pb[(size_t)r * ORTH_B + c];
+    }
+  }
+  __syncthreads();
+  for (int e = tid; e < D * k; e += ORTH_NT) {
+    const int j = e / D, r = e - j * D;
+    Y[e] = Ys[(size_t)j * ldy + r];
+  }
 }
 
 static size_t orth_smem_bytes(int D, int k, size_t es) {
@@ -262,7 +617,7 @@ __global__ void __launch_bounds__(TFX_THREADS) k_orth(T* Y, int D, int k) {
 // the matching eigenvectors as columns of V (n x n, column-major).
 // ---------------------------------------------------------------------------
 template <class T>
-__global__ void __launch_bounds__(TFX_THREADS) k_jacobi(const T* __restrict__ Ain, int n, T* __restrict__ evals,
+__global__ void __launch_bounds__(512) k_jacobi(const T* __restrict__ Ain, int n, T* __restrict__ evals,
                                                         T* __restrict__ V, int max_sweeps, int* __restrict__ sweeps_out) {
   extern __shared__ __align__(16) char smem[];
   const int m = (n + 1) & ~1;  // even size (a zero row/column pads odd n)
@@ -271,17 +626,18 @@ __global__ void __launch_bounds__(TFX_THREADS) k_jacobi(const T* __restrict__ Ai
   T* cs = Vs + (size_t)m * m;  // c[m/2], s[m/2]
   int* pr = (int*)(cs + m);    // pairs
   double* red = (double*)(pr + m + 2);
+  unsigned* blk = (unsigned*)(red + 2);  // (m/2)(m/2+1)/2 block indices
   const int tid = threadIdx.x;
-  for (int e = tid; e < m * m; e += TFX_THREADS) {
+  for (int e = tid; e < m * m; e += blockDim.x) {
     const int i = e / m, j = e - i * m;
     // symmetrised on load: Rayleigh-Ritz matrices arrive symmetric only up to rounding
     A[e] = (i < n && j < n) ? (T)(0.5 * ((double)Ain[i * n + j] + (double)Ain[j * n + i])) : T(0);
     Vs[e] = (i == j) ? T(1) : T(0);
   }
   __syncthreads();
-  const int sweep = cta_jacobi<T>(A, Vs, cs, pr, red, m, max_sweeps);
+  const int sweep = cta_jacobi<T>(A, Vs, cs, pr, red, m, max_sweeps, blk);
   // sort eigenvalues (descending) with their vectors
-  for (int i = tid; i < n; i += TFX_THREADS) {
+  for (int i = tid; i < n; i += blockDim.x) {
     const int rank = eig_rank<T>(A, m, n, i);
     evals[rank] = A[i * m + i];
     for (int r = 0; r < n; ++r) V[(size_t)rank * n + r] = Vs[i * m + r];
@@ -406,17 +762,19 @@ __global__ void __launch_bounds__(TFX_THREADS) k_cp_residual(const T* __restrict
 template <class T>
 __global__ void k_tensor_norms(const T* __restrict__ Tt, long long N, double* __restrict__ partial) {
   __shared__ double red[2][TFX_THREADS / 32];
-  double s2 = 0.0, s1 = 0.0;
+  // compensated accumulation in the working precision (FP64 per element would
+  // run at GB300's FP64 rate)
+  Acc<T> a2, a1;
   for (long long e = (long long)blockIdx.x * TFX_THREADS + threadIdx.x; e < N; e += (long long)gridDim.x * TFX_THREADS) {
-    const double t = (double)Tt[e];
-    s2 += t * t;
-    s1 += fabs(t);
+    const T t = __ldg(Tt + e);
+    a2.fma_(t, t);
+    a1.add(fabs(t));
   }
-  s2 = warp_sum(s2);
-  s1 = warp_sum(s1);
+  a2.warp_reduce();
+  a1.warp_reduce();
   if ((threadIdx.x & 31) == 0) {
-    red[0][threadIdx.x >> 5] = s2;
-    red[1][threadIdx.x >> 5] = s1;
+    red[0][threadIdx.x >> 5] = a2.value();
+    red[1][threadIdx.x >> 5] = a1.value();
   }
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -552,10 +910,69 @@ extern "C" int tfx_gemm(int dtype, const void* A, const void* B, void* C, long l
   return check_launch("gemm");
 }
 
+extern "C" int tfx_ttm(int dtype, const void* S, long long P, int D, long long Q, const void* Ut, int n, void* out,
+                       void* stream) {
+  if (!S || !Ut || !out || P < 1 || D < 1 || Q < 1 || n < 1) return tfx_set_error(TFX_STATUS_ERR_ARG, "ttm args");
+  cudaStream_t st = (cudaStream_t)stream;
+  const bool vec = dtype == TFX_F32 && D % 4 == 0 && Q % 4 == 0 && ((uintptr_t)S & 15) == 0 &&
+                   ((uintptr_t)Ut & 15) == 0 && ((uintptr_t)out & 15) == 0;
+  if (vec && Q >= 128) {
+    const int rows = n < 64 ? n : 64;
+    const int nw = (rows + 7) / 8;
+    const int mt = (n + 8 * nw - 1) / (8 * nw);
+    // wide tiles when there are enough of them to fill the GPU twice over
+    const bool wide = ((Q + 255) / 256) * P * mt >= 2LL * num_sms();
+    const long long tq = wide ? (Q + 255) / 256 : (Q + 127) / 128;
+    if (tq > 2147483647LL) return tfx_set_error(TFX_STATUS_ERR_UNSUPPORTED, "ttm too wide");
+    dim3 grid((unsigned)tq, (unsigned)(P < 65535 ? P : 65535), (unsigned)mt);
+    if (wide)
+      k_ttm_f32<8><<<grid, 32 * nw, 0, st>>>((const float*)Ut, (const float*)S, (float*)out, n, D, Q, P);
+    else
+      k_ttm_f32<4><<<grid, 32 * nw, 0, st>>>((const float*)Ut, (const float*)S, (float*)out, n, D, Q, P);
+    return check_launch("ttm");
+  }
+  // general shapes: strided batched GEMM, batched over p (Q >= 16) or over q
+  long long sd[9];
+  if (Q >= 16) {
+    const long long t[9] = {0, D, 1, (long long)D * Q, Q, 1, (long long)n * Q, Q, 1};
+    for (int i = 0; i < 9; ++i) sd[i] = t[i];
+    return tfx_gemm(dtype, Ut, S, out, n, Q, D, P, sd, 1.0, 0.0, stream);
+  }
+  const long long t[9] = {1, (long long)D * Q, Q, 0, 1, D, 1, (long long)n * Q, Q};
+  for (int i = 0; i < 9; ++i) sd[i] = t[i];
+  return tfx_gemm(dtype, S, Ut, out, P, n, D, Q, sd, 1.0, 0.0, stream);
+}
+
+template <class T, int RPL>
+static cudaError_t launch_orth(T* Y, int D, int k, size_t smb, cudaStream_t st) {
+  cudaError_t e = cudaFuncSetAttribute(k_orth_bcgs<T, RPL>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smb);
+  if (e != cudaSuccess) return e;
+  k_orth_bcgs<T, RPL><<<1, ORTH_NT, smb, st>>>(Y, D, k);
+  return cudaSuccess;
+}
+
 extern "C" int tfx_orthonormalize(int dtype, void* Y, int D, int k, void* stream) {
   if (!Y || D < 1 || k < 1 || k > 1024) return tfx_set_error(TFX_STATUS_ERR_ARG, "orthonormalize args");
   cudaStream_t st = (cudaStream_t)stream;
   const size_t es = dtype == TFX_F64 ? 8 : 4;
+  size_t oP, oPart, oC, oRed;
+  const size_t smb = dtype == TFX_F32 ? orth_bcgs_offsets<float>(D, k, &oP, &oPart, &oC, &oRed)
+                                      : orth_bcgs_offsets<double>(D, k, &oP, &oPart, &oC, &oRed);
+  if (smb <= 220 * 1024 && k <= 32 * ORTH_NW) {
+    cudaError_t e = cudaSuccess;
+    if (dtype == TFX_F32) {
+      if (D <= 128) e = launch_orth<float, 4>((float*)Y, D, k, smb, st);
+      else if (D <= 256) e = launch_orth<float, 8>((float*)Y, D, k, smb, st);
+      else if (D <= 512) e = launch_orth<float, 16>((float*)Y, D, k, smb, st);
+      else e = launch_orth<float, 0>((float*)Y, D, k, smb, st);
+    } else {
+      if (D <= 128) e = launch_orth<double, 4>((double*)Y, D, k, smb, st);
+      else if (D <= 256) e = launch_orth<double, 8>((double*)Y, D, k, smb, st);
+      else e = launch_orth<double, 0>((double*)Y, D, k, smb, st);
+    }
+    if (e != cudaSuccess) return tfx_set_cuda_error(e, "orth attr");
+    return check_launch("orthonormalize");
+  }
   const size_t sm = orth_smem_bytes(D, k, es);
   if (sm <= 200 * 1024) {
     cudaError_t e;
@@ -582,7 +999,8 @@ extern "C" size_t tfx_sym_eig_smem_bytes(int dtype, int n) {
   const size_t es = dtype == TFX_F64 ? 8 : 4;
   size_t b = 2 * (size_t)m * m * es + (size_t)m * es + (size_t)(m + 2) * sizeof(int);
   b = (b + 15) & ~(size_t)15;
-  return b + 2 * (TFX_THREADS / 32) * sizeof(double);
+  const size_t h = (size_t)m / 2;
+  return b + 2 * (TFX_THREADS / 32) * sizeof(double) + h * (h + 1) / 2 * sizeof(unsigned);
 }
 
 extern "C" int tfx_sym_eig(int dtype, const void* A, int n, void* evals, void* V, int max_sweeps, int* sweeps,
@@ -595,11 +1013,11 @@ extern "C" int tfx_sym_eig(int dtype, const void* A, int n, void* evals, void* V
   if (dtype == TFX_F32) {
     e = cudaFuncSetAttribute(k_jacobi<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     if (e != cudaSuccess) return tfx_set_cuda_error(e, "sym_eig attr");
-    k_jacobi<float><<<1, TFX_THREADS, sm, st>>>((const float*)A, n, (float*)evals, (float*)V, max_sweeps, sweeps);
+    k_jacobi<float><<<1, 512, sm, st>>>((const float*)A, n, (float*)evals, (float*)V, max_sweeps, sweeps);
   } else {
     e = cudaFuncSetAttribute(k_jacobi<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     if (e != cudaSuccess) return tfx_set_cuda_error(e, "sym_eig attr");
-    k_jacobi<double><<<1, TFX_THREADS, sm, st>>>((const double*)A, n, (double*)evals, (double*)V, max_sweeps, sweeps);
+    k_jacobi<double><<<1, 512, sm, st>>>((const double*)A, n, (double*)evals, (double*)V, max_sweeps, sweeps);
   }
   return check_launch("sym_eig");
 }

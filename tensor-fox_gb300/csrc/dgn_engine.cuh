@@ -66,8 +66,20 @@ __host__ __device__ inline WsLayout ws_layout(int L, int R, int nx, size_t es) {
   return w;
 }
 
+// Shared-memory layout of the third-order gradient (elements of the working
+// type): three unpadded slab stages of d1*d2 values, the transposed own
+// columns of the factors and M0 | M1 | M2 ((d0 + d1 + d2p) x 4 each), two
+// buffers of per-warp M0 partials, per-warp M2 partials; then the stage
+// barriers.  d2p: d2 rounded up to a multiple of four.
+__host__ __device__ inline size_t g3_stage(int d1, int d2) { return ((size_t)d1 * d2 + 4 + 3) & ~(size_t)3; }
+__host__ __device__ inline size_t g3_floats(int d0, int d1, int d2) {
+  const size_t d2p = ((size_t)d2 + 3) & ~(size_t)3;
+  return 3 * g3_stage(d1, d2) + 2 * (d0 + d1 + d2p) * 4 + 2 * (TFX_THREADS / 32) * 4 +
+         (TFX_THREADS / 32) * d2p * 4;
+}
+
 struct SmemPlan {
-  size_t sA, sB, sPart, sAk, sY, sM, sDG, sGam, sNorm, sBase, sIdx, rs4, rs12, misc, hist, rs1, rs1b, sScale;
+  size_t sA, sB, sPart, sAk, sY, sM, sDG, sGam, sNorm, sBase, sIdx, rs4, rs12, misc, hist, rs1, rs1b, sScale, wsl, sG3;
   size_t sQf, sWf, sP1o, sP2o, sVec;  // staged operands of the CG (valid when stage != 0)
   int stage;
   size_t total;
@@ -99,6 +111,14 @@ __host__ __device__ inline SmemPlan smem_plan(int TS, size_t es, int maxL, int m
   p.rs1 = o; o += al16(sizeof(RedScratch<1>));
   p.rs1b = o; o += al16(sizeof(RedScratch<1>));
   p.sScale = o; o += al16((size_t)maxL * maxncol * es);
+  p.wsl = o; o += al16(sizeof(PushSlots<3>));
+  // third-order gradient scratch (every mode up to 64): three slab stages,
+  // transposed own factor columns, M0 | M1 | M2, partial sums, stage barriers
+  p.sG3 = 0;
+  if (maxL == 3 && maxd <= 64) {
+    p.sG3 = o;
+    o += al16(g3_floats(maxd, maxd, maxd) * es + 64);
+  }
   p.stage = stage;
   p.sQf = p.sWf = p.sP1o = p.sP2o = p.sVec = o;
   if (stage) {
@@ -132,7 +152,7 @@ __device__ __forceinline__ char* dyn_smem() {
 // shared memory; otherwise they are read from global memory (L2).
 // ---------------------------------------------------------------------------
 struct CgOffsets {
-  size_t d, sQf, sWf, sP1o, sP2o, sAk, sY, sM, sDG, rs4, rs1, sVec;
+  size_t d, sQf, sWf, sP1o, sP2o, sAk, sY, sM, sDG, rs4, rs1, sVec, wsl;
 };
 
 // Copy n elements written by other CTAs of the team from global memory into
@@ -161,7 +181,8 @@ __device__ __forceinline__ void stage_copy(T* sdst, const T* gsrc, int n) {
 template <class T, bool STAGED>
 __device__ __forceinline__ void cg_matvec(const int L, const int R, const int nx, const int ncol, const int c0,
                                           const CgOffsets so, const T* Dglob, T* zout, const T* Wg, const T* P1g,
-                                          const T* P2g, T* zloc = nullptr, long long* cprof = nullptr) {
+                                          const T* P2g, T* zloc = nullptr, long long* cprof = nullptr,
+                                          bool prestaged = false) {
   // timers accumulate in registers of thread 0 (cprof points at its private array)
   long long tc = cprof ? clock64() : 0;
   auto ctick = [&](int ph) {
@@ -180,9 +201,12 @@ __device__ __forceinline__ void cg_matvec(const int L, const int R, const int nx
   const T* Din;
   const T* Wr;
   if (STAGED) {
+    // prestaged: the team already pushed the full input into sQf
     T* sQf = (T*)(sm + so.sQf);
-    stage_copy(sQf, Dglob, nx);
-    __syncthreads();
+    if (!prestaged) {
+      stage_copy(sQf, Dglob, nx);
+      __syncthreads();
+    }
     ctick(1);
     Din = sQf;
     Wr = (const T*)(sm + so.sWf);
@@ -193,15 +217,23 @@ __device__ __forceinline__ void cg_matvec(const int L, const int R, const int nx
   const T* sP1o = (const T*)(sm + so.sP1o);
   const T* sP2o = (const T*)(sm + so.sP2o);
   const int RN = R * ncol;
+  // A_k = D_k^T W_k on the owned columns, one output per thread item; the
+  // dot runs as two interleaved chains so that loads overlap the FMAs
+  const int ncg = (ncol + 3) >> 2;
   for (int e = tid; e < L * RN; e += TFX_THREADS) {
     const int k = e / RN, q = e - k * RN, a = q / ncol, c = q - a * ncol;
     const int dk = d[k];
     const T* dv = Din + off[k] + a * dk;
     const T* wv = Wr + off[k] + (c0 + c) * dk;
-    T acc = T(0);
+    T acc0 = T(0), acc1 = T(0);
+    int i = 0;
 #pragma unroll 4
-    for (int i = 0; i < dk; ++i) acc = fma(dv[i], wv[i], acc);
-    sAk[e] = acc;
+    for (; i + 1 < dk; i += 2) {
+      acc0 = fma(dv[i], wv[i], acc0);
+      acc1 = fma(dv[i + 1], wv[i + 1], acc1);
+    }
+    if (i < dk) acc0 = fma(dv[i], wv[i], acc0);
+    sAk[e] = acc0 + acc1;
   }
   __syncthreads();
   ctick(2);
@@ -218,31 +250,60 @@ __device__ __forceinline__ void cg_matvec(const int L, const int R, const int nx
   }
   __syncthreads();
   ctick(3);
-  // z_l = W_l Y_l + D_l P1_l over all owned outputs of all modes at once
-  const int ownn = ncol * (nx / R);
-  for (int e = tid; e < ownn; e += TFX_THREADS) {
-    int l = 0, rem = e;
-    while (rem >= ncol * d[l]) {
-      rem -= ncol * d[l];
+  // z_l = W_l Y_l + D_l P1_l over all owned outputs of all modes at once;
+  // a thread takes one row i of one mode and four owned columns
+  const int sumd = nx / R;
+  for (int e = tid; e < ncg * sumd; e += TFX_THREADS) {
+    const int cgi = e / sumd;
+    int l = 0, i = e - cgi * sumd;
+    while (i >= d[l]) {
+      i -= d[l];
       ++l;
     }
+    const int cb = cgi * 4, cn = min(4, ncol - cb);
     const int dl = d[l], ol = off[l];
-    const int c = rem / dl, i = rem - c * dl;
     const T* wrow = Wr + ol + i;
     const T* drow = Din + ol + i;
-    const T* yc = sY + (size_t)l * RN + c;
-    const T* p1c = STAGED ? sP1o + (size_t)l * R * ncol + c : P1g + (size_t)l * R * R + c0 + c;
+    const T* yc = sY + (size_t)l * RN + cb;
+    const T* p1c = STAGED ? sP1o + (size_t)l * R * ncol + cb : P1g + (size_t)l * R * R + c0 + cb;
     const int p1s = STAGED ? ncol : R;
-    T a1 = T(0), a2 = T(0);
+    T a1[4] = {T(0), T(0), T(0), T(0)}, a2[4] = {T(0), T(0), T(0), T(0)};
+    if (sizeof(T) == 4 && STAGED && (ncol & 3) == 0) {
+      // four owned columns as one 16-byte read of Y and of P1 per r
 #pragma unroll 4
-    for (int r = 0; r < R; ++r) {
-      a1 = fma(wrow[r * dl], yc[r * ncol], a1);
-      a2 = fma(drow[r * dl], p1c[r * p1s], a2);
+      for (int r = 0; r < R; ++r) {
+        const T w = wrow[r * dl], dd = drow[r * dl];
+        const float4 y4 = *reinterpret_cast<const float4*>(yc + r * ncol);
+        const float4 p4 = *reinterpret_cast<const float4*>(p1c + r * p1s);
+        a1[0] = fma(w, (T)y4.x, a1[0]);
+        a1[1] = fma(w, (T)y4.y, a1[1]);
+        a1[2] = fma(w, (T)y4.z, a1[2]);
+        a1[3] = fma(w, (T)y4.w, a1[3]);
+        a2[0] = fma(dd, (T)p4.x, a2[0]);
+        a2[1] = fma(dd, (T)p4.y, a2[1]);
+        a2[2] = fma(dd, (T)p4.z, a2[2]);
+        a2[3] = fma(dd, (T)p4.w, a2[3]);
+      }
+    } else {
+#pragma unroll 2
+      for (int r = 0; r < R; ++r) {
+        const T w = wrow[r * dl], dd = drow[r * dl];
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+          if (u < cn) {
+            a1[u] = fma(w, yc[r * ncol + u], a1[u]);
+            a2[u] = fma(dd, p1c[r * p1s + u], a2[u]);
+          }
+      }
     }
-    if (zloc)
-      zloc[e] = a1 + a2;
-    else
-      zout[ol + (c0 + c) * dl + i] = a1 + a2;
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+      if (u < cn) {
+        if (zloc)
+          zloc[ncol * (ol / R) + (cb + u) * dl + i] = a1[u] + a2[u];
+        else
+          zout[ol + (c0 + cb + u) * dl + i] = a1[u] + a2[u];
+      }
   }
   __syncthreads();
   ctick(4);
@@ -252,7 +313,7 @@ template <class T, bool STAGED>
 __device__ __forceinline__ int cg_team(const Team tm, const int L, const int R, const int nx, const int ncol,
                                        const int c0, const CgOffsets so, T* grad, T* jtj, T* y, T* r, T* P, T* Q,
                                        T* z, const T* Wg, const T* P1g, const T* P2g, const int budget,
-                                       const double cg_tol, double& rn_out, int& flip4, long long* cprof_g) {
+                                       const double cg_tol, double& rn_out, int& flipw, long long* cprof_g) {
   long long lprof[8] = {0, 0, 0, 0, 0, 0, 0, 0};
   long long* cprof = cprof_g ? lprof : nullptr;
   long long tc = cprof ? clock64() : 0;
@@ -268,7 +329,9 @@ __device__ __forceinline__ int cg_team(const Team tm, const int L, const int R, 
   const int* off = d + TFX_MAX_ORDER;
   const T* sM = (const T*)(sm + so.sM);
   const T* sDG = (const T*)(sm + so.sDG);
-  RedScratch<1>* rs1 = (RedScratch<1>*)(sm + so.rs1);
+  PushSlots<1>* ps1 = (PushSlots<1>*)(sm + so.wsl);
+  PushSlots<3>* ps3 = (PushSlots<3>*)(sm + so.wsl);
+  T* sQf = (T*)(sm + so.sQf);
   const int tid = threadIdx.x;
   // own slice: element (l, c, i) lives at local index ncol*(off[l]/R) + c*d[l] + i
   const int own = ncol * (nx / R);
@@ -282,8 +345,9 @@ __device__ __forceinline__ int cg_team(const Team tm, const int L, const int R, 
     vDG = vM + own;
   }
   cg_matvec<T, STAGED>(L, R, nx, ncol, c0, so, grad, jtj, Wg, P1g, P2g);
-  Acc<T> v[1];
-  double red[1];
+  // the CG scalars live in the working precision: on the FP32 path every
+  // thread would otherwise run FP64 divisions, which GB300 executes slowly
+  Acc<T> v[1], tot[1];
   for (int l = 0; l < L; ++l) {
     const int dl = d[l], base = off[l] + c0 * dl, n = ncol * dl, lb = ncol * (off[l] / R);
     for (int e = tid; e < n; e += TFX_THREADS) {
@@ -304,25 +368,34 @@ __device__ __forceinline__ int cg_team(const Team tm, const int L, const int R, 
       v[0].fma_(rr, rr);
     }
   }
-  team_sum_acc<1, T>(tm, v, red, rs1, flip4);
-  double rn = red[0];
-  if (rn == 0.0) rn = 1e-6;
+  team_sum_push<1>(tm, v, tot, ps1, flipw);
+  Acc<T> rnA = tot[0];
+  T rn = acc_val(rnA);
+  if (rn == T(0)) {
+    rn = T(1e-6);
+    rnA = Acc<T>();
+    rnA.add(rn);
+  }
   int maxit = budget;
-  double tol = cg_tol;
+  T tol = (T)cg_tol;
   if (nx > 100) {
     maxit = min(maxit, nx);
   } else {
-    tol = 0.0;
+    tol = T(0);
   }
   int itn = 0;
   bool broke = false;
   for (itn = 0; itn < maxit; ++itn) {
-    // Q = M P (owned part, published through global memory)
+    // Q = M P on the owned slice.  Staged: pushed straight into every team
+    // member's shared-memory copy of the full vector (their previous reads of
+    // it ended before the last team barrier); otherwise published through
+    // global memory.
     for (int l = 0; l < L; ++l) {
       const int dl = d[l], base = off[l] + c0 * dl, n = ncol * dl, lb = ncol * (off[l] / R);
       for (int e = tid; e < n; e += TFX_THREADS) {
         if (STAGED) {
-          Q[base + e] = vM[lb + e] * vP[lb + e];
+          const T q = vM[lb + e] * vP[lb + e];
+          for (int rr = 0; rr < tm.size; ++rr) tm.peer(sQf, rr)[base + e] = q;
         } else {
           const int c = e / dl;
           Q[base + e] = sM[l * ncol + c] * P[base + e];
@@ -331,10 +404,14 @@ __device__ __forceinline__ int cg_team(const Team tm, const int L, const int R, 
     }
     tm.sync();
     ctick(0);
-    cg_matvec<T, STAGED>(L, R, nx, ncol, c0, so, Q, z, Wg, P1g, P2g, STAGED ? vz : nullptr, cprof);
+    cg_matvec<T, STAGED>(L, R, nx, ncol, c0, so, Q, z, Wg, P1g, P2g, STAGED ? vz : nullptr, cprof, STAGED);
     if (cprof) tc = clock64();
-    Acc<T> w[1];
-    const T* Qs = STAGED ? (const T*)(sm + so.sQf) : Q;  // full Q, staged by the matvec
+    // FP32: one reduction gives P.z, r.z and z.z, and |r - alpha z|^2 follows
+    // as rn - 2 alpha r.z + alpha^2 z.z in float-float; FP64 keeps the
+    // reference's separate reduction of the updated residual
+    constexpr bool MERGED = sizeof(T) == 4;
+    Acc<T> w[3];
+    const T* Qs = STAGED ? (const T*)sQf : Q;
     for (int l = 0; l < L; ++l) {
       const int dl = d[l], base = off[l] + c0 * dl, n = ncol * dl, lb = ncol * (off[l] / R);
       for (int e = tid; e < n; e += TFX_THREADS) {
@@ -342,20 +419,34 @@ __device__ __forceinline__ int cg_team(const Team tm, const int L, const int R, 
           const T zz = vM[lb + e] * (vz[lb + e] + vDG[lb + e] * Qs[base + e]);
           vz[lb + e] = zz;
           w[0].fma_(vP[lb + e], zz);
+          if (MERGED) {
+            w[1].fma_(vr[lb + e], zz);
+            w[2].fma_(zz, zz);
+          }
         } else {
           const int c = e / dl, g = base + e;
           const T zz = sM[l * ncol + c] * (z[g] + sDG[l * ncol + c] * Q[g]);
           z[g] = zz;
           w[0].fma_(P[g], zz);
+          if (MERGED) {
+            w[1].fma_(r[g], zz);
+            w[2].fma_(zz, zz);
+          }
         }
       }
     }
-    team_sum_acc<1, T>(tm, w, red, rs1, flip4);
+    Acc<T> t3[3];
+    if (MERGED) {
+      team_sum_push<3>(tm, w, t3, ps3, flipw);
+    } else {
+      Acc<T> w1[1] = {w[0]};
+      team_sum_push<1>(tm, w1, tot, ps1, flipw);
+      t3[0] = tot[0];
+    }
     ctick(5);
-    double den = red[0];
-    if (den == 0.0) den = 1e-6;
-    const double alpha = rn / den;
-    const T ta = (T)alpha;
+    T den = acc_val(t3[0]);
+    if (den == T(0)) den = T(1e-6);
+    const T ta = rn / den;
     Acc<T> u[1];
     if (STAGED) {
       for (int e = tid; e < own; e += TFX_THREADS) {
@@ -376,12 +467,31 @@ __device__ __forceinline__ int cg_team(const Team tm, const int L, const int R, 
         }
       }
     }
-    team_sum_acc<1, T>(tm, u, red, rs1, flip4);
+    Acc<T> rnN;
+    bool exact = !MERGED;
+    if (MERGED) {
+      // rn_new = rn - 2 alpha (r.z) + alpha^2 (z.z), exact products
+      rnN = rnA;
+      const T m2a = T(-2) * ta;
+      rnN.fma_(m2a, t3[1].hi_or_v());
+      rnN.fma_(m2a, t3[1].lo_or_0());
+      const T a2 = ta * ta, a2e = fma(ta, ta, -a2);
+      rnN.fma_(a2, t3[2].hi_or_v());
+      rnN.fma_(a2e, t3[2].hi_or_v());
+      rnN.fma_(a2, t3[2].lo_or_0());
+      // deep cancellation: the stored residual's own rounding dominates, so
+      // its norm is reduced directly (the same decision in every thread)
+      if (!(acc_val(rnN) > T(1e-4) * rn)) exact = true;
+    }
+    if (exact) {
+      team_sum_push<1>(tm, u, tot, ps1, flipw);
+      rnN = tot[0];
+    }
     ctick(6);
-    const double rn_new = red[0];
-    const double beta = rn_new / rn;
+    const T rn_new = acc_val(rnN);
+    const T tb = rn_new / rn;
     rn = rn_new;
-    const T tb = (T)beta;
+    rnA = rnN;
     if (STAGED) {
       for (int e = tid; e < own; e += TFX_THREADS) vP[e] = (itn == 0) ? vr[e] + tb * vr[e] : vr[e] + tb * vP[e];
     } else {
@@ -407,11 +517,28 @@ __device__ __forceinline__ int cg_team(const Team tm, const int L, const int R, 
       for (int e = tid; e < n; e += TFX_THREADS) y[base + e] = vy[lb + e];
     }
   }
+  // the next reader of sQf (the next matvec's staging) runs after a team barrier
   __syncthreads();
   if (cprof_g)
     for (int k = 0; k < 8; ++k) cprof_g[k] += lprof[k];
-  rn_out = rn;
+  rn_out = (double)rn;
   return broke ? itn + 1 : maxit;
+}
+
+// four consecutive 16-byte aligned values from shared memory as vector reads
+__device__ __forceinline__ void lds4(const float* p, float (&v)[4]) {
+  const float4 a = *reinterpret_cast<const float4*>(p);
+  v[0] = a.x;
+  v[1] = a.y;
+  v[2] = a.z;
+  v[3] = a.w;
+}
+__device__ __forceinline__ void lds4(const double* p, double (&v)[4]) {
+  const double2 a = *reinterpret_cast<const double2*>(p), b = *reinterpret_cast<const double2*>(p + 2);
+  v[0] = a.x;
+  v[1] = a.y;
+  v[2] = b.x;
+  v[3] = b.y;
 }
 
 template <class T, int TS>
@@ -434,7 +561,7 @@ struct Engine {
   int* sIdx;
   RedScratch<4>* rs4;
   RedScratch<TFX_MAX_ORDER>* rs12;
-  int flip4, flip12, flip1, flip1b;
+  int flip4, flip12, flip1, flip1b, flipw;
   RedScratch<1>* rs1b;
   T* sScale;
   double damp, Tsize;
@@ -442,6 +569,10 @@ struct Engine {
   // staged operands: full search direction and factors, owned P1/P2 columns
   int stage;
   T *sQf, *sWf, *sP1o, *sP2o;
+  T* sG3;       // third-order gradient scratch, or nullptr
+  size_t g3off; // its offset in dynamic shared memory
+  unsigned g3base;  // slabs streamed so far: slab n uses stage n % 3, phase (n / 3) & 1
+  int g3err;      // a slab wait ran out
   const T* Wr;  // factors to read: shared-memory copy when staged
 
   __device__ __forceinline__ T& P1at(int l, int a, int c) {
@@ -601,6 +732,250 @@ struct Engine {
   }
 
   // -------------------------------------------------------------------------
+  // Third-order gradient for the owned columns without team communication.
+  // The tensor streams through a ring of three shared-memory stages, one slab
+  // T[i, :, :] (contiguous, d1*d2 values) per bulk copy (cp.async.bulk,
+  // completion on an mbarrier).  Per group of four owned columns c and slab i,
+  // eight threads per row j (rows j and j + 32) take k-groups q and q + 8 and form
+  //   Y[j, c]   = sum_k T[i, j, k] W2[k, c]           (W2 rows in registers)
+  //   M2[k, c] += T[i, j, k] W0[i, c] W1[j, c]         (registers, summed at the end)
+  //   M1[j, c] += Y[j, c] W0[i, c],  M0[i, c] = sum_j Y[j, c] W1[j, c]
+  // (the dimension tree of MTTKRP), and grad_l = M_l - W_l P1_l, the negative
+  // of GaussNewton.py:401-427.  Every sum has a fixed order: deterministic.
+  // Needs every mode <= 64, d1*d2 % 4 == 0 and a 16-byte aligned tensor.
+  // -------------------------------------------------------------------------
+  template <bool STAGED>
+  __device__ void gradient_l3() {
+    long long gt = gprof ? clock64() : 0;
+    auto gtick = [&](int ph) {
+      if (gprof) {
+        const long long now = clock64();
+        gprof[ph] += now - gt;
+        gt = now;
+      }
+    };
+    constexpr int NW = TFX_THREADS / 32;
+    const int d0 = d[0], d1 = d[1], d2 = d[2];
+    const int d2p = (d2 + 3) & ~3;
+    const int nkg = d2p >> 2;  // <= 16
+    char* smb = dyn_smem();
+    const T* Wl = STAGED ? (const T*)(smb + cgo.sWf) : W;
+    const T* P1l = STAGED ? (const T*)(smb + cgo.sP1o) : P1;
+    const int p1s = STAGED ? ncol : R;  // P1 column stride
+    const int p1c = STAGED ? 0 : c0;    // P1 column offset
+    const int SL = (int)g3_stage(d1, d2);
+    T* sT = (T*)(smb + g3off);                 // 3 stages
+    T* sF = sT + 3 * SL;                       // (d0 + d1 + d2p) x 4, own columns transposed
+    T* sMM = sF + (d0 + d1 + d2p) * 4;         // M0 | M1 | M2
+    T* sP0 = sMM + (d0 + d1 + d2p) * 4;        // [2][NW][4] M0 warp partials
+    T* sR2 = sP0 + 2 * NW * 4;                 // [NW][d2p][4] M2 warp partials
+    unsigned long long* mbar = (unsigned long long*)(smb + g3off + g3_floats(d0, d1, d2) * sizeof(T));
+    const T* sA4 = sF;
+    const T* sB4 = sF + d0 * 4;
+    const T* sC4 = sF + (d0 + d1) * 4;
+    T* sM0 = sMM;
+    T* sM1 = sMM + d0 * 4;
+    T* sM2 = sMM + (d0 + d1) * 4;
+    const int lane = tid & 31, wid = tid >> 5;
+    const int rs = tid >> 3, q8 = tid & 7;  // rows rs and rs + 32; k-groups q8 and q8 + 8
+    const unsigned bytes = (unsigned)((size_t)d1 * d2 * sizeof(T));
+    auto issue = [&](int i) {
+      if (tid == 0) {
+        const int b = (int)((g3base + i) % 3);
+        const unsigned mb = (unsigned)__cvta_generic_to_shared(mbar + b);
+        const unsigned dst = (unsigned)__cvta_generic_to_shared(sT + b * SL);
+        // the stage's previous contents were read by the generic proxy
+        asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(mb), "r"(bytes) : "memory");
+        asm volatile(
+            "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(dst),
+            "l"(Tt + (long long)i * d1 * d2), "r"(bytes), "r"(mb)
+            : "memory");
+      }
+    };
+    // bounded wait for slab i; a wait that runs out flags the solve
+    auto wait_slab = [&](int i) {
+      const unsigned n = g3base + i;
+      const unsigned mb = (unsigned)__cvta_generic_to_shared(mbar + n % 3);
+      const unsigned par = (n / 3) & 1;
+      unsigned ok = 0;
+      for (int it = 0; it < (1 << 24) && !ok; ++it)
+        asm volatile(
+            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(ok)
+            : "r"(mb), "r"(par)
+            : "memory");
+      if (!ok) g3err = 1;
+    };
+    for (int cb = 0; cb < ncol; cb += 4) {
+      const int cn = min(4, ncol - cb);
+      for (int e = tid; e < (d0 + d1 + d2p) * 4; e += TFX_THREADS) {
+        const int c = e & 3;
+        int l = 0, i = e >> 2;
+        if (i >= d0) {
+          i -= d0;
+          l = 1;
+          if (i >= d1) {
+            i -= d1;
+            l = 2;
+          }
+        }
+        sF[e] = (c < cn && i < d[l]) ? Wl[off[l] + (c0 + cb + c) * d[l] + i] : T(0);
+        sMM[e] = T(0);
+      }
+      __syncthreads();  // sF ready; the previous group is done with every stage
+      issue(0);
+      if (d0 > 1) issue(1);
+      // own k-groups q8 and q8 + 8 and their rows of W2
+      T creg[2][4][4], acc2[2][4][4];
+#pragma unroll
+      for (int s2 = 0; s2 < 2; ++s2) {
+        const int kg = q8 + 8 * s2;
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          T cc[4] = {T(0), T(0), T(0), T(0)};
+          if (kg < nkg) lds4(sC4 + (4 * kg + u) * 4, cc);
+#pragma unroll
+          for (int c = 0; c < 4; ++c) {
+            creg[s2][u][c] = cc[c];
+            acc2[s2][u][c] = T(0);
+          }
+        }
+      }
+      T bj[2][4], m1[2][4];
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+          bj[h][c] = T(0);
+          m1[h][c] = T(0);
+        }
+        if (rs + 32 * h < d1) lds4(sB4 + (rs + 32 * h) * 4, bj[h]);
+      }
+      gtick(0);
+      for (int i = 0; i < d0; ++i) {
+        wait_slab(i);
+        __syncthreads();  // every warp is past slab i-1: its stage may be refilled
+        gtick(1);
+        if (i + 2 < d0) issue(i + 2);
+        if (wid == NW - 1 && lane < 4 && i > 0) {  // M0 of slab i-1 from its warp partials
+          T sacc = T(0);
+          for (int w = 0; w < NW; ++w) sacc += sP0[((i - 1) & 1) * NW * 4 + w * 4 + lane];
+          sM0[(i - 1) * 4 + lane] = sacc;
+        }
+        gtick(2);
+        T ai[4];
+        lds4(sA4 + i * 4, ai);
+        T p0[4] = {T(0), T(0), T(0), T(0)};
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+          const int row = rs + 32 * h;
+          T y[4] = {T(0), T(0), T(0), T(0)};
+          if (row < d1) {
+            const T* tr = sT + ((g3base + i) % 3) * SL + row * d2;
+            T kr[4];
+#pragma unroll
+            for (int c = 0; c < 4; ++c) kr[c] = ai[c] * bj[h][c];
+#pragma unroll
+            for (int s2 = 0; s2 < 2; ++s2) {
+              const int kg = q8 + 8 * s2;
+              if (kg < nkg) {
+                T tv[4];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) tv[u] = (4 * kg + u < d2) ? tr[4 * kg + u] : T(0);
+#pragma unroll
+                for (int u = 0; u < 4; ++u)
+#pragma unroll
+                  for (int c = 0; c < 4; ++c) {
+                    y[c] = fma(tv[u], creg[s2][u][c], y[c]);
+                    acc2[s2][u][c] = fma(tv[u], kr[c], acc2[s2][u][c]);
+                  }
+              }
+            }
+          }
+#pragma unroll
+          for (int c = 0; c < 4; ++c) {
+            y[c] += __shfl_xor_sync(0xffffffffu, y[c], 1);
+            y[c] += __shfl_xor_sync(0xffffffffu, y[c], 2);
+            y[c] += __shfl_xor_sync(0xffffffffu, y[c], 4);
+            m1[h][c] = fma(y[c], ai[c], m1[h][c]);
+            if (q8 == 0) p0[c] = fma(y[c], bj[h][c], p0[c]);
+          }
+        }
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+          p0[c] += __shfl_xor_sync(0xffffffffu, p0[c], 8);
+          p0[c] += __shfl_xor_sync(0xffffffffu, p0[c], 16);
+        }
+        if (lane == 0)
+#pragma unroll
+          for (int c = 0; c < 4; ++c) sP0[(i & 1) * NW * 4 + wid * 4 + c] = p0[c];
+        gtick(3);
+      }
+      __syncthreads();
+      if (wid == NW - 1 && lane < 4) {
+        T sacc = T(0);
+        for (int w = 0; w < NW; ++w) sacc += sP0[((d0 - 1) & 1) * NW * 4 + w * 4 + lane];
+        sM0[(d0 - 1) * 4 + lane] = sacc;
+      }
+      if (q8 == 0)
+#pragma unroll
+        for (int h = 0; h < 2; ++h)
+          if (rs + 32 * h < d1)
+#pragma unroll
+            for (int c = 0; c < 4; ++c) sM1[(rs + 32 * h) * 4 + c] = m1[h][c];
+      // M2: the rows of a warp (lanes with the same q8), then the warps
+#pragma unroll
+      for (int s2 = 0; s2 < 2; ++s2)
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+#pragma unroll
+          for (int c = 0; c < 4; ++c) {
+            T v = acc2[s2][u][c];
+            v += __shfl_xor_sync(0xffffffffu, v, 8);
+            v += __shfl_xor_sync(0xffffffffu, v, 16);
+            const int kg = q8 + 8 * s2;
+            if (lane < 8 && kg < nkg) sR2[(wid * d2p + 4 * kg + u) * 4 + c] = v;
+          }
+      __syncthreads();
+      for (int e = tid; e < nkg * 16; e += TFX_THREADS) {
+        T v = T(0);
+        for (int w = 0; w < NW; ++w) v += sR2[w * d2p * 4 + e];
+        sM2[e] = v;
+      }
+      __syncthreads();
+      gtick(4);
+      const int sd = d0 + d1 + d2;
+      for (int e = tid; e < sd * cn; e += TFX_THREADS) {
+        const int c = e / sd;
+        int l = 0, i = e - c * sd;
+        const T* Ml = sM0;
+        if (i >= d0) {
+          i -= d0;
+          l = 1;
+          Ml = sM1;
+          if (i >= d1) {
+            i -= d1;
+            l = 2;
+            Ml = sM2;
+          }
+        }
+        const int dl = d[l];
+        T wp = T(0);
+        const T* p1 = P1l + (size_t)l * R * p1s + p1c + cb + c;
+        for (int s2 = 0; s2 < R; ++s2) wp = fma(Wl[off[l] + s2 * dl + i], p1[s2 * p1s], wp);
+        grad[off[l] + (c0 + cb + c) * dl + i] = Ml[i * 4 + c] - wp;
+      }
+      __syncthreads();  // sF and the M slots are rewritten by the next group
+      g3base += d0;
+      gtick(5);
+    }
+    // the CG reads every column of the gradient
+    tm.sync();
+    gtick(7);
+  }
+
+  // -------------------------------------------------------------------------
   // Gradient (GaussNewton.py:401-427): grad_l = T_(l) KR_l - W_l P1_l, the
   // negative of the reference's g.  Split-K over the team, partial d_l x R
   // tiles summed through distributed shared memory by the CTA owning the column.
@@ -709,12 +1084,13 @@ struct Engine {
   // CG inner solve (see cg_team above)
   CgOffsets cgo;
   long long* cprof;  // optional CG sub-phase timers (rank 0, thread 0)
+  long long* gprof;  // optional third-order gradient sub-phase timers
   __device__ int cg(int budget, double& rn_out) {
     if (stage)
       return cg_team<T, true>(tm, L, R, nx, ncol, c0, cgo, grad, jtj, y, r, P, Q, z, W, P1, P2, budget, op.cg_tol,
-                              rn_out, flip1, cprof);
+                              rn_out, flipw, cprof);
     return cg_team<T, false>(tm, L, R, nx, ncol, c0, cgo, grad, jtj, y, r, P, Q, z, W, P1, P2, budget, op.cg_tol,
-                             rn_out, flip1, cprof);
+                             rn_out, flipw, cprof);
   }
 
   // Column balancing of x into the factor buffer (Conversion.py:361-387),
@@ -1050,12 +1426,30 @@ __device__ void solve_problem(const tfx_dgn_problem& pb, const tfx_dgn_options& 
   E.cgo.rs4 = sp.rs4;
   E.cgo.rs1 = sp.rs1;
   E.cgo.sVec = sp.sVec;
+  E.cgo.wsl = sp.wsl;
   E.rs1b = (RedScratch<1>*)(smem + sp.rs1b);
   E.sScale = (T*)(smem + sp.sScale);
+  // third-order gradient path: every mode <= 64 (the plan), 16-byte slabs
+  E.sG3 = (sp.sG3 && pb.L == 3 && ((size_t)pb.dims[1] * pb.dims[2]) % 4 == 0 &&
+           (((unsigned long long)pb.tensor) & 15) == 0)
+              ? (T*)(smem + sp.sG3)
+              : nullptr;
+  E.g3off = sp.sG3;
+  E.g3base = 0;
+  E.g3err = 0;
+  if (E.sG3 && threadIdx.x == 0) {
+    unsigned long long* mb =
+        (unsigned long long*)(smem + sp.sG3 + g3_floats(pb.dims[0], pb.dims[1], pb.dims[2]) * sizeof(T));
+    for (int b = 0; b < 3; ++b)
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"((unsigned)__cvta_generic_to_shared(mb + b)));
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+  }
+  __syncthreads();
   E.flip1 = 0;
   E.flip1b = 0;
   E.flip4 = 0;
   E.flip12 = 0;
+  E.flipw = 0;
 
   // error / improvement history: every CTA keeps its own copy in shared
   // memory so that the stop tests never depend on another SM's writes
@@ -1094,6 +1488,7 @@ __device__ void solve_problem(const tfx_dgn_problem& pb, const tfx_dgn_options& 
   // optional phase timers (rank 0, thread 0): SM clock cycles per phase
   long long* prof = (E.tm.rank == 0 && threadIdx.x == 0) ? pb.prof : nullptr;
   E.cprof = prof ? prof + 8 : nullptr;
+  E.gprof = prof ? prof + 16 : nullptr;
   long long tclk = clock64(), t_start = tclk;
   auto tick = [&](int ph) {
     if (prof) {
@@ -1107,7 +1502,12 @@ __device__ void solve_problem(const tfx_dgn_problem& pb, const tfx_dgn_options& 
     tick(6);
     E.gramians_and_precond();
     tick(0);
-    E.gradient();
+    if (E.sG3 && E.stage)
+      E.template gradient_l3<true>();
+    else if (E.sG3)
+      E.template gradient_l3<false>();
+    else
+      E.gradient();
     tick(1);
     double rn;
     const int itn = E.cg(pb.budgets[it], rn);
@@ -1208,11 +1608,13 @@ __device__ void solve_problem(const tfx_dgn_problem& pb, const tfx_dgn_options& 
   const int iters = (it < maxiter) ? it + 1 : maxiter;
   tick(6);
   if (prof) prof[7] += clock64() - t_start;
+  if (E.tm.rank == 0 && threadIdx.x == 0) pb.result[2] = TFX_OK;
   E.tm.sync();
+  // any CTA whose bounded slab wait ran out marks the solve (after rank 0's write)
+  if (threadIdx.x == 0 && E.g3err) atomicMax(&pb.result[2], 3);
   if (E.tm.rank == 0 && threadIdx.x == 0) {
     pb.result[0] = stop;
     pb.result[1] = iters;
-    pb.result[2] = TFX_OK;
     pb.result[3] = n_dogleg;
     pb.info[0] = Tsize;
     pb.info[1] = best_error;

@@ -5,84 +5,135 @@
 namespace tfx {
 
 // Symmetric eigensolver on one CTA: cyclic Jacobi with the round-robin
-// (tournament) ordering, m/2 disjoint rotations per round applied in parallel.
-// A (m x m, m even, row-major, symmetric, zero-padded beyond n) and Vs (m x m,
-// column p at Vs[p*m]) live in shared memory; cs holds m values, pr m+2 ints,
-// red 2*(TFX_THREADS/32) doubles.  On return the diagonal of A holds the
+// (tournament) ordering, m/2 disjoint rotations per round.  A (m x m, m even,
+// row-major, symmetric, zero-padded beyond n) and Vs (m x m, column p at
+// Vs[p*m]) live in shared memory; cs holds m values, pr m+2 ints, red at least
+// two doubles (used as three int flags).  On return the diagonal of A holds the
 // eigenvalues and the columns of Vs the eigenvectors (unsorted).
+//
+// A pair (p, q) is rotated while |a_pq| > tol * sqrt(|a_pp a_qq|) (the
+// relative threshold of Demmel and Veselic, "Jacobi's method is more accurate
+// than QR", 1992), and the rotated a_pq is set to zero exactly, so the sweeps
+// end once a whole sweep rotates nothing; max_sweeps is only a safety cap.
+// One round updates every 2 x 2 block (rows of pair P, columns of pair Q) in
+// a single pass, R_P^T A_PQ R_Q, written to both triangles so A stays exactly
+// symmetric.  blockDim.x must be a multiple of 32.
 template <class T>
-__device__ int cta_jacobi(T* A, T* Vs, T* cs, int* pr, double* red, int m, int max_sweeps) {
-  const int tid = threadIdx.x;
-  const double eps = sizeof(T) == 8 ? 1e-14 : 2e-6;
+__device__ int cta_jacobi(T* A, T* Vs, T* cs, int* pr, double* red, int m, int max_sweeps,
+                          unsigned* blk = nullptr) {
+  const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, wid = tid >> 5, nw = nt >> 5;
+  const int h = m / 2;
+  const T tol = sizeof(T) == 8 ? T(4.5e-16) : T(2.4e-7);
+  // flag[s % 3]: a rotation happened in sweep s.  The flag cleared at the
+  // start of sweep s was last read at the end of sweep s - 2, with the
+  // barriers of sweep s - 1 in between.
+  volatile int* flag = (volatile int*)red;
+  if (tid == 0) flag[0] = 0;
+  // optional list of the h(h+1)/2 upper-triangle blocks (kp << 16 | kq), so
+  // that every thread takes at most a few blocks without index arithmetic
+  const int nblk = h * (h + 1) / 2;
+  if (blk)
+    for (int kp = wid; kp < h; kp += nw)
+      for (int kq = kp + lane; kq < h; kq += 32) blk[kp * h - kp * (kp - 1) / 2 + (kq - kp)] = (kp << 16) | kq;
+  __syncthreads();
   int sweep = 0;
   for (sweep = 0; sweep < max_sweeps; ++sweep) {
-    double off = 0.0, tot = 0.0;
-    for (int e = tid; e < m * m; e += blockDim.x) {
-      const double v = (double)A[e];
-      tot += v * v;
-      if (e / m != e % m) off += v * v;
-    }
-    off = warp_sum(off);
-    tot = warp_sum(tot);
-    if ((tid & 31) == 0) {
-      red[2 * (tid >> 5)] = off;
-      red[2 * (tid >> 5) + 1] = tot;
-    }
-    __syncthreads();
-    double so = 0.0, st = 0.0;
-    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
-      so += red[2 * w];
-      st += red[2 * w + 1];
-    }
-    __syncthreads();
-    if (so <= eps * eps * st || st == 0.0) break;
+    if (tid == 0) flag[(sweep + 1) % 3] = 0;
     for (int round = 0; round < m - 1; ++round) {
-      for (int kk = tid; kk < m / 2; kk += blockDim.x) {
-        const int a = (kk == 0) ? m - 1 : (kk + round) % (m - 1);
-        const int b = (m - 1 - kk + round) % (m - 1);
+      for (int kk = tid; kk < h; kk += nt) {
+        // round-robin pairs; both sums stay below 2(m-1), so one subtraction
+        // replaces the modulo
+        int a = kk + round, b = m - 1 - kk + round;
+        if (a >= m - 1) a -= m - 1;
+        if (b >= m - 1) b -= m - 1;
+        if (kk == 0) a = m - 1;
         const int p = a < b ? a : b, q = a < b ? b : a;
         pr[2 * kk] = p;
         pr[2 * kk + 1] = q;
         // rotation in the working precision (FP64 division and square root
-        // are slow on GB300; the FP64 path keeps them in FP64)
-        const T apq = A[p * m + q];
+        // are slow on GB300; the FP64 path keeps them in FP64).  This chain
+        // runs on one warp while the block waits, so the FP32 path uses the
+        // approximate reciprocal / reciprocal square root: an angle off by an
+        // ulp still gives an orthogonal rotation (c = 1/sqrt(1+t^2), s = t c)
+        // and the next sweep corrects the residue.
+        const T apq = A[p * m + q], app = A[p * m + p], aqq = A[q * m + q];
         T c = T(1), s = T(0);
-        if (apq != T(0)) {
-          const T tau = (A[q * m + q] - A[p * m + p]) / (T(2) * apq);
-          const T at = fabs(tau);
-          // for huge |tau| use t ~ 1/(2 tau) to avoid overflow of tau*tau
-          const T t = (at > T(1e18)) ? T(1) / (T(2) * tau)
-                                      : (tau >= T(0) ? T(1) : T(-1)) / (at + sqrt(T(1) + tau * tau));
-          c = T(1) / sqrt(T(1) + t * t);
+        if (apq != T(0) && fabs(apq) * fabs(apq) > tol * tol * fabs(app * aqq)) {
+          T t;
+          if (sizeof(T) == 8) {
+            const T tau = (aqq - app) / (T(2) * apq);
+            const T at = fabs(tau);
+            // for huge |tau| use t ~ 1/(2 tau) to avoid overflow of tau*tau
+            t = (at > T(1e150)) ? T(1) / (T(2) * tau) : (tau >= T(0) ? T(1) : T(-1)) / (at + sqrt(T(1) + tau * tau));
+            c = T(1) / sqrt(T(1) + t * t);
+          } else {
+            const float tau = __fdividef((float)(aqq - app), 2.f * (float)apq);
+            const float at = fabsf(tau);
+            const float s2 = fmaf(tau, tau, 1.f);
+            const float tt = (at > 1e18f) ? __fdividef(0.5f, tau) : copysignf(__fdividef(1.f, at + s2 * rsqrtf(s2)), tau);
+            t = (T)tt;
+            c = (T)rsqrtf(fmaf(tt, tt, 1.f));
+          }
           s = t * c;
+          flag[sweep % 3] = 1;
         }
         cs[kk] = c;
-        cs[m / 2 + kk] = s;
+        cs[h + kk] = s;
       }
       __syncthreads();
-      for (int e = tid; e < (m / 2) * m; e += blockDim.x) {
-        const int kk = e / m, i = e - kk * m;
-        const int p = pr[2 * kk], q = pr[2 * kk + 1];
-        const T c = cs[kk], s = cs[m / 2 + kk];
-        const T aip = A[i * m + p], aiq = A[i * m + q];
-        A[i * m + p] = c * aip - s * aiq;
-        A[i * m + q] = s * aip + c * aiq;
-        const T vip = Vs[p * m + i], viq = Vs[q * m + i];
-        Vs[p * m + i] = c * vip - s * viq;
-        Vs[q * m + i] = s * vip + c * viq;
+      // R_P^T A_PQ R_Q for one upper-triangle block, mirrored below
+      auto rotate_block = [&](int kp, int kq) {
+        const int p = pr[2 * kp], q = pr[2 * kp + 1], r = pr[2 * kq], u = pr[2 * kq + 1];
+        const T cp = cs[kp], sp = cs[h + kp], cr = cs[kq], sr = cs[h + kq];
+        if (sp == T(0) && sr == T(0)) return;
+        // columns (r, u) rotated first, then rows (p, q)
+        const T apr = A[p * m + r], apu = A[p * m + u], aqr = A[q * m + r], aqu = A[q * m + u];
+        const T xpr = cr * apr - sr * apu, xpu = sr * apr + cr * apu;
+        const T xqr = cr * aqr - sr * aqu, xqu = sr * aqr + cr * aqu;
+        T ypr = cp * xpr - sp * xqr, yqr = sp * xpr + cp * xqr;
+        T ypu = cp * xpu - sp * xqu, yqu = sp * xpu + cp * xqu;
+        if (kp == kq) {
+          // diagonal block: the rotation annihilates a_pq exactly
+          ypu = T(0);
+          yqr = T(0);
+        }
+        A[p * m + r] = ypr;
+        A[p * m + u] = ypu;
+        A[q * m + r] = yqr;
+        A[q * m + u] = yqu;
+        if (kp != kq) {
+          A[r * m + p] = ypr;
+          A[u * m + p] = ypu;
+          A[r * m + q] = yqr;
+          A[u * m + q] = yqu;
+        }
+      };
+      if (blk) {
+        for (int e = tid; e < nblk; e += nt) rotate_block((int)(blk[e] >> 16), (int)(blk[e] & 0xffffu));
+      } else {
+        // warp w takes block rows kp = w, w + nw, ...; its lanes the columns
+        for (int kp = wid; kp < h; kp += nw)
+          for (int kq = kp + lane; kq < h; kq += 32) rotate_block(kp, kq);
       }
-      __syncthreads();
-      for (int e = tid; e < (m / 2) * m; e += blockDim.x) {
-        const int kk = e / m, j = e - kk * m;
+      for (int kk = wid; kk < h; kk += nw) {
+        const T s = cs[h + kk];
+        if (s == T(0)) continue;
         const int p = pr[2 * kk], q = pr[2 * kk + 1];
-        const T c = cs[kk], s = cs[m / 2 + kk];
-        const T apj = A[p * m + j], aqj = A[q * m + j];
-        A[p * m + j] = c * apj - s * aqj;
-        A[q * m + j] = s * apj + c * aqj;
+        const T c = cs[kk];
+        T* vp = Vs + p * m;
+        T* vq = Vs + q * m;
+        for (int i = lane; i < m; i += 32) {
+          const T vip = vp[i], viq = vq[i];
+          vp[i] = c * vip - s * viq;
+          vq[i] = s * vip + c * viq;
+        }
       }
       __syncthreads();
     }
+    const int rotated = flag[sweep % 3];
+    if (!rotated) break;
   }
+  __syncthreads();
   return sweep;
 }
 

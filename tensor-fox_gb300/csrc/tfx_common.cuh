@@ -85,6 +85,8 @@ struct Acc<float> {
     add2(p, fmaf(x, y, -p));
   }
   __device__ __forceinline__ double value() const { return (double)hi + (double)lo; }
+  __device__ __forceinline__ float hi_or_v() const { return hi; }
+  __device__ __forceinline__ float lo_or_0() const { return lo; }
   __device__ __forceinline__ void warp_reduce() {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
@@ -102,6 +104,8 @@ struct Acc<double> {
   __device__ __forceinline__ void add(double x) { v += x; }
   __device__ __forceinline__ void fma_(double x, double y) { v = fma(x, y, v); }
   __device__ __forceinline__ double value() const { return v; }
+  __device__ __forceinline__ double hi_or_v() const { return v; }
+  __device__ __forceinline__ double lo_or_0() const { return 0.0; }
   __device__ __forceinline__ void warp_reduce() { v = warp_sum(v); }
 };
 
@@ -196,6 +200,199 @@ __device__ __forceinline__ void team_sum_acc(const Team& tm, Acc<T> (&v)[NV], do
                                              int& flip) {
   team_reduce_acc<NV, false>(tm, v, out, rs, flip);
 }
+
+// One-barrier team sum for the CG loop.  Every warp publishes its reduced
+// partial (a float-float pair, or a double on the FP64 path) in its own
+// double-buffered shared-memory slot; after one team barrier every warp of
+// every CTA reads all team_size x 8 partials, local and remote, and combines
+// them with shuffles.  No CTA-level barrier and no FP64 arithmetic on the FP32
+// path; every thread returns the totals as accumulators.  Two calls in a row
+// may reuse a slot buffer only after the barrier of the call in between,
+// which the alternating `flip` guarantees.
+template <int NV>
+struct WarpSlots {
+  double raw[2][TFX_THREADS / 32][NV];
+};
+
+template <int NV>
+__device__ __forceinline__ void team_sum_fast(const Team& tm, Acc<float> (&v)[NV], Acc<float> (&out)[NV],
+                                              WarpSlots<NV>* ws, int& flip) {
+  constexpr int NW = TFX_THREADS / 32;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int j = 0; j < NV; ++j) v[j].warp_reduce();
+  float2* mine = reinterpret_cast<float2*>(&ws->raw[flip][0][0]);
+  if (lane == 0)
+#pragma unroll
+    for (int j = 0; j < NV; ++j) mine[wid * NV + j] = make_float2(v[j].hi, v[j].lo);
+  tm.sync();
+  const int np = tm.size * NW;
+  float2 p[(TFX_MAX_TEAM * NW + 31) / 32][NV];
+#pragma unroll
+  for (int u = 0; u < (TFX_MAX_TEAM * NW + 31) / 32; ++u) {
+    const int q = lane + 32 * u;
+    if (q < np) {
+      const float2* src = tm.peer(mine, q / NW) + (q % NW) * NV;
+#pragma unroll
+      for (int j = 0; j < NV; ++j) p[u][j] = src[j];
+    } else {
+#pragma unroll
+      for (int j = 0; j < NV; ++j) p[u][j] = make_float2(0.f, 0.f);
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < NV; ++j) {
+    Acc<float> a;
+#pragma unroll
+    for (int u = 0; u < (TFX_MAX_TEAM * NW + 31) / 32; ++u) a.add2(p[u][j].x, p[u][j].y);
+    a.warp_reduce();
+    out[j] = a;
+  }
+  flip ^= 1;
+}
+
+template <int NV>
+__device__ __forceinline__ void team_sum_fast(const Team& tm, Acc<double> (&v)[NV], Acc<double> (&out)[NV],
+                                              WarpSlots<NV>* ws, int& flip) {
+  constexpr int NW = TFX_THREADS / 32;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int j = 0; j < NV; ++j) v[j].warp_reduce();
+  double* mine = &ws->raw[flip][0][0];
+  if (lane == 0)
+#pragma unroll
+    for (int j = 0; j < NV; ++j) mine[wid * NV + j] = v[j].v;
+  tm.sync();
+  const int np = tm.size * NW;
+  double p[(TFX_MAX_TEAM * NW + 31) / 32][NV];
+#pragma unroll
+  for (int u = 0; u < (TFX_MAX_TEAM * NW + 31) / 32; ++u) {
+    const int q = lane + 32 * u;
+    if (q < np) {
+      const double* src = tm.peer(mine, q / NW) + (q % NW) * NV;
+#pragma unroll
+      for (int j = 0; j < NV; ++j) p[u][j] = src[j];
+    } else {
+#pragma unroll
+      for (int j = 0; j < NV; ++j) p[u][j] = 0.0;
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < NV; ++j) {
+    Acc<double> a;
+#pragma unroll
+    for (int u = 0; u < (TFX_MAX_TEAM * NW + 31) / 32; ++u) a.add(p[u][j]);
+    a.warp_reduce();
+    out[j] = a;
+  }
+  flip ^= 1;
+}
+
+// Push-based team sum: the CTA reduces its warps' partials first (one CTA
+// barrier), then one lane per team member stores the CTA's partial into that
+// member's shared memory; after one team barrier every warp combines the
+// team_size partials sitting in its own shared memory with shuffles.  Remote
+// traffic is team_size stores per CTA and nothing remote is on the path after
+// the barrier.  Slots alternate with `flip` (see team_sum_fast).
+template <int NV>
+struct PushSlots {
+  double team[2][TFX_MAX_TEAM][NV];
+  double warp[TFX_THREADS / 32][NV];
+};
+
+template <int NV>
+__device__ __forceinline__ void team_sum_push(const Team& tm, Acc<float> (&v)[NV], Acc<float> (&out)[NV],
+                                              PushSlots<NV>* ps, int& flip) {
+  constexpr int NW = TFX_THREADS / 32;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  float2* wslot = reinterpret_cast<float2*>(&ps->warp[0][0]);
+  float2* tslot = reinterpret_cast<float2*>(&ps->team[flip][0][0]);
+#pragma unroll
+  for (int j = 0; j < NV; ++j) v[j].warp_reduce();
+  if (lane == 0)
+#pragma unroll
+    for (int j = 0; j < NV; ++j) wslot[wid * NV + j] = make_float2(v[j].hi, v[j].lo);
+  __syncthreads();
+  if (wid == 0) {
+#pragma unroll
+    for (int j = 0; j < NV; ++j) {
+      Acc<float> a;
+      if (lane < NW) {
+        const float2 q = wslot[lane * NV + j];
+        a.hi = q.x;
+        a.lo = q.y;
+      }
+#pragma unroll
+      for (int o = 1; o < NW; o <<= 1) {
+        const float oh = __shfl_xor_sync(0xffffffffu, a.hi, o);
+        const float ol = __shfl_xor_sync(0xffffffffu, a.lo, o);
+        a.add2(oh, ol);
+      }
+      // lanes 0..NW-1 hold the CTA total; every storing lane takes lane 0's
+      a.hi = __shfl_sync(0xffffffffu, a.hi, 0);
+      a.lo = __shfl_sync(0xffffffffu, a.lo, 0);
+      if (lane < tm.size) tm.peer(tslot, lane)[tm.rank * NV + j] = make_float2(a.hi, a.lo);
+    }
+  }
+  tm.sync();
+#pragma unroll
+  for (int j = 0; j < NV; ++j) {
+    Acc<float> a;
+    if (lane < tm.size) {
+      const float2 q = tslot[lane * NV + j];
+      a.hi = q.x;
+      a.lo = q.y;
+    }
+#pragma unroll
+    for (int o = 1; o < TFX_MAX_TEAM; o <<= 1) {
+      const float oh = __shfl_xor_sync(0xffffffffu, a.hi, o);
+      const float ol = __shfl_xor_sync(0xffffffffu, a.lo, o);
+      a.add2(oh, ol);
+    }
+    a.hi = __shfl_sync(0xffffffffu, a.hi, 0);
+    a.lo = __shfl_sync(0xffffffffu, a.lo, 0);
+    out[j] = a;
+  }
+  flip ^= 1;
+}
+
+template <int NV>
+__device__ __forceinline__ void team_sum_push(const Team& tm, Acc<double> (&v)[NV], Acc<double> (&out)[NV],
+                                              PushSlots<NV>* ps, int& flip) {
+  constexpr int NW = TFX_THREADS / 32;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  double* wslot = &ps->warp[0][0];
+  double* tslot = &ps->team[flip][0][0];
+#pragma unroll
+  for (int j = 0; j < NV; ++j) v[j].warp_reduce();
+  if (lane == 0)
+#pragma unroll
+    for (int j = 0; j < NV; ++j) wslot[wid * NV + j] = v[j].v;
+  __syncthreads();
+  if (wid == 0) {
+#pragma unroll
+    for (int j = 0; j < NV; ++j) {
+      double a = lane < NW ? wslot[lane * NV + j] : 0.0;
+#pragma unroll
+      for (int o = 1; o < NW; o <<= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+      a = __shfl_sync(0xffffffffu, a, 0);
+      if (lane < tm.size) tm.peer(tslot, lane)[tm.rank * NV + j] = a;
+    }
+  }
+  tm.sync();
+#pragma unroll
+  for (int j = 0; j < NV; ++j) {
+    double a = lane < tm.size ? tslot[lane * NV + j] : 0.0;
+#pragma unroll
+    for (int o = 1; o < TFX_MAX_TEAM; o <<= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+    out[j].v = __shfl_sync(0xffffffffu, a, 0);
+  }
+  flip ^= 1;
+}
+
+// the accumulator's value in the working precision
+__device__ __forceinline__ float acc_val(const Acc<float>& a) { return a.hi + a.lo; }
+__device__ __forceinline__ double acc_val(const Acc<double>& a) { return a.v; }
 
 template <int NV>
 __device__ __forceinline__ void team_sum(const Team& tm, double (&v)[NV], RedScratch<NV>* rs, int& flip) {

@@ -89,6 +89,7 @@ _EXTRA_SIGNATURES = {
     "tfx_mode_gram": [_I, _P, _LL, _I, _LL, _P, _P, _SZ, _P],
     "tfx_gemm": [_I, _P, _P, _P, _LL, _LL, _LL, _LL, POINTER(c_longlong), _D, _D, _P],
     "tfx_orthonormalize": [_I, _P, _I, _I, _P],
+    "tfx_ttm": [_I, _P, _LL, _I, _LL, _P, _I, _P, _P],
     "tfx_sym_eig": [_I, _P, _I, _P, _P, _I, _P, _P],
     "tfx_flip_signs": [_I, _P, _I, _I, _P],
     "tfx_cp_residual": [_I, _P, _I, POINTER(c_int), _I, _P, _P, _P, _P],

@@ -95,7 +95,7 @@ class _Batch:
         self.stats = torch.zeros((self.n, 4 * self.maxiter), dtype=torch.float64, device=tensors[0].device)
         self.result = torch.zeros((self.n, 4), dtype=torch.int32, device=tensors[0].device)
         self.info = torch.zeros((self.n, 8), dtype=torch.float64, device=tensors[0].device)
-        self.prof = torch.zeros((self.n, 16), dtype=torch.int64, device=tensors[0].device)
+        self.prof = torch.zeros((self.n, 24), dtype=torch.int64, device=tensors[0].device)
         self.desc = (_lib.DgnProblem * self.n)()
         for p in range(self.n):
             d = self.desc[p]

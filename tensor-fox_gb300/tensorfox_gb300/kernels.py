@@ -93,12 +93,7 @@ def ttm(S, shape, l, Ut):
     n = int(Ut.shape[0])
     out = torch.empty(P * n * Q, dtype=S.dtype, device=S.device)
     Uc = Ut.contiguous()
-    if Q >= 16:
-        # batch over p: (n x D) (D x Q)
-        gemm(Uc, S, out, n, Q, D, P, [0, D, 1, D * Q, Q, 1, n * Q, Q, 1])
-    else:
-        # batch over q: (P x D) (D x n)
-        gemm(S, Uc, out, P, n, D, Q, [1, D * Q, Q, 0, 1, D, 1, n * Q, Q])
+    _lib.call("tfx_ttm", _dt(S), _vp(S), P, D, Q, _vp(Uc), n, _vp(out), _st())
     new_shape = list(shape)
     new_shape[l] = n
     return out.view(*new_shape), new_shape
@@ -111,12 +106,18 @@ def orthonormalize(Y):
     return Y
 
 
-def sym_eig(A, max_sweeps=40):
-    """Eigenvalues (descending) and eigenvectors (rows of the returned (n, n) tensor)."""
+def sym_eig(A, max_sweeps=40, return_sweeps=False):
+    """Eigenvalues (descending) and eigenvectors (rows of the returned (n, n) tensor).
+
+    With ``return_sweeps`` the number of Jacobi sweeps taken is returned too."""
     n = A.shape[0]
     ev = torch.empty(n, dtype=A.dtype, device=A.device)
     V = torch.empty((n, n), dtype=A.dtype, device=A.device)
-    _lib.call("tfx_sym_eig", _dt(A), _vp(A.contiguous()), int(n), _vp(ev), _vp(V), int(max_sweeps), None, _st())
+    sw = torch.zeros(1, dtype=torch.int32, device=A.device) if return_sweeps else None
+    _lib.call("tfx_sym_eig", _dt(A), _vp(A.contiguous()), int(n), _vp(ev), _vp(V), int(max_sweeps),
+              _vp(sw) if sw is not None else None, _st())
+    if return_sweeps:
+        return ev, V, int(sw.cpu()[0])
     return ev, V
 
 

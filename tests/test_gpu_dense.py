@@ -176,3 +176,52 @@ def test_cpd_fp32_planted():
     f, out = tfx.cpd(T, R)
     assert out.rel_error < 2e-3
     assert _congruence(f, W) > 0.999
+
+
+@pytest.mark.parametrize("shape,l,n", [((512, 96, 64), 0, 50), ((50, 128, 2048), 1, 50), ((64, 64, 72), 0, 70),
+                                       ((12, 40, 128), 1, 9)])
+def test_ttm_f32_tiled(shape, l, n):
+    """FP32 mode products on the register-tiled path (D, Q multiples of 4, Q >= 128)."""
+    rng = np.random.default_rng(5)
+    T = rng.standard_normal(shape).astype(np.float32)
+    U = rng.standard_normal((shape[l], n)).astype(np.float32)
+    out, _ = kernels.ttm(dev(T, torch.float32), list(shape), l, dev(U.T.copy(), torch.float32))
+    ref = np.moveaxis(np.tensordot(U.T.astype(np.float64), T.astype(np.float64), axes=(1, l)), 0, l)
+    scale = np.sqrt(shape[l]) * np.abs(U).max() * np.abs(T).max()
+    np.testing.assert_allclose(out.cpu().numpy(), ref, rtol=0, atol=2e-6 * scale)
+
+
+def test_orthonormalize_f32_graded():
+    """CGS2 keeps FP32 columns orthonormal when their norms span eight decades (a
+    subspace-iteration block with signal and noise directions)."""
+    rng = np.random.default_rng(6)
+    D, k = 512, 60
+    scales = 10.0 ** -np.linspace(0, 8, k)
+    Y = (rng.standard_normal((k, D)) * scales[:, None]).astype(np.float32)
+    Yd = dev(Y, torch.float32)
+    kernels.orthonormalize(Yd)
+    Q = Yd.double().cpu().numpy()
+    np.testing.assert_allclose(Q @ Q.T, np.eye(k), atol=2e-6)
+    # the leading columns span the same space as the input's leading columns
+    for j in (1, 8, 20):
+        P = Q[:j].T @ Q[:j]
+        Yj = Y[:j].astype(np.float64)
+        assert np.linalg.norm(P @ Yj.T - Yj.T) <= 1e-5 * np.linalg.norm(Yj)
+
+
+@pytest.mark.parametrize("n", [60, 33])
+def test_sym_eig_f32_graded(n):
+    """FP32 Jacobi on a Rayleigh-Ritz sized matrix with a graded spectrum stops by
+    its relative threshold (well before the sweep cap) and resolves the leading pairs."""
+    rng = np.random.default_rng(7 + n)
+    V0 = np.linalg.qr(rng.standard_normal((n, n)))[0]
+    lam = 10.0 ** -np.linspace(0, 8, n)
+    A = (V0 * lam) @ V0.T
+    ev, V, sweeps = kernels.sym_eig(dev(A, torch.float32), return_sweeps=True)
+    assert sweeps < 20
+    ev, V = ev.double().cpu().numpy(), V.double().cpu().numpy()
+    np.testing.assert_allclose(ev[:10], lam[:10], rtol=5e-5)
+    # ~12 sweeps of 59 rotations per vector in FP32
+    np.testing.assert_allclose(V @ V.T, np.eye(n), atol=5e-5)
+    for i in range(5):
+        assert abs(abs(V[i] @ V0[:, i]) - 1.0) < 1e-5
