@@ -79,7 +79,7 @@ __host__ __device__ inline size_t g3_floats(int d0, int d1, int d2) {
 }
 
 struct SmemPlan {
-  size_t sA, sB, sPart, sAk, sY, sM, sDG, sGam, sNorm, sBase, sIdx, rs4, rs12, misc, hist, rs1, rs1b, sScale, wsl, sG3;
+  size_t sA, sB, sPart, sAk, sY, sM, sDG, sGam, sNorm, sBase, sIdx, rs4, rs12, misc, hist, rs1, rs1b, sScale, wsl, sG3, sE3;
   size_t sQf, sWf, sP1o, sP2o, sVec;  // staged operands of the CG (valid when stage != 0)
   int stage;
   size_t total;
@@ -115,9 +115,13 @@ __host__ __device__ inline SmemPlan smem_plan(int TS, size_t es, int maxL, int m
   // third-order gradient scratch (every mode up to 64): three slab stages,
   // transposed own factor columns, M0 | M1 | M2, partial sums, stage barriers
   p.sG3 = 0;
+  p.sE3 = 0;
   if (maxL == 3 && maxd <= 64) {
     p.sG3 = o;
     o += al16(g3_floats(maxd, maxd, maxd) * es + 64);
+    // residual scratch: W1 and W2 with rows padded to four (R x d padded)
+    p.sE3 = o;
+    o += al16((size_t)maxR * 2 * (((size_t)maxd + 3) & ~(size_t)3) * es);
   }
   p.stage = stage;
   p.sQf = p.sWf = p.sP1o = p.sP2o = p.sVec = o;
@@ -572,6 +576,7 @@ struct Engine {
   T* sG3;       // third-order gradient scratch, or nullptr
   size_t g3off; // its offset in dynamic shared memory
   unsigned g3base;  // slabs streamed so far: slab n uses stage n % 3, phase (n / 3) & 1
+  size_t e3off;     // third-order residual scratch offset
   int g3err;      // a slab wait ran out
   const T* Wr;  // factors to read: shared-memory copy when staged
 
@@ -1159,6 +1164,119 @@ struct Engine {
 
   // ||T - [[W]]|| / ||T|| (Conversion.py:117-141 + Critical.py:14-22), fused:
   // the model tile is built in registers and never stored.
+  // -------------------------------------------------------------------------
+  // Third-order relative error |T - [[W]]| / |T| (Auxiliar.py:131-158 via
+  // GaussNewton.py:197): the team splits the slabs T[i, :, :], which stream
+  // through the gradient's stage ring; a thread forms a 4 x 4 block of
+  //   X[j, k] = sum_r W0[i, r] W1[j, r] W2[k, r]
+  // from W1 and W2 staged with rows padded to four, and sums (T - X)^2 in
+  // float-float.  Same conditions as the third-order gradient.
+  // -------------------------------------------------------------------------
+  __device__ double rel_error_l3(const T* Wf) {
+    const int d0 = d[0], d1 = d[1], d2 = d[2];
+    const int d1p = (d1 + 3) & ~3, d2p = (d2 + 3) & ~3;
+    char* smb = dyn_smem();
+    T* sBt = (T*)(smb + e3off);  // R x d1p
+    T* sCt = sBt + R * d1p;      // R x d2p
+    const int SL = (int)g3_stage(d1, d2);
+    T* sT = (T*)(smb + g3off);
+    unsigned long long* mbar = (unsigned long long*)(smb + g3off + g3_floats(d0, d1, d2) * sizeof(T));
+    for (int e = tid; e < R * d1p; e += TFX_THREADS) {
+      const int r = e / d1p, j = e - r * d1p;
+      sBt[e] = j < d1 ? Wf[off[1] + r * d1 + j] : T(0);
+    }
+    for (int e = tid; e < R * d2p; e += TFX_THREADS) {
+      const int r = e / d2p, k = e - r * d2p;
+      sCt[e] = k < d2 ? Wf[off[2] + r * d2 + k] : T(0);
+    }
+    const int first = tm.rank, step = tm.size;
+    const int nmy = first < d0 ? (d0 - 1 - first) / step + 1 : 0;
+    const unsigned bytes = (unsigned)((size_t)d1 * d2 * sizeof(T));
+    auto issue = [&](int t) {
+      if (tid == 0) {
+        const int b = (int)((g3base + t) % 3);
+        const unsigned mb = (unsigned)__cvta_generic_to_shared(mbar + b);
+        const unsigned dst = (unsigned)__cvta_generic_to_shared(sT + b * SL);
+        asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(mb), "r"(bytes) : "memory");
+        asm volatile(
+            "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(dst),
+            "l"(Tt + (long long)(first + t * step) * d1 * d2), "r"(bytes), "r"(mb)
+            : "memory");
+      }
+    };
+    __syncthreads();  // staged W1, W2; every stage is free (the gradient ended with barriers)
+    if (nmy > 0) issue(0);
+    if (nmy > 1) issue(1);
+    const int nk4 = d2p >> 2, nj4 = d1p >> 2;
+    const int j4 = tid / nk4, k4 = tid - j4 * nk4;
+    const bool active = tid < nj4 * nk4;  // <= 16 x 16
+    Acc<T> acc;
+    for (int t = 0; t < nmy; ++t) {
+      const unsigned n = g3base + t;
+      {
+        const unsigned mb = (unsigned)__cvta_generic_to_shared(mbar + n % 3);
+        const unsigned par = (n / 3) & 1;
+        unsigned ok = 0;
+        for (int it = 0; it < (1 << 24) && !ok; ++it)
+          asm volatile(
+              "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+              : "=r"(ok)
+              : "r"(mb), "r"(par)
+              : "memory");
+        if (!ok) g3err = 1;
+      }
+      __syncthreads();  // every warp is past slab t-1: its stage may be refilled
+      if (t + 2 < nmy) issue(t + 2);
+      if (active) {
+        const int i = first + t * step;
+        T x[4][4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+#pragma unroll
+          for (int v = 0; v < 4; ++v) x[u][v] = T(0);
+        const T* a = Wf + off[0] + i;
+#pragma unroll 2
+        for (int r = 0; r < R; ++r) {
+          const T ai = a[r * d0];
+          T b[4], c[4];
+          lds4(sBt + r * d1p + 4 * j4, b);
+          lds4(sCt + r * d2p + 4 * k4, c);
+#pragma unroll
+          for (int u = 0; u < 4; ++u) {
+            const T bu = ai * b[u];
+#pragma unroll
+            for (int v = 0; v < 4; ++v) x[u][v] = fma(bu, c[v], x[u][v]);
+          }
+        }
+        const T* slab = sT + (n % 3) * SL;
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const int j = 4 * j4 + u;
+#pragma unroll
+          for (int v = 0; v < 4; ++v) {
+            const int k = 4 * k4 + v;
+            if (j < d1 && k < d2) {
+              const T df = slab[j * d2 + k] - x[u][v];
+              acc.fma_(df, df);
+            }
+          }
+        }
+      }
+    }
+    g3base += nmy;
+    Acc<T> v1[1] = {acc}, tot[1];
+    team_sum_push<1>(tm, v1, tot, (PushSlots<1>*)(smb + cgo.wsl), flipw);
+    // one thread forms the double result (FP64 is slow on GB300), the CTA reads it
+    double* res = (double*)(smb + e3off);
+    __syncthreads();  // the staged factors are no longer read
+    if (tid == 0) *res = sqrt(acc_val_d(tot[0])) / Tsize;
+    __syncthreads();
+    const double out = *res;
+    __syncthreads();  // the slot is scratch again
+    return out;
+  }
+
   __device__ double rel_error(const T* Wf) {
     const int tx = tid & 15, ty = tid >> 4;
     const long long Q0 = N / d[0];
@@ -1298,7 +1416,7 @@ struct Engine {
       tm.sync();
       stage_W();
       team_sum<4>(tm, s, rs4, flip4);
-      error = rel_error(Wr);
+      error = sG3 ? rel_error_l3(Wr) : rel_error(Wr);
       const double num = (Tsize * Tsize) * (old_error * old_error - error * error);
       if (s[0] != 0.0) {
         gain = num / s[0];
@@ -1435,6 +1553,7 @@ __device__ void solve_problem(const tfx_dgn_problem& pb, const tfx_dgn_options& 
               ? (T*)(smem + sp.sG3)
               : nullptr;
   E.g3off = sp.sG3;
+  E.e3off = sp.sE3;
   E.g3base = 0;
   E.g3err = 0;
   if (E.sG3 && threadIdx.x == 0) {
@@ -1524,7 +1643,7 @@ __device__ void solve_problem(const tfx_dgn_problem& pb, const tfx_dgn_options& 
     E.tm.sync();
     E.stage_W();
     tick(3);
-    error = E.rel_error(E.Wr);
+    error = E.sG3 ? E.rel_error_l3(E.Wr) : E.rel_error(E.Wr);
     tick(4);
     if (it > 3 && error > op.tol_jump * old_error) {
       error = E.dogleg(error);

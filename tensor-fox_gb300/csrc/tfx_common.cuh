@@ -393,6 +393,9 @@ __device__ __forceinline__ void team_sum_push(const Team& tm, Acc<double> (&v)[N
 // the accumulator's value in the working precision
 __device__ __forceinline__ float acc_val(const Acc<float>& a) { return a.hi + a.lo; }
 __device__ __forceinline__ double acc_val(const Acc<double>& a) { return a.v; }
+// the accumulator's value in double
+__device__ __forceinline__ double acc_val_d(const Acc<float>& a) { return (double)a.hi + (double)a.lo; }
+__device__ __forceinline__ double acc_val_d(const Acc<double>& a) { return a.v; }
 
 template <int NV>
 __device__ __forceinline__ void team_sum(const Team& tm, double (&v)[NV], RedScratch<NV>* rs, int& flip) {

@@ -85,19 +85,32 @@ def _precision(T, options):
     return 'fp64' if np.asarray(T).dtype == np.float64 else 'fp32'
 
 
-def starting_point_random(dims, R, options):
-    """'random' initialisation in the compressed space (Initialization.py:61-94)."""
+def starting_point_random(dims, R, options, vectorized=False):
+    """'random' initialisation in the compressed space (Initialization.py:61-94).
+
+    ``vectorized`` balances all columns at once; its column norms may differ
+    from the per-column ones in the last bit of a float64, which a float32
+    engine never sees."""
     f = [np.random.randn(dims[l], R) for l in range(len(dims))]
     for l in range(len(dims)):             # clean_zeros (Initialization.py:361-386)
         W = f[l]
         for i, r in zip(*np.nonzero(W == 0.0)):
             W[i, r] = 1e-4 * np.random.randn() * np.linalg.norm(W)
-    for r in range(R):                      # equalize (Conversion.py:361-387)
-        nr = np.array([np.linalg.norm(f[l][:, r]) for l in range(len(dims))])
-        if np.prod(nr) != 0.0:
-            g = np.prod(nr) ** (1 / len(dims))
-            for l in range(len(dims)):
-                f[l][:, r] = (g / nr[l]) * f[l][:, r]
+    L = len(dims)
+    if vectorized:                          # equalize, all columns together
+        nr = np.stack([np.linalg.norm(f[l], axis=0) for l in range(L)])
+        p = np.prod(nr, axis=0)
+        ok = p != 0.0
+        g = np.where(ok, p, 1.0) ** (1 / L)
+        for l in range(L):
+            f[l] = np.where(ok, g / np.where(ok, nr[l], 1.0), 1.0) * f[l]
+    else:
+        for r in range(R):                  # equalize (Conversion.py:361-387)
+            nr = np.array([np.linalg.norm(f[l][:, r]) for l in range(L)])
+            if np.prod(nr) != 0.0:
+                g = np.prod(nr) ** (1 / L)
+                for l in range(L):
+                    f[l][:, r] = (g / nr[l]) * f[l][:, r]
     if options.symm:
         s = f[0]
         for l in range(1, len(dims)):
@@ -168,7 +181,7 @@ def tricpd(T, R, options):
             W = torch.from_numpy(np.asarray(o.initialization[ordering[l]], dtype=np.float64)).to(Td.device, dt)
             init.append(kernels.matmul(Uts[l], W).double().cpu().numpy())
     elif o.initialization == 'random':
-        init = starting_point_random(core, R, o)
+        init = starting_point_random(core, R, o, vectorized=(prec == 'fp32'))
     else:
         raise NotImplementedError("initialization %r is outside the dGN path" % (o.initialization,))
     x0 = _flat_dev(init, dt, Td.device)
