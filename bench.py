@@ -262,6 +262,8 @@ def run_ours(args):
     t_gram = g0.elapsed_time(g1) / 1e3 / nrep
 
     batched = run_batched(args) if not args.no_batched else None
+    sparse_leg = run_sparse(args) if not args.no_sparse else None
+    autograd_leg = run_autograd(args) if not args.no_batched else None
     flops = 2.0 * DIMS[0] * DIMS[0] * DIMS[1] * DIMS[2]
     hbm, bf16, src = peaks()
     achieved_tf = flops / t_gram / 1e12
@@ -297,6 +299,10 @@ def run_ours(args):
         line["cpu_baseline"] = cpu
     if batched is not None:
         line["batched"] = batched
+    if sparse_leg is not None:
+        line["sparse"] = sparse_leg
+    if autograd_leg is not None:
+        line["autograd"] = autograd_leg
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:
@@ -304,7 +310,95 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
-def run_batched(args, n=1024, seed=7):
+def run_sparse(args, dims=(20000, 20000, 20000), nnz=10_000_000, R=16, seed=11):
+    """c5: COO MTTKRP and sparse residual at 20000^3 with 1e7 nonzeros, rank 16.
+
+    Algorithmic bytes per MTTKRP mode and per residual pass: nnz * (L*4 + 4) --
+    int32 coordinates (re-encoded once at the boundary) plus an FP32 value; the
+    16-wide factor rows (1.28 MB per mode) are gathered from L2 and not counted.
+    Setup (coordinate encoding, the per-mode counting sorts) is done once before
+    the timed region."""
+    import torch
+    from tensorfox_gb300 import sparse as tsp
+    rng = np.random.default_rng(seed)
+    L = len(dims)
+    space = int(np.prod(np.array(dims, dtype=np.int64)))
+    key = np.unique(rng.integers(0, space, size=int(nnz * 1.001), dtype=np.int64))[:nnz]
+    idx = np.empty((key.size, L), dtype=np.int64)
+    rem = key.copy()
+    for l in range(L - 1, -1, -1):
+        idx[:, l] = rem % dims[l]
+        rem //= dims[l]
+    W = [rng.standard_normal((d, R)).astype(np.float32) for d in dims]
+    vals = np.ones((key.size, R), dtype=np.float32)
+    for l in range(L):
+        vals *= W[l][idx[:, l]]
+    vals = vals.sum(axis=1)
+    vals += 0.01 * np.linalg.norm(vals) / np.sqrt(vals.size) * rng.standard_normal(vals.size).astype(np.float32)
+    X = tsp.DeviceCOO(vals, idx, dims, torch.float32)
+    Wd = [torch.from_numpy(w).cuda() for w in W]
+    for l in range(L):
+        tsp.coo_mttkrp(X, Wd, l)      # builds the per-mode sorted copies
+    tsp.sparse_residual_sq(X, Wd)
+    torch.cuda.synchronize()
+    stream = torch.cuda.current_stream()
+    reps = 5
+    bytes_pass = float(X.nnz) * (L * 4 + 4)
+    out = {"workload": "COO %s, %d nonzeros (unique uniform coordinates), rank %d, planted N(0,1) + 1%% noise"
+           % ("x".join(str(d) for d in dims), X.nnz, R), "bytes_per_pass": bytes_pass}
+    hbm, _, src = peaks()
+    for l in range(L):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for _ in range(reps):
+            tsp.coo_mttkrp(X, Wd, l)
+        b.record(stream)
+        torch.cuda.synchronize()
+        t = a.elapsed_time(b) / 1e3 / reps
+        out["mttkrp_mode%d" % l] = {"ms": t * 1e3, "GBps": bytes_pass / t / 1e9, "frac_hbm": bytes_pass / t / 1e9 / hbm}
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record(stream)
+    for _ in range(reps):
+        r2 = tsp.sparse_residual_sq(X, Wd)
+    b.record(stream)
+    torch.cuda.synchronize()
+    t = a.elapsed_time(b) / 1e3 / reps
+    out["residual"] = {"ms": t * 1e3, "GBps": bytes_pass / t / 1e9, "frac_hbm": bytes_pass / t / 1e9 / hbm,
+                       "rel_error_planted": float(np.sqrt(r2.item()) / np.linalg.norm(vals))}
+    out["hbm_peak_GBps"] = hbm
+    out["cpu_reference"] = "not run at this scale: the reference's sparse core product alone is ~3e13 FMA"
+    return out
+
+
+def run_autograd(args, R=64, seed=5):
+    """c3: CP fit loss of a 256x256x3x3 FP32 weight tensor at rank 64, forward + backward."""
+    import torch
+    import tensorfox_gb300 as tfx
+    g = torch.Generator(device="cuda").manual_seed(seed)
+    dims = (256, 256, 3, 3)
+    Wt = torch.randn(dims, device="cuda", generator=g)
+    fs = [(torch.randn((d, R), device="cuda", generator=g) / np.sqrt(np.sqrt(R))).requires_grad_() for d in dims]
+    for _ in range(3):
+        loss = tfx.cp_fit_loss(Wt, fs)
+        loss.backward()
+    torch.cuda.synchronize()
+    stream = torch.cuda.current_stream()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    reps = 20
+    a.record(stream)
+    for _ in range(reps):
+        loss = tfx.cp_fit_loss(Wt, fs)
+        loss.backward()
+    b.record(stream)
+    torch.cuda.synchronize()
+    t = a.elapsed_time(b) / 1e3 / reps
+    N = float(np.prod(dims))
+    flops = 2.0 * R * N + 4 * 2.0 * R * N       # forward residual + four MTTKRPs
+    return {"workload": "CP fit loss, 256x256x3x3 FP32, rank 64, forward + backward", "ms": t * 1e3,
+            "GFLOPs": flops / t / 1e9, "loss": float(loss.item())}
+
+
+def run_batched(args, n=4096, seed=7):
     """c4-style batch: n small FP32 CPDs (dims U[8,64], rank U[2,12], noise 1e-4).
 
     Reports the batch wall time and the engine's J^T J v throughput in the
@@ -385,6 +479,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--no-sparse", action="store_true")
     ap.add_argument("--case", default=None, help="tc_gram_small | engine_core (profiling workloads)")
     args = ap.parse_args()
     if args.case:
