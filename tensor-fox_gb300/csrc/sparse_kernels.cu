@@ -144,6 +144,111 @@ __global__ void __launch_bounds__(256) k_coo_mttkrp(const int* __restrict__ sidx
   }
 }
 
+// four consecutive factor values: one 16-byte read when the row is aligned
+__device__ __forceinline__ float4 ld4(const float* p, bool aligned) {
+  if (aligned) return __ldg(reinterpret_cast<const float4*>(p));
+  return make_float4(__ldg(p), __ldg(p + 1), __ldg(p + 2), __ldg(p + 3));
+}
+
+// FP32 COO MTTKRP with R % 4 == 0: four lanes per entry, lane q holding components r0 + 4q .. r0 + 4q + 3, so each factor
+// row of an entry is gathered as four 16-byte reads by four lanes (one 64-byte
+// row per entry and mode) instead of sixteen scalar reads by one lane; eight
+// entries of the row are in flight per warp.  Lanes with the same q combine
+// their float-float partial sums with shuffles at the end of the row.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_coo_mttkrp_f4(const int* __restrict__ sidx, const float* __restrict__ svals,
+                                                       long long nnz, const long long* __restrict__ rowptr, CooShape sh,
+                                                       int mode, const float* const* __restrict__ Wrow,
+                                                       float* __restrict__ out, int r0) {
+  const int lane = threadIdx.x & 31, q = lane & 3, slot = lane >> 2;
+  const int warps = (gridDim.x * blockDim.x) >> 5;
+  const int d = sh.dims[mode];
+  const int R = sh.R;
+  const int rq = r0 + 4 * q;
+  const bool on = rq < R;
+  const float* wb[TFX_MAX_ORDER];
+  bool al = true;  // rows are 16-byte aligned when every factor base is (R % 4 == 0)
+  for (int m = 0; m < sh.L; ++m) {
+    wb[m] = Wrow[m] + rq;
+    al = al && ((unsigned long long)Wrow[m] & 15ull) == 0;
+  }
+  for (int row = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; row < d; row += warps) {
+    const long long b = rowptr[row], e = rowptr[row + 1];
+    Acc<float> acc[4];
+    for (long long k = b + slot; k < e; k += 8) {
+      const float v = svals[k];
+      float p0 = v, p1 = v, p2 = v, p3 = v;
+      if (on) {
+        for (int m = 0; m < sh.L; ++m) {
+          if (m == mode) continue;
+          const float4 w = ld4(wb[m] + (size_t)sidx[(size_t)m * nnz + k] * R, al);
+          p0 *= w.x;
+          p1 *= w.y;
+          p2 *= w.z;
+          p3 *= w.w;
+        }
+      }
+      acc[0].add(p0);
+      acc[1].add(p1);
+      acc[2].add(p2);
+      acc[3].add(p3);
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+#pragma unroll
+      for (int o = 4; o < 32; o <<= 1) {
+        const float oh = __shfl_xor_sync(0xffffffffu, acc[u].hi, o);
+        const float ol = __shfl_xor_sync(0xffffffffu, acc[u].lo, o);
+        acc[u].add2(oh, ol);
+      }
+    }
+    if (slot == 0 && on) {
+      const float4 r4 = make_float4(acc[0].hi + acc[0].lo, acc[1].hi + acc[1].lo, acc[2].hi + acc[2].lo,
+                                    acc[3].hi + acc[3].lo);
+      *reinterpret_cast<float4*>(out + (size_t)row * R + rq) = r4;
+    }
+  }
+}
+
+// FP32 residual with R % 4 == 0: 16-byte gathers of the factor rows (when
+// aligned), the model summed in a fixed order.
+__global__ void __launch_bounds__(256) k_sparse_residual_f4(const int* __restrict__ idx32, const float* __restrict__ vals,
+                                                            long long nnz, CooShape sh,
+                                                            const float* const* __restrict__ Wrow,
+                                                            double* __restrict__ partial) {
+  __shared__ double red[8];
+  Acc<float> acc;
+  const int R = sh.R, L = sh.L;
+  bool al = true;
+  for (int l = 0; l < L; ++l) al = al && ((unsigned long long)Wrow[l] & 15ull) == 0;
+  for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < nnz; k += (long long)gridDim.x * blockDim.x) {
+    const float* w[TFX_MAX_ORDER];
+    for (int l = 0; l < L; ++l) w[l] = Wrow[l] + (size_t)idx32[(size_t)l * nnz + k] * R;
+    float model = 0.f;
+    for (int r = 0; r < R; r += 4) {
+      float4 p = ld4(w[0] + r, al);
+      for (int l = 1; l < L; ++l) {
+        const float4 x = ld4(w[l] + r, al);
+        p.x *= x.x;
+        p.y *= x.y;
+        p.z *= x.z;
+        p.w *= x.w;
+      }
+      model += (p.x + p.y) + (p.z + p.w);
+    }
+    const float df = vals[k] - model;
+    acc.fma_(df, df);
+  }
+  acc.warp_reduce();
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc.value();
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += red[w];
+    partial[blockIdx.x] = s;
+  }
+}
+
 // ---------------------------------------------------------------------------
 // nnz-only residual: partial sums of (v - sum_r prod_l W_l[i_l, r])^2 per block
 // ---------------------------------------------------------------------------
@@ -445,7 +550,10 @@ extern "C" int tfx_coo_mttkrp(int dtype, const int* sidx, const void* svals, lon
   const int d = dims[mode];
   const int blocks = (int)std::max<long long>(1, std::min<long long>(((long long)d * 32 + 255) / 256, 16LL * sms()));
   for (int r0 = 0; r0 < R; r0 += 16) {
-    if (dtype == TFX_F32)
+    if (dtype == TFX_F32 && R % 4 == 0 && ((unsigned long long)out & 15) == 0)
+      k_coo_mttkrp_f4<<<blocks, 256, 0, st>>>(sidx, (const float*)svals, nnz, rowptr, sh, mode,
+                                              (const float* const*)Wrow_dev, (float*)out, r0);
+    else if (dtype == TFX_F32)
       k_coo_mttkrp<float, 16><<<blocks, 256, 0, st>>>(sidx, (const float*)svals, nnz, rowptr, sh, mode,
                                                       (const float* const*)Wrow_dev, (float*)out, r0);
     else
@@ -466,7 +574,10 @@ extern "C" int tfx_sparse_residual(int dtype, const int* idx32, const void* vals
   cudaStream_t st = (cudaStream_t)stream;
   const int blocks = (int)std::max<long long>(1, std::min<long long>((nnz + 255) / 256, 8LL * sms()));
   double* partial = (double*)scratch;
-  if (dtype == TFX_F32)
+  if (dtype == TFX_F32 && R % 4 == 0)
+    k_sparse_residual_f4<<<blocks, 256, 0, st>>>(idx32, (const float*)vals, nnz, sh, (const float* const*)Wrow_dev,
+                                                 partial);
+  else if (dtype == TFX_F32)
     k_sparse_residual<float><<<blocks, 256, 0, st>>>(idx32, (const float*)vals, nnz, sh, (const float* const*)Wrow_dev,
                                                      partial);
   else

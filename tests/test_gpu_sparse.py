@@ -34,7 +34,8 @@ def rm(W, dt):
 
 
 @pytest.mark.parametrize("dims,R,nnz", [((10, 9, 8), 3, 60), ((30, 20, 25), 7, 900), ((6, 5, 4, 3), 4, 200),
-                                        ((40, 30, 20), 20, 3000)])
+                                        ((40, 30, 20), 20, 3000), ((50, 40, 30), 16, 5000),
+                                        ((25, 30, 35), 32, 4000)])
 @pytest.mark.parametrize("dt", [torch.float64, torch.float32])
 def test_coo_mttkrp_vs_dense(dims, R, nnz, dt):
     data, idxs, W = coo(dims, R, nnz, 1)
@@ -122,3 +123,34 @@ def test_reference_sparse_doctest():
         err = np.linalg.norm(T - orc.cpd2tens(f)) / np.linalg.norm(T)
         best = min(best, err)
     assert best < 1e-4
+
+
+@pytest.mark.parametrize("R", [16, 12])
+def test_coo_vectorized_paths_with_unaligned_factors(R):
+    """The FP32 R % 4 == 0 kernels read factor rows as 16-byte vectors; factor
+    bases off a 16-byte boundary take their scalar reads, with the same result."""
+    dims, nnz = (30, 25, 20), 2500
+    data, idxs, W = coo(dims, R, nnz, 3)
+    X = sparse.DeviceCOO(data, idxs, dims, torch.float32)
+    T = dense_of(data, idxs, dims)
+    Tl = [orc.unfold(T, l + 1) for l in range(len(dims))]
+    al = rm(W, torch.float32)
+    # the same factors at a 4-byte offset inside a larger buffer
+    un = []
+    for w in W:
+        buf = torch.zeros(w.size + 1, dtype=torch.float32, device="cuda")
+        buf[1:] = torch.from_numpy(np.ascontiguousarray(w, dtype=np.float32).ravel()).cuda()
+        un.append(buf[1:].view(w.shape))
+    assert all(u.data_ptr() % 16 != 0 for u in un)
+    for l in range(len(dims)):
+        ref = orc.mttkrp(Tl, W, l)
+        for fac in (al, un):
+            got = sparse.coo_mttkrp(X, fac, l).double().cpu().numpy()
+            np.testing.assert_allclose(got, ref, rtol=1e-5, atol=1e-5 * np.abs(ref).max())
+    model = np.ones((len(data), R))
+    for l in range(len(dims)):
+        model *= W[l][np.asarray(idxs)[:, l]]
+    want = float(np.sum((np.asarray(data) - model.sum(axis=1)) ** 2))
+    for fac in (al, un):
+        got = float(sparse.sparse_residual_sq(X, fac).item())
+        assert abs(got - want) <= 1e-4 * want
