@@ -104,6 +104,10 @@ class Clocks:
                 "samples": len(sm)}
 
 
+def rank_world():
+    return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1"))
+
+
 def dist_info():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -227,10 +231,8 @@ def run_ours(args):
     barrier()
     t_e2e = (time.perf_counter() - t0) / max(1, args.steps // 2)
     if world > 1:
-        import torch.distributed as dist
-        tt = torch.tensor([t_dev, t_e2e], device=dev)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_dev, t_e2e = float(tt[0]), float(tt[1])
+        from tensorfox_gb300.distributed import max_over_ranks
+        t_dev, t_e2e = max_over_ranks([t_dev, t_e2e], device=dev)
 
     # the plain FP32 path on the same input (the north_star's "plain" comparison)
     plain = tfx.make_options(None)
@@ -421,11 +423,16 @@ def run_batched(args, n=4096, seed=7):
     np.random.seed(0)
     tfx.cpd_batch(Ts[:64], Rs[:64], o)
     torch.cuda.synchronize()
+    # with several ranks the problems are sharded (contiguous slices) and the
+    # results gathered; the time is the maximum over ranks
     t0 = time.perf_counter()
     np.random.seed(0)
-    outs = tfx.cpd_batch(Ts, Rs, o)
+    outs = tfx.cpd_batch_distributed(Ts, Rs, o)
     torch.cuda.synchronize()
     t = time.perf_counter() - t0
+    if rank_world()[1] > 1:
+        from tensorfox_gb300.distributed import max_over_ranks
+        t = max_over_ranks([t], device=torch.device("cuda", torch.cuda.current_device()))[0]
     errs = np.array([op.rel_error for _, op in outs])
     # J^T J v products the engine ran (counted on the device), with the
     # algorithmic bytes of each: read W and v, write z (s*3*n_x) and the FP64
@@ -467,6 +474,10 @@ def run_case(case):
             b.launch(gauss_newton.auto_cluster(tuple(S.shape), RANK))
         torch.cuda.synchronize()
         print(json.dumps({"case": case, "result": b.result[0].cpu().numpy().tolist()}))
+    elif case == "sparse_c5":
+        # the c5 COO MTTKRP and residual (20000^3, 1e7 nonzeros, rank 16)
+        res = run_sparse(None)
+        print(json.dumps({"case": case, "mttkrp_mode0_ms": res["mttkrp_mode0"]["ms"]}))
     else:
         raise SystemExit("unknown case " + case)
 
@@ -480,7 +491,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-sparse", action="store_true")
-    ap.add_argument("--case", default=None, help="tc_gram_small | engine_core (profiling workloads)")
+    ap.add_argument("--case", default=None, help="tc_gram_small | engine_core | sparse_c5 (profiling workloads)")
     args = ap.parse_args()
     if args.case:
         run_case(args.case)

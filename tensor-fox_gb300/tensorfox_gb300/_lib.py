@@ -18,6 +18,15 @@ class TfxError(RuntimeError):
     """Raised when an entry point of the C ABI returns a non-zero status."""
 
 
+def check_solve_status(result_rows):
+    """Raise if any solved problem reports a non-zero status (``result[:, 2]``),
+    e.g. a bounded device wait of the engine that ran out."""
+    import numpy as _np
+    st = _np.asarray(result_rows)[..., 2]
+    if _np.any(st != 0):
+        raise TfxError("dGN engine reported status %d (3 = a bounded device wait ran out)" % int(st.max()))
+
+
 class DgnProblem(ctypes.Structure):
     _fields_ = [("L", c_int), ("R", c_int), ("dims", c_int * MAX_ORDER),
                 ("tensor", c_void_p), ("x", c_void_p), ("best", c_void_p), ("work", c_void_p),

@@ -11,7 +11,7 @@ import sys
 import numpy as np
 import torch
 
-from . import _dev, kernels
+from . import _dev, _lib, kernels
 from .compression import mlsvd_device
 from .gauss_newton import _Batch, advance_rng, auto_cluster
 from .options import make_options
@@ -130,6 +130,7 @@ def _run_dgn(Td, x0, R, options, prec):
     c = options.cluster or auto_cluster(tuple(Td.shape), R)
     b.launch(c)
     res = b.result[0].cpu().numpy()
+    _lib.check_solve_status(res)
     stats = b.stats[0].cpu().numpy()
     n = int(res[1])
     advance_rng(options, n)

@@ -206,6 +206,7 @@ def cpd_batch(tensors, ranks, options=None):
     info_h = info.cpu().numpy()
     st_h = stats.cpu().numpy()
     rs_h = result.cpu().numpy()
+    _lib.check_solve_status(rs_h)
     out = []
     for p in range(n):
         R = int(Rs[p])

@@ -179,6 +179,7 @@ def dGN(T, factors, R, options=None, precision=None):
     x0 = torch.from_numpy(_dev.flat_factors(factors)).to(device=Td.device, dtype=dt)
     b = dGN_device(Td, x0, R, options, prec)
     res = b.result[0].cpu().numpy()
+    _lib.check_solve_status(res)
     stats = b.stats[0].cpu().numpy()
     n = int(res[1])
     advance_rng(options, n)
