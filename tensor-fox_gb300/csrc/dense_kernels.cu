@@ -1035,6 +1035,134 @@ extern "C" int tfx_flip_signs(int dtype, void* U, int D, int n, void* stream) {
 
 extern "C" size_t tfx_cp_residual_scratch_bytes(void) { return (size_t)8 * (8 * 1024 + 8); }
 
+// ---------------------------------------------------------------------------
+// FP32 ||T - [[W]]||^2 as a register-tiled GEMM with the Khatri-Rao operand
+// generated on the fly.  A block owns 256 columns q of the other modes: it
+// forms their Khatri-Rao rows once (R x 256, shared memory, R <= 64), then
+// walks every row tile of mode 0: the model tile (8 rows per warp, 8 x 8
+// outputs per lane as in k_ttm_f32) = W_0 (rows x R) KR^T (R x 256), and the
+// epilogue subtracts the streamed tensor tile and accumulates squares in
+// float-float.  Block partials are summed in FP64 by k_sum_partials.
+// ---------------------------------------------------------------------------
+constexpr int RES_BN = 256, RES_RMAX = 64;
+
+__global__ void __launch_bounds__(256, 2) k_cp_residual_f32(const float* __restrict__ Tt, const float* __restrict__ W,
+                                                            CpShape sh, long long Q0, double* __restrict__ partial) {
+  constexpr int TN = 8, BN = RES_BN, AKS = RES_RMAX + 4;
+  extern __shared__ __align__(16) float res_sm[];
+  float* sKR = res_sm;                      // [RES_RMAX][BN]
+  float* sA = sKR + RES_RMAX * BN;          // [64][AKS]
+  __shared__ int sIdx[BN][TFX_MAX_ORDER];
+  __shared__ double red[8];
+  __shared__ int sD[TFX_MAX_ORDER], sOff[TFX_MAX_ORDER];  // shape, indexed at run time
+  const int nw = blockDim.x >> 5, nt = blockDim.x;
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+#pragma unroll
+  for (int l = 0; l < TFX_MAX_ORDER; ++l)
+    if (tid == l) {
+      sD[l] = sh.d[l];
+      sOff[l] = sh.off[l];
+    }
+  const int L = sh.L, R = sh.R, d0 = sh.d[0];
+  const int Rp = (R + 3) & ~3;
+  const int BM = 8 * nw;
+  const long long qt = (Q0 + BN - 1) / BN;
+  Acc<float> acc2;
+  for (long long t = blockIdx.x; t < qt; t += gridDim.x) {
+    const long long q0 = t * BN;
+    __syncthreads();  // shape copied; the previous tile's readers are done
+    for (int c = tid; c < BN; c += nt) {
+      long long q = q0 + c;
+      if (q >= Q0) q = Q0 - 1;  // padding columns repeat a valid one; their terms are skipped
+      for (int l = L - 1; l >= 1; --l) {
+        sIdx[c][l] = (int)(q % sD[l]);
+        q /= sD[l];
+      }
+    }
+    __syncthreads();
+    for (int e = tid; e < Rp * BN; e += nt) {
+      const int r = e / BN, c = e - r * BN;
+      float v = 0.f;
+      if (r < R) {
+        v = 1.f;
+        for (int l = 1; l < L; ++l) v *= __ldg(W + sOff[l] + (size_t)r * sD[l] + sIdx[c][l]);
+      }
+      sKR[r * BN + c] = v;
+    }
+    for (int m0 = 0; m0 < d0; m0 += BM) {
+      __syncthreads();  // KR rows ready / the previous row tile's W_0 slab consumed
+      for (int e = tid; e < BM * Rp; e += nt) {
+        const int m = e / Rp, r = e - m * Rp;
+        sA[m * AKS + r] = (m0 + m < d0 && r < R) ? __ldg(W + (size_t)r * d0 + m0 + m) : 0.f;
+      }
+      __syncthreads();
+      float acc[8][TN];
+#pragma unroll
+      for (int i = 0; i < 8; ++i)
+#pragma unroll
+        for (int j = 0; j < TN; ++j) acc[i][j] = 0.f;
+      for (int k4 = 0; k4 < Rp; k4 += 4) {
+        float4 a[8];
+#pragma unroll
+        for (int i = 0; i < 8; ++i) a[i] = *(const float4*)&sA[(wid * 8 + i) * AKS + k4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          float bv[TN];
+#pragma unroll
+          for (int j4 = 0; j4 < TN / 4; ++j4) {
+            const float4 v = *(const float4*)&sKR[(k4 + u) * BN + j4 * 128 + lane * 4];
+            bv[4 * j4 + 0] = v.x;
+            bv[4 * j4 + 1] = v.y;
+            bv[4 * j4 + 2] = v.z;
+            bv[4 * j4 + 3] = v.w;
+          }
+#pragma unroll
+          for (int i = 0; i < 8; ++i) {
+            const float ai = u == 0 ? a[i].x : u == 1 ? a[i].y : u == 2 ? a[i].z : a[i].w;
+#pragma unroll
+            for (int j = 0; j < TN; ++j) acc[i][j] = fmaf(ai, bv[j], acc[i][j]);
+          }
+        }
+      }
+      // epilogue: the tensor tile (4 consecutive q per read when aligned)
+#pragma unroll
+      for (int i = 0; i < 8; ++i) {
+        const int m = m0 + wid * 8 + i;
+        if (m >= d0) continue;
+#pragma unroll
+        for (int j4 = 0; j4 < TN / 4; ++j4) {
+          const long long q = q0 + j4 * 128 + lane * 4;
+          const float* tp = Tt + (long long)m * Q0 + q;
+          if (q + 3 < Q0 && ((((unsigned long long)tp) & 15) == 0)) {
+            const float4 tv = __ldcs(reinterpret_cast<const float4*>(tp));
+            const float e0 = tv.x - acc[i][4 * j4], e1 = tv.y - acc[i][4 * j4 + 1];
+            const float e2 = tv.z - acc[i][4 * j4 + 2], e3 = tv.w - acc[i][4 * j4 + 3];
+            acc2.fma_(e0, e0);
+            acc2.fma_(e1, e1);
+            acc2.fma_(e2, e2);
+            acc2.fma_(e3, e3);
+          } else {
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+              if (q + u < Q0) {
+                const float df = __ldcs(tp + u) - acc[i][4 * j4 + u];
+                acc2.fma_(df, df);
+              }
+          }
+        }
+      }
+    }
+  }
+  acc2.warp_reduce();
+  if (lane == 0) red[wid] = acc2.value();
+  __syncthreads();
+  if (tid == 0) {
+    double sum = 0.0;
+    for (int w = 0; w < nw; ++w) sum += red[w];
+    partial[blockIdx.x] = sum;
+  }
+}
+
 extern "C" int tfx_cp_residual(int dtype, const void* T, int L, const int* dims, int R, const void* W, double* out,
                                void* scratch, void* stream) {
   if (!T || !dims || !W || !out || !scratch || L < 2 || L > TFX_MAX_ORDER || R < 1)
@@ -1050,10 +1178,24 @@ extern "C" int tfx_cp_residual(int dtype, const void* T, int L, const int* dims,
     s += dims[l];
     if (l) Q0 *= dims[l];
   }
-  const long long tiles = ((dims[0] + 63) / 64) * ((Q0 + 63) / 64);
-  const int blocks = (int)std::max<long long>(1, std::min<long long>(tiles, 8LL * num_sms()));
   cudaStream_t st = (cudaStream_t)stream;
   double* partial = (double*)scratch;
+  if (dtype == TFX_F32 && Q0 >= RES_BN && R <= RES_RMAX) {
+    const int rows = dims[0] < 64 ? dims[0] : 64;
+    const int nw = (rows + 7) / 8;
+    const long long tiles = (Q0 + RES_BN - 1) / RES_BN;
+    const int blocks = (int)std::max<long long>(1, std::min<long long>(tiles, 2LL * num_sms()));
+    const size_t smb = ((size_t)RES_RMAX * RES_BN + 64 * (RES_RMAX + 4)) * sizeof(float);
+    cudaError_t e = cudaFuncSetAttribute(k_cp_residual_f32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smb);
+    if (e != cudaSuccess) return tfx_set_cuda_error(e, "cp_residual attr");
+    k_cp_residual_f32<<<blocks, 32 * nw, smb, st>>>((const float*)T, (const float*)W, sh, Q0, partial);
+    int r = check_launch("cp_residual");
+    if (r) return r;
+    k_sum_partials<<<1, 32, 0, st>>>(partial, blocks, 1, out);
+    return check_launch("sum_partials");
+  }
+  const long long tiles = ((dims[0] + 63) / 64) * ((Q0 + 63) / 64);
+  const int blocks = (int)std::max<long long>(1, std::min<long long>(tiles, 8LL * num_sms()));
   if (dtype == TFX_F32)
     k_cp_residual<float, 4><<<blocks, TFX_THREADS, 0, st>>>((const float*)T, (const float*)W, sh, partial);
   else

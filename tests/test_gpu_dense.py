@@ -66,7 +66,8 @@ def test_orthonormalize():
     np.testing.assert_allclose(P @ Y.T, Y.T, atol=1e-9)
 
 
-@pytest.mark.parametrize("dims,R", [((20, 15, 12), 4), ((9, 8, 7, 6), 3), ((70, 3, 66), 5)])
+@pytest.mark.parametrize("dims,R", [((20, 15, 12), 4), ((9, 8, 7, 6), 3), ((70, 3, 66), 5), ((100, 40, 30), 7),
+                                    ((65, 33, 17), 20), ((12, 300, 2), 50)])
 @pytest.mark.parametrize("dt", [torch.float64, torch.float32])
 def test_cp_residual_and_norms(dims, R, dt):
     rng = np.random.default_rng(4)
