@@ -265,6 +265,7 @@ def run_ours(args):
 
     batched = run_batched(args) if not args.no_batched else None
     sparse_leg = run_sparse(args) if not args.no_sparse else None
+    c1_leg = run_c1(args) if not args.no_batched else None
     autograd_leg = run_autograd(args) if not args.no_batched else None
     flops = 2.0 * DIMS[0] * DIMS[0] * DIMS[1] * DIMS[2]
     hbm, bf16, src = peaks()
@@ -303,6 +304,8 @@ def run_ours(args):
         line["batched"] = batched
     if sparse_leg is not None:
         line["sparse"] = sparse_leg
+    if c1_leg is not None:
+        line["c1_fp64"] = c1_leg
     if autograd_leg is not None:
         line["autograd"] = autograd_leg
     if rank == 0:
@@ -398,6 +401,43 @@ def run_autograd(args, R=64, seed=5):
     flops = 2.0 * R * N + 4 * 2.0 * R * N       # forward residual + four MTTKRPs
     return {"workload": "CP fit loss, 256x256x3x3 FP32, rank 64, forward + backward", "ms": t * 1e3,
             "GFLOPs": flops / t / 1e9, "loss": float(loss.item())}
+
+
+def run_c1(args, seed=101):
+    """c1: plain dGN CPD of a dense FP64 100^3 tensor at rank 10 (planted N(0,1)
+    factors, noise 1e-6 relative, default options): the FP64 GPU path against the
+    FP64 NumPy oracle on the host cores, both timed on the same input."""
+    import torch
+    import tensorfox_gb300 as tfx
+    rng = np.random.default_rng(seed)
+    dims, R = (100, 100, 100), 10
+    W = [rng.standard_normal((d, R)) for d in dims]
+    T = np.einsum("ir,jr,kr->ijk", *W)
+    E = rng.standard_normal(dims)
+    T += 1e-6 * np.linalg.norm(T) / np.linalg.norm(E) * E
+    Td = torch.from_numpy(T).cuda()
+    for _ in range(2):
+        np.random.seed(0)
+        tfx.cpd(Td, R, None)
+    torch.cuda.synchronize()
+    reps = 3
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        np.random.seed(0)
+        _, out = tfx.cpd(Td, R, None)
+    torch.cuda.synchronize()
+    t_gpu = (time.perf_counter() - t0) / reps
+    res = {"workload": "dense FP64 100x100x100, rank 10, noise 1e-6, default options",
+           "gpu_s": t_gpu, "gpu_rel_error": float(out.rel_error), "gpu_steps": int(out.num_steps)}
+    if not args.no_cpu_baseline:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import tfx_oracle as orc
+        np.random.seed(0)
+        t0 = time.perf_counter()
+        _, oc = orc.cpd(T, R, None)
+        res.update({"cpu_oracle_s": time.perf_counter() - t0, "cpu_rel_error": float(oc.rel_error),
+                    "cpu_cores": os.cpu_count()})
+    return res
 
 
 def run_batched(args, n=4096, seed=7):

@@ -226,3 +226,16 @@ def test_sym_eig_f32_graded(n):
     np.testing.assert_allclose(V @ V.T, np.eye(n), atol=5e-5)
     for i in range(5):
         assert abs(abs(V[i] @ V0[:, i]) - 1.0) < 1e-5
+
+
+@pytest.mark.parametrize("M,K,N,tA,tB", [(60, 512, 512, False, False), (50, 60, 512, False, False),
+                                         (70, 64, 256, False, False), (60, 512, 60, False, True),
+                                         (33, 20, 130, False, False), (16, 48, 96, True, False)])
+def test_matmul_f32(M, K, N, tA, tB):
+    """FP32 device products: the wide ones on the register-tiled kernel, the rest on the tiled GEMM."""
+    rng = np.random.default_rng(8)
+    A = rng.standard_normal((K, M) if tA else (M, K)).astype(np.float32)
+    B = rng.standard_normal((N, K) if tB else (K, N)).astype(np.float32)
+    got = kernels.matmul(dev(A, torch.float32), dev(B, torch.float32), transA=tA, transB=tB).double().cpu().numpy()
+    ref = (A.T if tA else A).astype(np.float64) @ (B.T if tB else B).astype(np.float64)
+    np.testing.assert_allclose(got, ref, rtol=0, atol=2e-6 * np.sqrt(K) * np.abs(ref).max())
