@@ -76,8 +76,9 @@ def matmul(A, B, transA=False, transB=False):
     K = A.shape[0] if transA else A.shape[1]
     N = B.shape[0] if transB else B.shape[1]
     C = torch.empty((M, N), dtype=A.dtype, device=A.device)
-    if (not transA and not transB and A.dtype == torch.float32 and K % 4 == 0 and N % 4 == 0 and N >= 128):
-        # a short left factor times a wide right one: the register-tiled mode-product kernel
+    if (not transA and not transB and A.dtype == torch.float32 and K % 4 == 0 and N % 4 == 0 and N >= 16384):
+        # a short left factor times a wide right one (enough column tiles to fill
+        # the GPU): the register-tiled mode-product kernel
         A = A.contiguous()
         B = B.contiguous()
         _lib.call("tfx_ttm", _dt(B), _vp(B), 1, int(K), int(N), _vp(A), int(M), _vp(C), _st())

@@ -228,7 +228,7 @@ def test_sym_eig_f32_graded(n):
         assert abs(abs(V[i] @ V0[:, i]) - 1.0) < 1e-5
 
 
-@pytest.mark.parametrize("M,K,N,tA,tB", [(60, 512, 512, False, False), (50, 60, 512, False, False),
+@pytest.mark.parametrize("M,K,N,tA,tB", [(60, 512, 512, False, False), (50, 60, 20480, False, False),
                                          (70, 64, 256, False, False), (60, 512, 60, False, True),
                                          (33, 20, 130, False, False), (16, 48, 96, True, False)])
 def test_matmul_f32(M, K, N, tA, tB):
