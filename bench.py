@@ -222,14 +222,16 @@ def run_ours(args):
         barrier()
     launches = _lib.launch_count() - l0
     t_dev = ev0.elapsed_time(ev1) / 1e3 / args.steps
-    # end to end: pinned host tensor in, NumPy factors out
+    # end to end: pinned host tensor in (H2D inside the call), NumPy factors out
+    np.random.seed(0)
+    tfx.cpd(Th, R, opts)
     barrier()
     t0 = time.perf_counter()
-    for _ in range(max(1, args.steps // 2)):
+    for _ in range(args.steps):
         np.random.seed(0)
         f_e2e, out_e2e = tfx.cpd(Th, R, opts)
     barrier()
-    t_e2e = (time.perf_counter() - t0) / max(1, args.steps // 2)
+    t_e2e = (time.perf_counter() - t0) / args.steps
     if world > 1:
         from tensorfox_gb300.distributed import max_over_ranks
         t_dev, t_e2e = max_over_ranks([t_dev, t_e2e], device=dev)
