@@ -295,7 +295,7 @@ def run_ours(args):
             "plain_fp32": {"value": t_plain, "unit": "s", "rel_error": float(out_plain.rel_error)},
             "e2e": {"value": t_e2e, "unit": "s", "h2d_bytes_per_step": int(T.nbytes),
                     "d2h_bytes_per_step": int(sum(d * R * 8 for d in DIMS))},
-            "roofline": {"bound": "tensor", "kernel": "k_gram_tc (tcgen05 TF32 mode-1 Gram, 512 x 262144, incl. split-K reduce)",
+            "roofline": {"bound": "tensor", "kernel": "k_gram_tc2 (tcgen05 TF32 mode-1 Gram, 512 x 262144, 2x2 super-blocks, incl. split-K reduce)",
                          "achieved": achieved_tf, "peak": bf16, "unit": "TFLOP/s", "frac": achieved_tf / bf16,
                          "traffic": traffic, "peak_source": src + " bf16 dense (TF32 tensor rate is half of it)"},
             "gpu_launches": int(launches / max(1, args.steps)) * args.steps,

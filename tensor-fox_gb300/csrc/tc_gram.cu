@@ -245,6 +245,170 @@ __global__ void __launch_bounds__(128, 1)
   }
 }
 
+// ---------------------------------------------------------------------------
+// Two-by-two variant: one CTA computes a 256 x 256 super-block (I, J), I <= J,
+// i.e. the four 128 x 128 blocks of row tiles {2I, 2I+1} x column tiles
+// {2J, 2J+1} (three on the diagonal), with four accumulators filling the
+// SM's 512 TMEM columns.  A stage holds four tiles (two when I == J) for 16
+// (12) MMAs, so every byte brought from L2 feeds twice the MMAs of the
+// single-block kernel.  Same split-K partial layout (upper blocks only).
+// ---------------------------------------------------------------------------
+#define TC2_STAGES 3
+
+struct TcGram2Smem {
+  alignas(1024) unsigned char t[TC2_STAGES][4][TCG_TILE_BYTES];  // row tiles 2I, 2I+1, 2J, 2J+1
+  alignas(8) uint64_t full[TC2_STAGES];
+  alignas(8) uint64_t empty[TC2_STAGES];
+  alignas(8) uint64_t done;
+  uint32_t tmem_base;
+  int abort;
+};
+
+__global__ void __launch_bounds__(128, 1)
+    k_gram_tc2(const __grid_constant__ CUtensorMap tmap, int D, long long P, int qchunks, int ksplit, float* part,
+               int* err) {
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  TcGram2Smem& S = *reinterpret_cast<TcGram2Smem*>((((uintptr_t)smem_raw) + 1023) & ~(uintptr_t)1023);
+  const int nt = (D + TCG_BM - 1) / TCG_BM;
+  const int ns = (nt + 1) / 2;
+  int t = blockIdx.x, I = 0;
+  while (t >= ns - I) {
+    t -= ns - I;
+    ++I;
+  }
+  const int J = I + t;
+  const bool diag = I == J;
+  // accumulator p: (A slot, B slot, block row tile, block column tile)
+  const int npair = diag ? 3 : 4;
+  const int pa[4] = {0, 0, diag ? 1 : 1, 1};
+  const int pb[4] = {diag ? 0 : 2, diag ? 1 : 3, diag ? 1 : 2, 3};
+  const long long nchunk = P * qchunks;
+  const long long c0 = nchunk * blockIdx.y / ksplit, c1 = nchunk * (blockIdx.y + 1) / ksplit;
+  const int nit = (int)(c1 - c0);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+
+  if (threadIdx.x == 0) {
+    for (int s2 = 0; s2 < TC2_STAGES; ++s2) {
+      mbar_init(&S.full[s2], 1);
+      mbar_init(&S.empty[s2], 1);
+    }
+    mbar_init(&S.done, 1);
+    S.abort = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 512;" ::"r"(smem_u32(&S.tmem_base))
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = S.tmem_base;
+  const int nload = diag ? 2 : 4;
+  const uint32_t tx = (uint32_t)nload * TCG_TILE_BYTES;
+
+  if (warp == 0 && lane == 0) {
+    int issued = 0;
+    for (int it = 0; it < nit; ++it) {
+      const int s2 = it % TC2_STAGES;
+      if (it >= TC2_STAGES) {
+        if (!mbar_wait(&S.empty[s2], ((it / TC2_STAGES) - 1) & 1)) {
+          atomicExch(err, 1);
+          S.abort = 1;
+          break;
+        }
+      }
+      if (*(volatile int*)&S.abort) break;
+      const long long c = c0 + it;
+      const int p = (int)(c / qchunks);
+      const int q = (int)(c - (long long)p * qchunks) * TCG_BK;
+      mbar_expect_tx(&S.full[s2], tx);
+      tma_load_3d(S.t[s2][0], &tmap, &S.full[s2], q, (2 * I) * TCG_BM, p);
+      tma_load_3d(S.t[s2][1], &tmap, &S.full[s2], q, (2 * I + 1) * TCG_BM, p);
+      if (!diag) {
+        tma_load_3d(S.t[s2][2], &tmap, &S.full[s2], q, (2 * J) * TCG_BM, p);
+        tma_load_3d(S.t[s2][3], &tmap, &S.full[s2], q, (2 * J + 1) * TCG_BM, p);
+      }
+      ++issued;
+    }
+    if (*(volatile int*)&S.abort) {
+      for (int it = (issued > TC2_STAGES ? issued - TC2_STAGES : 0); it < issued; ++it)
+        mbar_wait(&S.full[it % TC2_STAGES], (it / TC2_STAGES) & 1);
+    }
+  } else if (warp == 1 && lane == 0) {
+    constexpr uint32_t idesc = tf32_idesc();
+    for (int it = 0; it < nit; ++it) {
+      const int s2 = it % TC2_STAGES;
+      if (!mbar_wait(&S.full[s2], (it / TC2_STAGES) & 1)) {
+        atomicExch(err, 2);
+        S.abort = 1;
+        break;
+      }
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      for (int pp = 0; pp < npair; ++pp) {
+        const uint64_t da = sw128_desc(S.t[s2][pa[pp]]);
+        const uint64_t db = sw128_desc(S.t[s2][pb[pp]]);
+#pragma unroll
+        for (int kk = 0; kk < TCG_BK / 8; ++kk)
+          mma_tf32(tmem + (uint32_t)(pp * TCG_BM), da + (uint64_t)(kk * 2), db + (uint64_t)(kk * 2), idesc,
+                   (it > 0 || kk > 0) ? 1u : 0u);
+      }
+      mma_commit(&S.empty[s2]);
+    }
+    mma_commit(&S.done);
+  }
+  __syncwarp();
+  if (threadIdx.x == 0) {
+    if (!mbar_wait(&S.done, 0)) {
+      atomicExch(err, 3);
+      S.abort = 1;
+    }
+  }
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const bool ok_all = !*(volatile int*)&S.abort;
+  float* out = part + (size_t)blockIdx.y * D * D;
+  for (int pp = 0; pp < npair; ++pp) {
+    const int bi = (pa[pp] == 0 ? 2 * I : 2 * I + 1);
+    const int bj = (pb[pp] == 0 ? 2 * I : pb[pp] == 1 ? 2 * I + 1 : pb[pp] == 2 ? 2 * J : 2 * J + 1);
+    if (ok_all && nit > 0) {
+      const int row = bi * TCG_BM + warp * 32 + lane;
+#pragma unroll 1
+      for (int cc = 0; cc < TCG_BM; cc += 32) {
+        uint32_t v[32];
+        const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(pp * TCG_BM + cc);
+        asm volatile(
+            "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+            "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+            : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+              "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15]),
+              "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]), "=r"(v[22]),
+              "=r"(v[23]), "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]),
+              "=r"(v[30]), "=r"(v[31])
+            : "r"(taddr));
+        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+        if (row < D) {
+          const int col0 = bj * TCG_BM + cc;
+          float* o = out + (size_t)row * D + col0;
+          for (int j = 0; j < 32; ++j)
+            if (col0 + j < D) o[j] = __uint_as_float(v[j]);
+        }
+      }
+    } else if (ok_all && nit == 0) {
+      for (int e = threadIdx.x; e < TCG_BM * TCG_BM; e += blockDim.x) {
+        const int r = bi * TCG_BM + e / TCG_BM, c = bj * TCG_BM + e % TCG_BM;
+        if (r < D && c < D) out[(size_t)r * D + c] = 0.f;
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 0) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;" ::"r"(tmem) : "memory");
+  }
+}
+
 __global__ void k_gram_tc_reduce(const float* __restrict__ part, int D, int ksplit, float* __restrict__ G) {
   const long long n = (long long)D * D;
   for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x) {
@@ -287,9 +451,13 @@ static int sm_count() {
   return n;
 }
 
+// the 2 x 2 super-block kernel serves Grams with at least two row tiles
+static bool tc_use2(int D) { return (D + TCG_BM - 1) / TCG_BM >= 2; }
+
 static int tc_splits(long long P, int D, long long Q) {
   const int nt = (D + TCG_BM - 1) / TCG_BM;
-  const long long tiles = (long long)nt * (nt + 1) / 2;
+  const int ns = (nt + 1) / 2;
+  const long long tiles = tc_use2(D) ? (long long)ns * (ns + 1) / 2 : (long long)nt * (nt + 1) / 2;
   const long long chunks = P * ((Q + TCG_BK - 1) / TCG_BK);
   long long ks = (sm_count() + tiles - 1) / tiles;
   ks = std::min<long long>(ks, std::max<long long>(1, chunks / 8));
@@ -323,13 +491,23 @@ extern "C" int tfx_mode_gram_tc(const float* S, long long P, int D, long long Q,
                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   if (r != CUDA_SUCCESS) return tfx_set_error(TFX_STATUS_ERR_ARG, "tensor map encoding failed");
   const int nt = (D + TCG_BM - 1) / TCG_BM;
-  const int tiles = nt * (nt + 1) / 2;
   const int qchunks = (int)((Q + TCG_BK - 1) / TCG_BK);
-  const size_t sm = sizeof(TcGramSmem) + 1024;
   cudaStream_t st = (cudaStream_t)stream;
-  cudaError_t e = cudaFuncSetAttribute(k_gram_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-  if (e != cudaSuccess) return tfx_set_cuda_error(e, "mode_gram_tc smem");
-  k_gram_tc<<<dim3(tiles, ks), 128, sm, st>>>(map, D, P, qchunks, ks, (float*)scratch, err);
+  cudaError_t e;
+  if (tc_use2(D)) {
+    const int ns = (nt + 1) / 2;
+    const int tiles = ns * (ns + 1) / 2;
+    const size_t sm = sizeof(TcGram2Smem) + 1024;
+    e = cudaFuncSetAttribute(k_gram_tc2, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    if (e != cudaSuccess) return tfx_set_cuda_error(e, "mode_gram_tc smem");
+    k_gram_tc2<<<dim3(tiles, ks), 128, sm, st>>>(map, D, P, qchunks, ks, (float*)scratch, err);
+  } else {
+    const int tiles = nt * (nt + 1) / 2;
+    const size_t sm = sizeof(TcGramSmem) + 1024;
+    e = cudaFuncSetAttribute(k_gram_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    if (e != cudaSuccess) return tfx_set_cuda_error(e, "mode_gram_tc smem");
+    k_gram_tc<<<dim3(tiles, ks), 128, sm, st>>>(map, D, P, qchunks, ks, (float*)scratch, err);
+  }
   e = cudaGetLastError();
   if (e != cudaSuccess) return tfx_set_cuda_error(e, "mode_gram_tc launch");
   tfx_count_launch(1);

@@ -11,7 +11,7 @@ from tensorfox_gb300 import kernels  # noqa: E402
 
 
 @pytest.mark.parametrize("shape,l", [((256, 64, 32), 0), ((128, 4096), 0), ((300, 40, 36), 0), ((20, 200, 64), 1),
-                                     ((7, 130, 5, 32), 1), ((512, 96, 64), 0)])
+                                     ((7, 130, 5, 32), 1), ((512, 96, 64), 0), ((700, 8, 32), 0)])
 def test_tc_gram_matches_fp64(shape, l):
     rng = np.random.default_rng(7)
     T = rng.standard_normal(shape).astype(np.float32)
