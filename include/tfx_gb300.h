@@ -71,7 +71,7 @@ int tfx_ttm(int dtype, const void* S, long long P, int D, long long Q, const voi
             void* stream);
 /* The same Gram on the 5th-generation tensor cores: TMA-fed SWIZZLE_128B tiles,
  * tcgen05.mma kind::tf32 into TMEM, FP32 accumulation, split-K partials summed
- * in FP64.  FP32 input only; Q >= 32 and Q % 4 == 0; S 16-byte aligned.  *err
+ * in compensated FP32.  FP32 input only; Q >= 32 and Q % 4 == 0; S 16-byte aligned.  *err
  * (device int) receives a non-zero code if a bounded wait expired. */
 size_t tfx_mode_gram_tc_scratch_bytes(long long P, int D, long long Q);
 int tfx_mode_gram_tc(const float* S, long long P, int D, long long Q, float* G, void* scratch, size_t scratch_bytes,

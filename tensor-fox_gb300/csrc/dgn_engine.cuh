@@ -1754,6 +1754,23 @@ __global__ void __launch_bounds__(TFX_THREADS, 1)
   solve_problem<T, TS>(pb, op, tm, smem, sp);
 }
 
+// The same engine for batches of small problems, one CTA each: compiled for
+// TFX_DENSE_CTAS resident CTAs per SM (fewer registers per thread), so that
+// more problems run at once when their shared-memory plans fit.
+#ifndef TFX_DENSE_CTAS
+#define TFX_DENSE_CTAS 2
+#endif
+template <class T, int TS>
+__global__ void __launch_bounds__(TFX_THREADS, TFX_DENSE_CTAS)
+    dgn_kernel_dense(const tfx_dgn_problem* __restrict__ probs, int nprob, tfx_dgn_options op, SmemPlan sp) {
+  extern __shared__ __align__(16) char smem[];
+  Team tm = make_team(1);
+  const int pid = blockIdx.x;
+  if (pid >= nprob) return;
+  tfx_dgn_problem pb = probs[pid];
+  solve_problem<T, TS>(pb, op, tm, smem, sp);
+}
+
 }  // namespace tfx
 
 
@@ -1767,6 +1784,17 @@ namespace tfx {
 template <class T, int TS>
 static int launch_dgn(const tfx_dgn_problem* d_probs, int nprob, const tfx_dgn_options* op, int cluster,
                       const SmemPlan& sp, cudaStream_t st) {
+  if (cluster == 1 && TS <= 2 && nprob > 1 && TFX_DENSE_CTAS * (sp.total + 1024) <= 227 * 1024) {
+    // many small problems: several CTAs per SM
+    auto kd = dgn_kernel_dense<T, TS>;
+    cudaError_t e = cudaFuncSetAttribute(kd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sp.total);
+    if (e != cudaSuccess) return tfx_set_cuda_error(e, "dgn smem attribute");
+    kd<<<nprob, TFX_THREADS, sp.total, st>>>(d_probs, nprob, *op, sp);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return tfx_set_cuda_error(e, "dgn launch");
+    tfx_count_launch(1);
+    return TFX_STATUS_OK;
+  }
   auto kfn = dgn_kernel<T, TS>;
   cudaError_t e = cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sp.total);
   if (e != cudaSuccess) return tfx_set_cuda_error(e, "dgn smem attribute");

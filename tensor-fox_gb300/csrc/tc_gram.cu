@@ -8,7 +8,7 @@
 // TMEM.  Warp 0 issues TMA loads into a ring of shared-memory stages, warp 1
 // issues tcgen05.mma (kind::tf32, M = N = 128, K = 8, four per stage), and all
 // four warps read the accumulator back with tcgen05.ld for the epilogue.
-// Split-K partials are summed by k_gram_reduce-like code in FP64.
+// Split-K partials are summed in float-float (compensated FP32).
 //
 // Replaces the streaming passes of the randomized SVD (Compression.py:337-518)
 // for dense modes with Q a multiple of 4 (TMA row pitch) and Q >= 32.
@@ -414,9 +414,10 @@ __global__ void k_gram_tc_reduce(const float* __restrict__ part, int D, int kspl
   for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x) {
     const int i = (int)(e / D), j = (int)(e - (long long)i * D);
     const long long src = (i / TCG_BM <= j / TCG_BM) ? e : (long long)j * D + i;
-    double s = 0.0;
-    for (int k = 0; k < ksplit; ++k) s += (double)part[(size_t)k * n + src];
-    G[e] = (float)s;
+    // compensated FP32 sum of the partials, in split order (FP64 adds are slow on GB300)
+    Acc<float> s;
+    for (int k = 0; k < ksplit; ++k) s.add(__ldcs(part + (size_t)k * n + src));
+    G[e] = s.hi + s.lo;
   }
 }
 

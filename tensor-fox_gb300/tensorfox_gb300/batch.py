@@ -39,6 +39,53 @@ def _al(n, a=64):
     return (int(n) + a - 1) // a * a
 
 
+def _random_starts(core_dims, Rs, x_off, xh):
+    """Random starting points of every problem, in problem order, written into
+    ``xh`` (the engines' flat layout, column-major per mode).
+
+    The draws are one ``np.random.randn`` call for the whole batch, which
+    yields the same values as the per-problem, per-mode calls of
+    Initialization.py:61-83 taken one after the other.  Column balancing
+    (Conversion.py:361-387) is applied to all columns at once.  A draw that
+    hits an exact zero (probability ~0) falls back to the per-problem path,
+    whose zero replacement draws extra values."""
+    n = len(Rs)
+    L = core_dims.shape[1]
+    sizes = core_dims.astype(np.int64) * Rs.astype(np.int64)[:, None]          # (n, L) block sizes
+    total = int(sizes.sum())
+    state = np.random.get_state()
+    vals = np.random.randn(total)
+    if np.any(vals == 0.0):
+        np.random.set_state(state)
+        for p in range(n):
+            f = _equalize_random([int(d) for d in core_dims[p]], int(Rs[p]))
+            xh[x_off[p]:x_off[p] + sum(W.size for W in f)] = np.concatenate([W.flatten('F') for W in f])
+        return
+    # block (p, l): d x R values, row-major as drawn
+    bsz = sizes.ravel()
+    bstart = np.concatenate([[0], np.cumsum(bsz)[:-1]])
+    bd = np.repeat(core_dims.ravel().astype(np.int64), bsz)                    # d of each value's block
+    bR = np.repeat(np.repeat(Rs.astype(np.int64), L), bsz)                      # R of each value's block
+    within = np.arange(total, dtype=np.int64) - np.repeat(bstart, bsz)
+    row, col = within // bR, within % bR
+    # column ids: problem p, column r -> one id per (p, r); block ids -> (p, l)
+    prob = np.repeat(np.repeat(np.arange(n, dtype=np.int64), L), bsz)
+    roff = np.concatenate([[0], np.cumsum(Rs.astype(np.int64))[:-1]])
+    pc = roff[prob] + col                                                        # (p, r) id
+    mode = np.repeat(np.tile(np.arange(L, dtype=np.int64), n), bsz)
+    lc = pc * L + mode                                                           # (p, r, l) id
+    nrm = np.sqrt(np.bincount(lc, weights=vals * vals, minlength=int(Rs.sum()) * L)).reshape(-1, L)
+    prod = np.prod(nrm, axis=1)
+    ok = prod != 0.0
+    g = np.where(ok, prod, 1.0) ** (1.0 / L)
+    scale = np.where(ok[:, None], g[:, None] / np.where(nrm == 0, 1.0, nrm), 1.0)   # (sum R, L)
+    scaled = vals * scale.ravel()[lc]
+    # destination: problem offset + mode offset + column-major position r * d + i
+    moff = np.concatenate([np.zeros((n, 1), dtype=np.int64), np.cumsum(sizes, axis=1)[:, :-1]], axis=1).ravel()
+    dst = x_off[prob] + np.repeat(moff, bsz) + col * bd + row
+    xh[dst] = scaled
+
+
 def _equalize_random(dims, R):
     f = [np.random.randn(d, R) for d in dims]
     for l in range(len(dims)):
@@ -98,11 +145,13 @@ def cpd_batch(tensors, ranks, options=None):
     c_off = np.concatenate([[0], np.cumsum([_al(v) for v in c_sz])])
     s_sz = [sum(mm) for mm in mins]
     s_off = np.concatenate([[0], np.cumsum([_al(v, 8) for v in s_sz])])
-    host = np.empty(int(t_off[-1]), dtype=np.float64 if prec == 'fp64' else np.float32)
+    # pinned staging buffer: one copy per problem into it, one fast H2D copy
+    pinned = torch.empty(int(t_off[-1]), dtype=torch.float64 if prec == 'fp64' else torch.float32, pin_memory=True)
+    host = pinned.numpy()
     for p, (T, ordering) in enumerate(zip(tensors, orders)):
         a = T.detach().cpu().numpy() if isinstance(T, torch.Tensor) else np.asarray(T)
-        host[t_off[p]:t_off[p] + N[p]] = np.transpose(a, ordering).ravel()
-    Tbuf = torch.from_numpy(host).to(dev)
+        host[t_off[p]:t_off[p] + N[p]].reshape(shapes[p])[...] = np.transpose(a, ordering)
+    Tbuf = pinned.to(dev, non_blocking=False)
     work = torch.empty(int(w_off[-1]), dtype=dt, device=dev)
     Ubuf = torch.empty(int(u_off[-1]), dtype=dt, device=dev)
     Cbuf = torch.empty(max(1, int(c_off[-1])), dtype=dt, device=dev)
@@ -135,9 +184,7 @@ def cpd_batch(tensors, ranks, options=None):
     nx = np.array([int(Rs[p]) * int(core_dims[p].sum()) for p in range(n)], dtype=np.int64)
     x_off = np.concatenate([[0], np.cumsum([_al(v) for v in nx])])
     xh = np.zeros(int(x_off[-1]), dtype=np.float64)
-    for p in range(n):
-        f = _equalize_random([int(d) for d in core_dims[p]], int(Rs[p]))
-        xh[x_off[p]:x_off[p] + nx[p]] = np.concatenate([W.flatten('F') for W in f])
+    _random_starts(core_dims, Rs, x_off, xh)
     X0 = torch.from_numpy(xh).to(device=dev, dtype=dt)
     best = torch.empty_like(X0)
     ws_b = []
