@@ -37,6 +37,22 @@ size_t tfx_dgn_workspace_bytes(int dtype, int L, const int* dims, int R);
 int tfx_dgn_solve(int dtype, const tfx_dgn_problem* h_probs, tfx_dgn_problem* d_probs, int nprob,
                   const tfx_dgn_options* options, int cluster, void* stream);
 
+/* ---- alternating least squares ---------------------------------------------
+ * Alternating_Least_Squares.py:18 als(T, factors, R, options) -> (factors,
+ * step_sizes, errors, improv, gradients, stop), any order 2..12, rank <= 96.
+ * x: the start point (flat layout), overwritten with the LAST iterate (which
+ * the reference returns); best: the best iterate; stats: [4*maxiter] errors,
+ * step sizes, improvements, gradients; result: [4] stop code, iterations,
+ * status, pseudo-inverse fallbacks; info: [5] |T|, best error, 0, sum|T|, 0.
+ * options: maxiter, tol, tol_step, tol_improv, tol_grad, symm, factors_norm.
+ * The whole solve is one CUDA-graph launch on `stream` (a while-node repeats
+ * one iteration until the stop tests fire); work: tfx_als_workspace_bytes()
+ * bytes, 256-byte aligned. */
+size_t tfx_als_workspace_bytes(int dtype, int L, const int* dims, int R);
+int tfx_als_solve(int dtype, const void* T, int L, const int* dims, int R, void* x, void* best, double* stats,
+                  int* result, double* info, const tfx_dgn_options* options, void* work, size_t work_bytes,
+                  void* stream);
+
 /* ---- batches of small problems (the rank/stats sweeps, TensorFox.py:820-1039,
  * run cpd on many small tensors): one CTA per problem.
  * tfx_batch_mlsvd: Compression.py:141-156 (mlsvd 'seq') per problem, modes <= 64;

@@ -477,6 +477,121 @@ def dGN(T, factors, R, options, budgets=None, trace=None):
     return best_factors, step_sizes[:n], errors[:n], improv[:n], gradients[:n], stop
 
 
+def als_iteration(Tl, factors):
+    """One ALS sweep (Alternating_Least_Squares.py:204-235, general case): mode by
+    mode, ``W_l = T_(l) · pinv(KR_l^T)`` with the freshly updated factors."""
+    L = len(factors)
+    for l in range(L):
+        order = [m for m in reversed(range(L)) if m != l]
+        M = kr_chain([factors[m] for m in order])
+        factors[l] = Tl[l] @ np.linalg.pinv(M.T)
+    return factors
+
+
+def als(T, factors, R, options):
+    """Alternating least squares (Alternating_Least_Squares.py:18-201).
+
+    Returns ``(factors, step_sizes, errors, improv, gradients, stop)``; unlike
+    ``dGN`` the factors returned are the LAST iterate (the reference keeps a
+    best copy but does not return it)."""
+    o = options
+    maxiter = o.maxiter
+    tol, tol_step, tol_improv, tol_grad = o.tol, o.tol_step, o.tol_improv, o.tol_grad
+    L = len(factors)
+    factors = [np.array(W, dtype=np.float64) for W in factors]
+    Tsize = norm(T)
+    error = 1
+    stop = 5
+    const = 1 + int(maxiter / 10)
+    x = cpd2flat(factors)
+    step_sizes, errors = np.empty(maxiter), np.empty(maxiter)
+    improv, gradients = np.empty(maxiter), np.empty(maxiter)
+    Tl = [unfold(np.asarray(T, dtype=np.float64), l + 1) for l in range(L)]
+    it = 0
+    for it in range(maxiter):
+        old_x, old_error = x, error
+        factors = als_iteration(Tl, factors)
+        x = cpd2flat(factors)
+        factors = transform(factors, o.symm, o.factors_norm)
+        error = fastnorm(Tl[0], cpd2unfold1(factors)) / Tsize
+        step_sizes[it] = norm(x - old_x)
+        errors[it] = error
+        with np.errstate(divide='ignore', invalid='ignore'):
+            gradients[it] = np.abs(old_error - error) / step_sizes[it]
+        improv[it] = errors[it] if it == 0 else np.abs(errors[it - 1] - errors[it])
+        if it > 1:
+            if errors[it] < tol:
+                stop = 0
+                break
+            if step_sizes[it] < tol_step:
+                stop = 1
+                break
+            if improv[it] < tol_improv:
+                stop = 2
+                break
+            if gradients[it] < tol_grad:
+                stop = 3
+                break
+            if it > 2 * const and it % const == 0:
+                mean1 = np.mean(errors[it - 2 * const: it - const])
+                mean2 = np.mean(errors[it - const: it])
+                if mean1 - mean2 <= tol_improv:
+                    stop = 4
+                    break
+                mean3 = np.mean(improv[it - const: it])
+                if mean3 < 1e-3 * mean2:
+                    stop = 7
+                    break
+            if error > max(1, Tsize ** 2) / (1e-16 + tol):
+                stop = 6
+                break
+    n = it + 1
+    return factors, step_sizes[:n], errors[:n], improv[:n], gradients[:n], stop
+
+
+def rank_bounds(dims, method='dGN'):
+    """(Rmin, Rmax) of the rank search (TensorFox.py:863-873)."""
+    L = len(dims)
+    if L > 3:
+        if method == 'dGN':
+            return 1, int(np.prod(np.sort(np.array(dims))[1:]))
+        return 2, int(np.min(dims))
+    m, n, p = dims
+    return 1, int(min(m * n, m * p, n * p))
+
+
+def rank(best_error_of, dims, method='dGN'):
+    """The rank search of TensorFox.py:820-939 with the CPD replaced by
+    ``best_error_of(r)`` (the best relative error over the trials at rank r;
+    order > 3 at r = 1 counts as 1 without a CPD).  Returns
+    ``(final_rank, error_per_rank)``."""
+    L = len(dims)
+    Rmin, Rmax = rank_bounds(dims, method)
+    epr = np.empty(Rmax)
+    final_rank = None
+    r = 1
+    for r in range(1, Rmax + 1):
+        best_error = 1.0 if (L > 3 and r == 1) else best_error_of(r)
+        epr[r - 1] = best_error
+        if best_error < 1e-14:
+            final_rank = r
+            break
+        if r > Rmin and np.abs(epr[r - 1] - epr[r - 2]) < 1e-5 and best_error < 0.5:
+            final_rank = int(np.nanargmin(epr[0:r])) + 1
+            break
+        if r > 2:
+            prev = np.abs(epr[r - 2] - epr[r - 3])
+            cur = np.abs(epr[r - 1] - epr[r - 2])
+            with np.errstate(divide='ignore', invalid='ignore'):
+                if prev / cur > 100 and best_error < 0.5:
+                    final_rank = r - 1
+                    break
+    epr = epr[0:r]
+    if final_rank is None:
+        final_rank = int(np.nanargmin(epr)) + 1
+    return int(final_rank), epr
+
+
 # ----------------------------------------------------------------------------
 # compression (Compression.py)
 # ----------------------------------------------------------------------------
@@ -687,7 +802,7 @@ class Output:
 
 
 def cpd(T, R, options=None, timings=None):
-    """``cpd`` → ``tricpd`` for method 'dGN' (TensorFox.py:69-255, 424-655).
+    """``cpd`` → ``tricpd`` for methods 'dGN' and 'als' (TensorFox.py:69-255, 424-655).
 
     Returns ``(factors, output)`` where ``output`` carries num_steps, rel_error,
     accuracy, step_sizes, errors, improv, gradients and stop like the reference's.
@@ -721,12 +836,13 @@ def cpd(T, R, options=None, timings=None):
     S, U, T1, sigmas = mlsvd(Ts, Tsize, R, o)
     _mark('mlsvd')
     init = starting_point(S, U, R, ordering, o)
-    factors, ss, er, im, gr, st = dGN(S, init, R, o)
+    solver = als if o.method == 'als' else dGN
+    factors, ss, er, im, gr, st = solver(S, init, R, o)
     _mark('dgn')
     factors = [U[l] @ factors[l] for l in range(len(factors))]
     refine = o.refine and not sparse_in
     if refine:
-        factors, ss2, er2, im2, gr2, st2 = dGN(Ts, factors, R, o)
+        factors, ss2, er2, im2, gr2, st2 = solver(Ts, factors, R, o)
     else:
         ss2, er2, im2, gr2, st2 = np.array([0]), np.array([0]), np.array([0]), np.array([0]), 8
     out = Output()

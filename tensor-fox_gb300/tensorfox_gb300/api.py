@@ -150,14 +150,24 @@ def _decompress(Uts, best_flat, core_dims, R):
     return torch.cat(outs)
 
 
+def _run_als(Td, x0, R, options, prec):
+    from .als import als_device, split_stats
+    x, best, stats, res, info = als_device(Td, x0, R, options, prec)
+    n = int(res[1])
+    ss, er, im, gr = split_stats(stats, int(options.maxiter), n)
+    return (x, ss, er, im, gr, int(res[0]))
+
+
 def tricpd(T, R, options):
-    """Compression, starting point, dGN, decompression, refinement, final error."""
+    """Compression, starting point, dGN or ALS, decompression, refinement, final
+    error (TensorFox.py:424-655)."""
     o = options
     if isinstance(T, list):
         from .sparse import tricpd_sparse
         return tricpd_sparse(T, R, o)
-    if o.method != 'dGN':
-        raise NotImplementedError("method %r is outside the damped Gauss-Newton path" % (o.method,))
+    if o.method not in ('dGN', 'als'):
+        raise NotImplementedError("method %r is outside the damped Gauss-Newton and ALS paths" % (o.method,))
+    solve = _run_als if o.method == 'als' else _run_dgn
     prec = _precision(T, o)
     dt = _dev.torch_dtype(prec)
     shape = tuple(int(d) for d in T.shape)
@@ -186,10 +196,10 @@ def tricpd(T, R, options):
     else:
         raise NotImplementedError("initialization %r is outside the dGN path" % (o.initialization,))
     x0 = _flat_dev(init, dt, Td.device)
-    best, ss, er, im, gr, st = _run_dgn(S, x0, R, o, prec)
+    best, ss, er, im, gr, st = solve(S, x0, R, o, prec)
     Wf = _decompress(Uts, best, core, R)
     if o.refine:
-        Wf, ss2, er2, im2, gr2, st2 = _run_dgn(Td, Wf, R, o, prec)
+        Wf, ss2, er2, im2, gr2, st2 = solve(Td, Wf, R, o, prec)
     else:
         ss2, er2, im2, gr2, st2 = np.array([0]), np.array([0]), np.array([0]), np.array([0]), 8
     if o.refine:
@@ -212,7 +222,7 @@ def tricpd(T, R, options):
 
 
 def cpd(T, R, options=False):
-    """Drop-in for TensorFox.cpd (TensorFox.py:69-255), method 'dGN'."""
+    """Drop-in for TensorFox.cpd (TensorFox.py:69-255), methods 'dGN' and 'als'."""
     _dev.require_cuda()
     if isinstance(T, list):
         dims_orig = T[2]

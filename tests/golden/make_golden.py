@@ -3,8 +3,9 @@
 Run from the repository root, in a container where the reference source tree is
 mounted (see ``ref_harness.py``):
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py [case ...]
 
+With case names, only those fixtures are regenerated (see ``CASES``).
 Each ``.npz`` holds seeded inputs and the reference's outputs for one case.  The
 fixtures are small (a few hundred KB in total) and committed; tests compare both
 the oracle (``oracle/tfx_oracle.py``) and the CUDA path against them.
@@ -26,6 +27,7 @@ import TensorFox.Conversion as cnv  # noqa: E402
 import TensorFox.Critical as crt  # noqa: E402
 import TensorFox.Compression as cmpr  # noqa: E402
 import TensorFox.MultilinearAlgebra as mla  # noqa: E402
+import TensorFox.Alternating_Least_Squares as alsm  # noqa: E402
 
 
 def save(name, **arrays):
@@ -212,29 +214,116 @@ def reference_tests_case(name):
          ones_init_errors=out_ones.errors[0])
 
 
-def main():
-    with contextlib.redirect_stdout(io.StringIO()):
-        pass
-    units("units_L3", [7, 5, 4], 3, 1)
-    units("units_L4", [5, 4, 3, 3], 2, 2)
-    units("units_L3_big", [12, 10, 9], 4, 3, damp=0.2, cg_iters=9)
-    units("units_L5", [4, 3, 3, 2, 2], 3, 4)
-    kr_case("kr_unfold", 5)
-    dogleg_units("dogleg_units", 6)
-    dgn_case("dgn_static_L3", [9, 8, 7], 3, 11, inner_method='cg_static', cg_maxiter=8, maxiter=40)
-    dgn_case("dgn_cg_L3", [12, 10, 9], 4, 12, maxiter=60)
-    dgn_case("dgn_cg_L4", [6, 5, 5, 4], 3, 13, maxiter=50)
-    dgn_case("dgn_dogleg_L3", [8, 7, 6], 3, 14, noise=0.2, tol_jump=0.99, maxiter=30)
-    dgn_case("dgn_small_L3", [4, 4, 3], 2, 15, maxiter=80)
-    mlsvd_case("mlsvd_seq", [20, 15, 12], 4, 21)
-    mlsvd_case("mlsvd_classic", [18, 14, 11], 3, 22, method='classic')
-    mlsvd_case("mlsvd_seq_L4", [10, 9, 8, 7], 3, 23)
-    cpd_case("cpd_c1_small", [30, 25, 20], 5, 31, 1e-6)
-    cpd_case("cpd_L4", [12, 11, 10, 9], 3, 32, 1e-4)
-    cpd_case("cpd_refine", [15, 12, 10], 4, 33, 1e-3, refine=True)
-    sparse_case("sparse_L3", [10, 9, 8], 3, 60, 41)
-    reference_tests_case("ref_tests_2x2x2")
+def als_case(name, dims, R, seed, noise=1e-3, spread=0.3, **opts):
+    """ALS trajectory (Alternating_Least_Squares.py:18-201) from an explicit start."""
+    T, W = planted(dims, R, noise, seed)
+    rng = np.random.default_rng(seed + 1000)
+    init = [w + spread * rng.standard_normal(w.shape) for w in W]
+    o = Opt()
+    for k, v in opts.items():
+        setattr(o, k, v)
+    o = tfx.make_options(o)
+    f, ss, er, im, gr, st = alsm.als(T, [w.copy() for w in init], R, o)
+    save(name, T=T, init_x=np.concatenate([w.flatten('F') for w in init]), R=R, seed=seed,
+         dims=np.array(dims), final_x=np.concatenate([w.flatten('F') for w in f]),
+         step_sizes=ss, errors=er, improv=im, gradients=gr, stop=st,
+         opt_names=np.array(list(opts.keys())), opt_values=np.array([repr(v) for v in opts.values()]))
+
+
+def rank_case(name, dims, tables, trials=3):
+    """TensorFox.py:820-939 rank(): the stopping rules, with cpd replaced by a table
+    of relative errors per (rank, trial) so that only the driver logic runs."""
+    L = len(dims)
+    out_ranks, out_err, lens, flat = [], [], [], []
+    for table in tables:
+        calls = []
+
+        def fake_cpd(T, r, options=False, _t=table, _c=calls):
+            _c.append(r)
+            k = sum(1 for x in _c if x == r) - 1
+
+            class Out:
+                pass
+            o = Out()
+            o.rel_error = float(_t[r - 1][k])
+            return None, o
+        mod = sys.modules["TensorFox.TensorFox"]
+        real = mod.cpd
+        mod.cpd = fake_cpd
+        try:
+            with contextlib.redirect_stdout(io.StringIO()):
+                fr, epr = mod.rank(np.zeros(dims), plot=False, trials=trials)
+        finally:
+            mod.cpd = real
+        out_ranks.append(fr)
+        out_err.append(np.asarray(epr))
+        lens.append(len(table))
+        flat.append(np.asarray(table, dtype=np.float64).ravel())
+    save(name, dims=np.array(dims), trials=trials, table_lens=np.array(lens), tables=np.concatenate(flat),
+         final_rank=np.array(out_ranks), error_lens=np.array([len(e) for e in out_err]),
+         errors=np.concatenate(out_err))
+
+
+def rank_tables(L, n, trials, seed):
+    """Seeded per-(rank, trial) error tables that exercise every stopping rule."""
+    rng = np.random.default_rng(seed)
+    tabs = []
+    # error flattens (|e_r - e_{r-1}| < 1e-5, e < 0.5) after the true rank 4
+    e = [0.9, 0.6, 0.3, 0.01, 0.01 - 4e-6, 0.01 - 5e-6]
+    tabs.append([[x * (1 + 0.5 * t) for t in range(trials)] for x in e] + [[1.0] * trials] * (n - len(e)))
+    # exact fit at rank 3 (error < 1e-14)
+    e = [0.5, 0.2, 1e-15]
+    tabs.append([[x, x * 2, x * 3] [:trials] for x in e] + [[1.0] * trials] * (n - len(e)))
+    # abrupt drop: previous difference / current difference > 100
+    e = [0.8, 0.4, 0.39, 1e-3, 1e-3 - 1e-6, 1e-3 - 2e-6]
+    tabs.append([[x] * trials for x in e] + [[1.0] * trials] * (n - len(e)))
+    # no rule fires: runs to Rmax, final rank = argmin
+    e = list(np.sort(rng.uniform(0.6, 0.9, n))[::-1] + np.arange(n) * 1e-3)
+    tabs.append([[x + 1e-3 * t for t in range(trials)] for x in e])
+    # the flat-error rule with error >= 0.5 does not fire
+    e = [0.9, 0.7, 0.7 - 1e-6, 0.3, 0.05, 0.05 - 1e-6]
+    tabs.append([[x] * trials for x in e] + [[1.0] * trials] * (n - len(e)))
+    return tabs
+
+
+CASES = {
+    "units_L3": lambda: units("units_L3", [7, 5, 4], 3, 1),
+    "units_L4": lambda: units("units_L4", [5, 4, 3, 3], 2, 2),
+    "units_L3_big": lambda: units("units_L3_big", [12, 10, 9], 4, 3, damp=0.2, cg_iters=9),
+    "units_L5": lambda: units("units_L5", [4, 3, 3, 2, 2], 3, 4),
+    "kr_unfold": lambda: kr_case("kr_unfold", 5),
+    "dogleg_units": lambda: dogleg_units("dogleg_units", 6),
+    "dgn_static_L3": lambda: dgn_case("dgn_static_L3", [9, 8, 7], 3, 11, inner_method='cg_static', cg_maxiter=8,
+                                      maxiter=40),
+    "dgn_cg_L3": lambda: dgn_case("dgn_cg_L3", [12, 10, 9], 4, 12, maxiter=60),
+    "dgn_cg_L4": lambda: dgn_case("dgn_cg_L4", [6, 5, 5, 4], 3, 13, maxiter=50),
+    "dgn_dogleg_L3": lambda: dgn_case("dgn_dogleg_L3", [8, 7, 6], 3, 14, noise=0.2, tol_jump=0.99, maxiter=30),
+    "dgn_small_L3": lambda: dgn_case("dgn_small_L3", [4, 4, 3], 2, 15, maxiter=80),
+    "mlsvd_seq": lambda: mlsvd_case("mlsvd_seq", [20, 15, 12], 4, 21),
+    "mlsvd_classic": lambda: mlsvd_case("mlsvd_classic", [18, 14, 11], 3, 22, method='classic'),
+    "mlsvd_seq_L4": lambda: mlsvd_case("mlsvd_seq_L4", [10, 9, 8, 7], 3, 23),
+    "cpd_c1_small": lambda: cpd_case("cpd_c1_small", [30, 25, 20], 5, 31, 1e-6),
+    "cpd_L4": lambda: cpd_case("cpd_L4", [12, 11, 10, 9], 3, 32, 1e-4),
+    "cpd_refine": lambda: cpd_case("cpd_refine", [15, 12, 10], 4, 33, 1e-3, refine=True),
+    "sparse_L3": lambda: sparse_case("sparse_L3", [10, 9, 8], 3, 60, 41),
+    "ref_tests_2x2x2": lambda: reference_tests_case("ref_tests_2x2x2"),
+    "als_L3": lambda: als_case("als_L3", [12, 10, 9], 4, 51, maxiter=60),
+    "als_L4": lambda: als_case("als_L4", [7, 6, 5, 4], 3, 52, maxiter=80),
+    "als_stall_L3": lambda: als_case("als_stall_L3", [9, 8, 7], 5, 53, noise=0.3, spread=1.0, maxiter=120),
+    "als_symm_L3": lambda: als_case("als_symm_L3", [6, 6, 6], 3, 54, noise=1e-2, maxiter=30, symm=True),
+    "als_norm_L3": lambda: als_case("als_norm_L3", [8, 7, 6], 3, 55, maxiter=30, factors_norm=2.0),
+    "cpd_als": lambda: cpd_case("cpd_als", [20, 16, 12], 4, 56, 1e-5, method='als'),
+    "cpd_als_refine": lambda: cpd_case("cpd_als_refine", [14, 12, 10], 3, 57, 1e-4, method='als', refine=True,
+                                       maxiter=100),
+    "rank_rules_L3": lambda: rank_case("rank_rules_L3", [4, 3, 3], rank_tables(3, 9, 3, 58)),
+    "rank_rules_L4": lambda: rank_case("rank_rules_L4", [3, 3, 2, 2], rank_tables(4, 18, 2, 59), trials=2),
+}
+
+
+def main(names=None):
+    for name in (names or list(CASES)):
+        CASES[name]()
 
 
 if __name__ == "__main__":
-    main()
+    main(sys.argv[1:])

@@ -168,3 +168,54 @@ def test_reference_doctest_tensor():
     _, out = orc.cpd(g["T"], 3, o)
     np.testing.assert_allclose(out.rel_error, float(g["ones_init_error"]), rtol=1e-8)
     assert out.rel_error < 0.14
+
+
+ALS_CASES = ["als_L3", "als_L4", "als_stall_L3", "als_symm_L3", "als_norm_L3"]
+
+
+@pytest.mark.parametrize("name", ALS_CASES)
+def test_als_trajectory_matches_reference(name):
+    g = load_golden(name)
+    dims, R = [int(d) for d in g["dims"]], int(g["R"])
+    f, ss, er, im, gr, st = orc.als(g["T"], split_x(g["init_x"], dims, R), R, _opts(g))
+    assert st == int(g["stop"])
+    assert len(er) == len(g["errors"])
+    np.testing.assert_allclose(er, g["errors"], rtol=1e-9, atol=1e-14)
+    np.testing.assert_allclose(ss, g["step_sizes"], rtol=1e-9, atol=1e-14)
+    np.testing.assert_allclose(im, g["improv"], rtol=1e-6, atol=1e-14)
+    np.testing.assert_allclose(orc.cpd2flat(f), g["final_x"], rtol=1e-8, atol=1e-10)
+
+
+@pytest.mark.parametrize("name", ["cpd_als", "cpd_als_refine"])
+def test_cpd_als_matches_reference(name):
+    g = load_golden(name)
+    o = _opts(g)
+    np.random.seed(int(g["seed"]))
+    f, out = orc.cpd(g["T"], int(g["R"]), o)
+    assert out.num_steps == int(g["num_steps"])
+    assert list(out.stop) == list(g["stop"])
+    np.testing.assert_allclose(out.rel_error, float(g["rel_error"]), rtol=1e-6)
+    np.testing.assert_allclose(np.concatenate([w.flatten('F') for w in f]), g["factors"], rtol=1e-6, atol=1e-8)
+
+
+def rank_tables(g):
+    """The per-(rank, trial) error tables of a rank fixture."""
+    t = int(g["trials"])
+    out, s = [], 0
+    for n in g["table_lens"]:
+        out.append(g["tables"][s:s + n * t].reshape(n, t))
+        s += n * t
+    return out
+
+
+@pytest.mark.parametrize("name", ["rank_rules_L3", "rank_rules_L4"])
+def test_rank_rules_match_reference(name):
+    g = load_golden(name)
+    dims = [int(d) for d in g["dims"]]
+    s = 0
+    for k, tab in enumerate(rank_tables(g)):
+        fr, epr = orc.rank(lambda r: float(np.min(tab[r - 1])), dims)
+        n = int(g["error_lens"][k])
+        assert fr == int(g["final_rank"][k])
+        np.testing.assert_array_equal(epr, g["errors"][s:s + n])
+        s += n
