@@ -135,6 +135,12 @@ int tfx_mttkrp(int dtype, const void* T, int L, const int* dims, int R, const vo
 int tfx_cp_full(int dtype, int L, const int* dims, int R, const void* W, void* out, void* stream);
 size_t tfx_cp_wp1_scratch_bytes(int L, int R);
 int tfx_cp_wp1(int dtype, int L, const int* dims, int R, const void* W, void* out, void* scratch, void* stream);
+/* Backward of the fit loss ||T - [[W]]||^2 in one call: grad (flat layout) =
+ * 2 (W_l P1_l - T_(l) KR_l) for every mode, twice the gradient g of
+ * GaussNewton.py:401-427 (compute_grad). */
+size_t tfx_cp_fit_grad_scratch_bytes(int dtype, int L, const int* dims, int R);
+int tfx_cp_fit_grad(int dtype, const void* T, int L, const int* dims, int R, const void* W, void* grad, void* scratch,
+                    size_t scratch_bytes, void* stream);
 
 /* ---- sparse (COO) ----------------------------------------------------------
  * TensorFox.py:476-481: int64 (nnz x L) coordinates -> int32 L x nnz; *err = 1

@@ -9,7 +9,8 @@
 //   W_l = MTTKRP_l H_l^+,
 // and the only contraction with the tensor is the MTTKRP (tfx_mttkrp).  H_l^+
 // comes from the symmetric sweep operator (Gauss-Jordan elimination on an SPD
-// matrix, FP64, shared memory); when a pivot falls below 1e-12 of its diagonal
+// matrix, in shared memory; FP32 on the FP32 path, FP64 otherwise or when the
+// FP32 pivots degrade); when an FP64 pivot falls below 1e-12 of its diagonal
 // (H_l numerically singular) the solve switches to a Jacobi eigen-decomposition
 // and inverts the eigenvalues above 1e-13 of the largest (a pseudo-inverse).
 //
@@ -19,8 +20,9 @@
 // clears the loop condition with cudaGraphSetConditional.  No host round trip
 // per iteration; the loop always ends after maxiter iterations at the latest.
 //
-// Precision: factors and the MTTKRP in the working type; Gramians, H_l, its
-// inverse, the step size, the residual and every control scalar in FP64.
+// Precision: factors, the MTTKRP and H_l^+ in the working type (H_l^+ from an
+// FP64 sweep whenever the FP32 one loses its pivots); Gramians, H_l, the step
+// size, the residual and every control scalar in FP64.
 #include <math.h>
 #include <stdint.h>
 
@@ -131,12 +133,50 @@ __global__ void k_als_gram_sum(const double* __restrict__ gpart, int nblk, int R
 }
 
 // ---------------------------------------------------------------------------
-// H_l^+ for H_l = o_{m != l} G_m (one CTA).  Sweep operator: after sweeping
+// Sweep operator on A (R x R inside an m x m row-major buffer): after sweeping
 // pivot k, A[k][k] = -1/p, A[i][k] = A[k][i] = A[i][k]/p and
-// A[i][j] -= A[i][k] A[k][j] / p; after all pivots A = -H^{-1}.  A pivot below
-// 1e-12 of H's own diagonal entry marks H numerically singular: the kernel then
-// recomputes H and forms the pseudo-inverse from a Jacobi eigen-decomposition.
-// Output: Hinv (R x R, row-major) in the working type.
+// A[i][j] -= A[i][k] A[k][j] / p; after all pivots A = -H^{-1}.  Returns false
+// (uniformly across the CTA) when a pivot is not above thr times H's own
+// diagonal entry piv[k].
+// ---------------------------------------------------------------------------
+template <class C>
+__device__ bool sweep_inverse(C* A, int m, int R, const double* piv, C* cs, volatile int* fail, double thr) {
+  const int tid = threadIdx.x, RR = R * R;
+  if (tid == 0) *fail = 0;
+  __syncthreads();
+  for (int k = 0; k < R; ++k) {
+    const C p = A[k * m + k];
+    if (!((double)p > thr * piv[k])) {
+      if (tid == 0) *fail = 1;
+      break;
+    }
+    for (int i = tid; i < R; i += NT) cs[i] = A[i * m + k];
+    __syncthreads();
+    const C ip = C(1) / p;
+    for (int e = tid; e < RR; e += NT) {
+      const int i = e / R, j = e - i * R;
+      const C aik = cs[i], akj = cs[j];
+      C v;
+      if (i == k && j == k) v = -ip;
+      else if (i == k) v = akj * ip;
+      else if (j == k) v = aik * ip;
+      else v = A[i * m + j] - aik * akj * ip;
+      A[i * m + j] = v;
+    }
+    __syncthreads();
+  }
+  __syncthreads();
+  return *fail == 0;
+}
+
+// ---------------------------------------------------------------------------
+// H_l^+ for H_l = o_{m != l} G_m (one CTA), written as Hinv (R x R) in the
+// working type.  FP32 path: the sweep runs in FP32 (the factor update it feeds
+// is FP32; an update off by a relative e moves the ALS objective by O(e^2)),
+// with a pivot floor of 1e-4 of the diagonal; FP64 path, or when that floor is
+// crossed: the sweep in FP64 with a floor of 1e-12.  Below that H is singular
+// to working accuracy and the pseudo-inverse comes from a Jacobi
+// eigen-decomposition (eigenvalues above 1e-13 of the largest inverted).
 // ---------------------------------------------------------------------------
 template <class T>
 __global__ void __launch_bounds__(NT) k_als_inv(const double* __restrict__ G, int L, int l, int R, T* __restrict__ Hinv,
@@ -144,13 +184,14 @@ __global__ void __launch_bounds__(NT) k_als_inv(const double* __restrict__ G, in
   extern __shared__ __align__(16) char smem[];
   const int m = (R + 1) & ~1;
   double* A = (double*)smem;          // m x m
-  double* V = A + (size_t)m * m;      // m x m (eigenvectors in the fallback)
+  double* V = A + (size_t)m * m;      // m x m (FP32 sweep, then eigenvectors in the fallback)
   double* cs = V + (size_t)m * m;     // m values
   int* pr = (int*)(cs + m);           // m + 2 ints
   double* red = (double*)(pr + m + 2);  // 4 doubles
-  double* piv = red + 4;              // R pivots' reference diagonals
+  double* piv = red + 4;              // H's diagonal
   const int tid = threadIdx.x;
   const int RR = R * R;
+  volatile int* fail = (volatile int*)(red + 2);
   auto h_entry = [&](int a, int b) {
     double p = 1.0;
     for (int k = 0; k < L; ++k)
@@ -163,43 +204,28 @@ __global__ void __launch_bounds__(NT) k_als_inv(const double* __restrict__ G, in
   }
   __syncthreads();
   for (int k = tid; k < R; k += NT) piv[k] = A[k * m + k];
-  volatile int* fail = (volatile int*)red;
-  if (tid == 0) *fail = 0;
   __syncthreads();
-  for (int k = 0; k < R; ++k) {
-    const double p = A[k * m + k];
-    // every thread reads the same pivot; the test is uniform across the CTA
-    if (!(p > 1e-12 * piv[k])) {
-      if (tid == 0) *fail = 1;
-      break;
-    }
-    // stash column k (= row k) before the update overwrites it
-    for (int i = tid; i < R; i += NT) cs[i] = A[i * m + k];
+  if (sizeof(T) == 4) {
+    float* A32 = (float*)V;
+    for (int e = tid; e < m * m; e += NT) A32[e] = (float)A[e];
     __syncthreads();
-    const double ip = 1.0 / p;
-    for (int e = tid; e < RR; e += NT) {
-      const int i = e / R, j = e - i * R;
-      const double aik = cs[i], akj = cs[j];
-      double v;
-      if (i == k && j == k) v = -ip;
-      else if (i == k) v = akj * ip;
-      else if (j == k) v = aik * ip;
-      else v = A[i * m + j] - aik * akj * ip;
-      A[i * m + j] = v;
+    if (sweep_inverse<float>(A32, m, R, piv, (float*)cs, fail, 1e-4)) {
+      for (int e = tid; e < RR; e += NT) {
+        const int i = e / R, j = e - i * R;
+        Hinv[e] = (T)(-A32[i * m + j]);
+      }
+      return;
     }
-    __syncthreads();
   }
-  __syncthreads();
-  if (!*fail) {
+  if (sweep_inverse<double>(A, m, R, piv, cs, fail, 1e-12)) {
     for (int e = tid; e < RR; e += NT) {
       const int i = e / R, j = e - i * R;
       Hinv[e] = (T)(-A[i * m + j]);
     }
     return;
   }
-  // pseudo-inverse from the eigen-decomposition of H (rare: H singular to
-  // working accuracy)
-  __syncthreads();
+  // pseudo-inverse from the eigen-decomposition of H (H singular to working
+  // accuracy)
   for (int e = tid; e < m * m; e += NT) {
     const int a = e / m, b = e - a * m;
     A[e] = (a < R && b < R) ? h_entry(a, b) : 0.0;

@@ -38,7 +38,13 @@ def _flat(factors):
     return torch.cat([W.detach().t().contiguous().reshape(-1) for W in factors])
 
 
+_DECLARED = None
+
+
 def _declare():
+    global _DECLARED
+    if _DECLARED is not None:
+        return _DECLARED
     lib = _lib.load()
     P, I, SZ = ctypes.c_void_p, ctypes.c_int, ctypes.c_size_t
     lib.tfx_mttkrp.argtypes = [I, P, I, ctypes.POINTER(ctypes.c_int), I, P, I, P, P, SZ, P]
@@ -48,6 +54,10 @@ def _declare():
     lib.tfx_cp_wp1.argtypes = [I, I, ctypes.POINTER(ctypes.c_int), I, P, P, P, P]
     lib.tfx_cp_wp1_scratch_bytes.restype = SZ
     lib.tfx_cp_wp1_scratch_bytes.argtypes = [I, I]
+    lib.tfx_cp_fit_grad.argtypes = [I, P, I, ctypes.POINTER(ctypes.c_int), I, P, P, P, SZ, P]
+    lib.tfx_cp_fit_grad_scratch_bytes.restype = SZ
+    lib.tfx_cp_fit_grad_scratch_bytes.argtypes = [I, I, ctypes.POINTER(ctypes.c_int), I]
+    _DECLARED = lib
     return lib
 
 
@@ -104,25 +114,41 @@ class CPReconstruct(torch.autograd.Function):
         return tuple(mttkrp(G, factors, l) if ctx.needs_input_grad[l] else None for l in range(len(factors)))
 
 
+def fit_grad(T, W_flat, dims, R):
+    """Flat gradient of ||T - [[W]]||^2: 2 (W_l P1_l - MTTKRP(T, l)) per mode
+    (one ``tfx_cp_fit_grad`` call)."""
+    lib = _declare()
+    cd = _cint(dims)
+    nb = int(lib.tfx_cp_fit_grad_scratch_bytes(_dt(T), len(dims), cd, R))
+    scratch = torch.empty(nb, dtype=torch.uint8, device=T.device)
+    out = torch.empty_like(W_flat)
+    _lib.check(lib.tfx_cp_fit_grad(_dt(T), _vp(T), len(dims), cd, R, _vp(W_flat), _vp(out), _vp(scratch), nb, _st()))
+    return out
+
+
 class CPFitLoss(torch.autograd.Function):
     @staticmethod
     def forward(ctx, T, *factors):
         from .kernels import cp_residual_sq
         T = T.contiguous()
-        ctx.save_for_backward(T, *factors)
         R = int(factors[0].shape[1])
-        return cp_residual_sq(T, list(T.shape), _flat(factors).to(T.dtype), R)[0].to(T.dtype)
+        W_flat = _flat(factors).to(T.dtype)
+        ctx.save_for_backward(T, W_flat, *factors)
+        return cp_residual_sq(T, list(T.shape), W_flat, R)[0].to(T.dtype)
 
     @staticmethod
     def backward(ctx, gl):
-        T, *factors = ctx.saved_tensors
-        wp1 = _wp1(factors)
-        grads = []
-        for l in range(len(factors)):
-            if ctx.needs_input_grad[l + 1]:
-                grads.append(2.0 * gl * (wp1[l] - mttkrp(T, factors, l)))
-            else:
-                grads.append(None)
+        T, W_flat, *factors = ctx.saved_tensors
+        dims = [int(W.shape[0]) for W in factors]
+        R = int(factors[0].shape[1])
+        grads = [None] * len(factors)
+        if any(ctx.needs_input_grad[1:]):
+            g = fit_grad(T, W_flat, dims, R).mul_(gl.to(T.dtype))
+            s = 0
+            for l, d in enumerate(dims):
+                if ctx.needs_input_grad[l + 1]:
+                    grads[l] = g[s:s + d * R].view(R, d).t().to(factors[l].dtype)
+                s += d * R
         gT = 2.0 * gl * (T - cp_full(factors)) if ctx.needs_input_grad[0] else None
         return (gT, *grads)
 

@@ -68,7 +68,7 @@ def _cluster_candidates(c, R):
 class _Batch:
     """Device buffers for a set of dGN problems solved in one engine launch."""
 
-    def __init__(self, tensors, xs, R_list, options, precision):
+    def __init__(self, tensors, xs, R_list, options, precision, budgets=None):
         self.precision = precision
         dt = _dev.torch_dtype(precision)
         self.es = 8 if precision == "fp64" else 4
@@ -87,7 +87,11 @@ class _Batch:
             dims_c = (ctypes.c_int * L)(*t.shape)
             nb = lib.tfx_dgn_workspace_bytes(_dev.lib_dtype(precision), L, dims_c, int(R))
             self.ws.append(torch.empty(int(nb), dtype=torch.uint8, device=t.device))
-        self.budgets = [torch.from_numpy(cg_budgets(options, t.dim())).to(t.device) for t in tensors]
+        if budgets is None:
+            self.budgets = [torch.from_numpy(cg_budgets(options, t.dim())).to(t.device) for t in tensors]
+        else:   # per-problem caps drawn by the caller (maxiter ints each)
+            self.budgets = [torch.from_numpy(np.ascontiguousarray(b, dtype=np.int32)).to(t.device)
+                            for b, t in zip(budgets, tensors)]
         sched = options.init_damp if isinstance(options.init_damp, list) else None
         self.sched = None
         if sched is not None:

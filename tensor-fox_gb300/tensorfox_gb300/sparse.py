@@ -161,10 +161,10 @@ def mlsvd_sparse_device(X, R, options):
 
 def tricpd_sparse(T, R, options):
     """``tricpd`` for ``[data, idxs, dims]`` (TensorFox.py:424-655, sparse branches)."""
-    from .api import Output, starting_point_random, _decompress, _run_dgn, unsort_dims
+    from .api import Output, starting_point_random, _decompress, _run_dgn, _run_als, unsort_dims
     o = options
-    if o.method != 'dGN':
-        raise NotImplementedError("method %r is outside the damped Gauss-Newton path" % (o.method,))
+    if o.method not in ('dGN', 'als'):
+        raise NotImplementedError("method %r is outside the damped Gauss-Newton and ALS paths" % (o.method,))
     data, idxs, dims = T
     data = np.asarray(data, dtype=np.float64)
     idxs = np.asarray(idxs, dtype=np.int64).reshape(len(data), -1)
@@ -185,7 +185,7 @@ def tricpd_sparse(T, R, options):
     else:
         init = starting_point_random(core, R, o)
     x0 = torch.from_numpy(_dev.flat_factors(init)).to(device=S.device, dtype=dt)
-    best, ss, er, im, gr, st = _run_dgn(S, x0, R, o, prec)
+    best, ss, er, im, gr, st = (_run_als if o.method == 'als' else _run_dgn)(S, x0, R, o, prec)
     Wf = _decompress(Uts, best, core, R)
     factors = _dev.unflat(Wf.double().cpu().numpy(), [int(d) for d in sdims], R)
     # final error on the stored entries (Auxiliar.py:155-159), sorted order
