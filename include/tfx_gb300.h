@@ -66,6 +66,12 @@ int tfx_batch_decompress(int dtype, const tfx_batch_problem* d_probs, int nprob,
                          void* const* wfull_dev, void* stream);
 int tfx_batch_residual(int dtype, const tfx_batch_problem* d_probs, int nprob, void* const* wfull_dev, double* out2,
                        void* stream);
+/* Auxiliar.py:93-115 sort_dims for a whole batch on the device: problem p's
+ * tensor (h_probs[p].tensor, dims = the sorted dims) is filled from src_dev[p],
+ * the caller's C-order tensor; perm_dev[p*L + l] is the caller's axis that
+ * becomes sorted mode l. */
+int tfx_batch_permute(int dtype, const tfx_batch_problem* h_probs, tfx_batch_problem* d_probs, int nprob,
+                      const void* const* src_dev, const int* perm_dev, void* stream);
 
 /* ---- compression (MLSVD) --------------------------------------------------
  * Compression.py:192-237 compute_svd / 400-518 randomized_svd: the unfolding's

@@ -86,6 +86,9 @@ typedef struct tfx_dgn_options {
   int use_damp_sched; /* 1: damp_sched holds init_damp as a list */
   int symm;           /* options.symm */
   double factors_norm; /* options.factors_norm (0 = off) */
+  int tile;           /* engine register tile of the small contractions: 1, 2 or 4
+                         (16*tile rows and columns per CTA tile); 0 = chosen from
+                         the largest dimension or rank of the batch */
 } tfx_dgn_options;
 
 #ifdef __cplusplus

@@ -8,6 +8,8 @@
 //                        clean_compression truncation and the mode product.
 //   tfx_batch_decompress factors_l = U_l W_l per problem (TensorFox.py:573-574)
 //   tfx_batch_residual   ||T - [[W]]||^2 and ||T||^2 per problem (Auxiliar.py:131-151)
+//   tfx_batch_permute    per problem, the caller's tensor with its modes put in
+//                        decreasing size (Auxiliar.py:93-115 sort_dims) on the device
 //
 // Problems are described by tfx_batch_problem (include/tfx_gb300_types.h).
 #include <math.h>
@@ -309,6 +311,65 @@ extern "C" int tfx_batch_mlsvd(int dtype, const tfx_batch_problem* h_probs, tfx_
   }
   e = cudaGetLastError();
   if (e != cudaSuccess) return tfx_set_cuda_error(e, "batch_mlsvd");
+  tfx_count_launch(1);
+  return TFX_STATUS_OK;
+}
+
+// One CTA per problem: dst (the problem's tensor, C-order over the sorted dims)
+// gathers from src[p] (C-order over the caller's dims); perm[p*L + l] is the
+// caller's axis that became sorted mode l.  Writes are coalesced; the strided
+// reads stay within one small tensor (L2-resident).
+template <class T>
+__global__ void __launch_bounds__(256) k_batch_permute(const tfx_batch_problem* __restrict__ probs, int nprob,
+                                                       const T* const* __restrict__ src, const int* __restrict__ perm) {
+  const int p = blockIdx.x;
+  if (p >= nprob) return;
+  const tfx_batch_problem& q = probs[p];
+  const int L = q.L;
+  long long sstride[TFX_MAX_ORDER];   // caller's stride of sorted mode l
+  long long ostr[TFX_MAX_ORDER];      // caller's C-order strides
+  int odim[TFX_MAX_ORDER];
+  for (int l = 0; l < L; ++l) {
+    const int a = perm[p * L + l];
+    if (a < 0 || a >= L) return;  // not a permutation of 0..L-1: leave the problem untouched
+    odim[a] = q.dims[l];
+  }
+  long long s = 1;
+  for (int a = L - 1; a >= 0; --a) {
+    ostr[a] = s;
+    s *= odim[a];
+  }
+  long long N = 1;
+  for (int l = 0; l < L; ++l) {
+    sstride[l] = ostr[perm[p * L + l]];
+    N *= q.dims[l];
+  }
+  const T* in = src[p];
+  T* out = (T*)q.tensor;
+  for (long long e = threadIdx.x; e < N; e += blockDim.x) {
+    long long r = e, off = 0;
+    for (int l = L - 1; l >= 0; --l) {
+      const long long i = r % q.dims[l];
+      r /= q.dims[l];
+      off += i * sstride[l];
+    }
+    out[e] = in[off];
+  }
+}
+
+extern "C" int tfx_batch_permute(int dtype, const tfx_batch_problem* h_probs, tfx_batch_problem* d_probs, int nprob,
+                                 const void* const* src_dev, const int* perm_dev, void* stream) {
+  if (int s = batch_check(h_probs, nprob)) return s;
+  if (!d_probs || !src_dev || !perm_dev) return tfx_set_error(TFX_STATUS_ERR_ARG, "batch_permute");
+  cudaStream_t st = (cudaStream_t)stream;
+  cudaError_t e = cudaMemcpyAsync(d_probs, h_probs, sizeof(tfx_batch_problem) * nprob, cudaMemcpyHostToDevice, st);
+  if (e != cudaSuccess) return tfx_set_cuda_error(e, "batch descriptors");
+  if (dtype == TFX_F32)
+    k_batch_permute<float><<<nprob, 256, 0, st>>>(d_probs, nprob, (const float* const*)src_dev, perm_dev);
+  else
+    k_batch_permute<double><<<nprob, 256, 0, st>>>(d_probs, nprob, (const double* const*)src_dev, perm_dev);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return tfx_set_cuda_error(e, "batch_permute");
   tfx_count_launch(1);
   return TFX_STATUS_OK;
 }

@@ -39,7 +39,9 @@ extern "C" int tfx_dgn_solve(int dtype, const tfx_dgn_problem* h_probs, tfx_dgn_
     maxR = q.R > maxR ? q.R : maxR;
   }
   maxdim_or_R = maxd > maxR ? maxd : maxR;
-  const int TS = maxdim_or_R <= 16 ? 1 : (maxdim_or_R <= 32 ? 2 : 4);
+  if (op->tile != 0 && op->tile != 1 && op->tile != 2 && op->tile != 4)
+    return tfx_set_error(TFX_STATUS_ERR_ARG, "tile must be 0, 1, 2 or 4");
+  const int TS = op->tile ? op->tile : (maxdim_or_R <= 16 ? 1 : (maxdim_or_R <= 32 ? 2 : 4));
   const int maxncol = (maxR + cluster - 1) / cluster;
   const size_t es = dtype == TFX_F64 ? 8 : 4;
   if (op->maxiter > 4096) return tfx_set_error(TFX_STATUS_ERR_UNSUPPORTED, "maxiter above 4096");

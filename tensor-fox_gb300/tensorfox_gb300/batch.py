@@ -18,11 +18,12 @@ iteration, one value per problem for each iteration (same distribution as
 GaussNewton.py:267).
 """
 import ctypes
+import os
 
 import numpy as np
 import torch
 
-from . import _dev, _lib
+from . import _dev, _lib, tuner
 from .api import Output, consistency, sort_dims
 from .gauss_newton import _inner_of
 from .options import make_options
@@ -103,13 +104,57 @@ def _equalize_random(dims, R):
     return f
 
 
-def cpd_batch(tensors, ranks, options=None):
+def _tuned_launch(prec, L, core_dims, Rs, work, dd, launch):
+    """(tile, order) for this batch from the autotuner, timing candidates on a
+    sample of the batch's own problems (their outputs are rewritten by the
+    full launch)."""
+    import torch
+    n = len(Rs)
+    mc, mr = int(core_dims.max()), int(Rs.max())
+    key = tuner.signature(prec, L, mc, mr, n)
+    tu = tuner.tuner()
+    hit = tu.lookup(key)
+    cands = tuner.candidates(mc, mr)
+    if hit is not None and hit in cands:
+        return hit
+    sm = torch.cuda.get_device_properties(0).multi_processor_count
+    idx = tuner.sample_indices(n, 2 * sm)
+
+    def run(c):
+        tile, order = c
+        sel = idx[tuner.order_largest_first(work[idx])] if order == 'largest_first' else idx
+        stream = torch.cuda.current_stream()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        launch(dd[sel], tile)            # warm-up (first use of a kernel variant)
+        a.record(stream)
+        launch(dd[sel], tile)
+        b.record(stream)
+        b.synchronize()
+        return a.elapsed_time(b) / 1e3
+    return tu.choose(key, cands, run)
+
+
+def cpd_batch(tensors, ranks, options=None, timings=None, tune=True):
     """CPD of every tensor in ``tensors`` with the matching rank in ``ranks``.
 
     Returns a list of ``(factors, output)`` pairs like ``cpd``.  Dense FP32 or
     FP64 inputs (NumPy or torch); every dimension <= 64; method 'dGN'.
+    ``timings`` (a dict), when given, receives the wall seconds of each stage
+    (the device is synchronised between stages, so only for profiling).
+    ``tune``: pick the engine's tile and problem order with the autotuner
+    (``tuner.py``; the first batch of a new size class pays for the timing);
+    ``options.tile`` (1, 2 or 4) forces a tile with the largest-first order.
     """
     _dev.require_cuda()
+    import time as _time
+    _t = [_time.perf_counter()]
+
+    def _mark(name):
+        if timings is not None:
+            torch.cuda.synchronize()
+            now = _time.perf_counter()
+            timings[name] = timings.get(name, 0.0) + now - _t[0]
+            _t[0] = now
     o = make_options(options)
     n = len(tensors)
     if n == 0:
@@ -145,13 +190,27 @@ def cpd_batch(tensors, ranks, options=None):
     c_off = np.concatenate([[0], np.cumsum([_al(v) for v in c_sz])])
     s_sz = [sum(mm) for mm in mins]
     s_off = np.concatenate([[0], np.cumsum([_al(v, 8) for v in s_sz])])
-    # pinned staging buffer: one copy per problem into it, one fast H2D copy
+    # pinned staging buffer: each tensor copied as it is (contiguous copies,
+    # several host threads), one H2D copy, then the mode permutation of every
+    # problem on the device (tfx_batch_permute)
     pinned = torch.empty(int(t_off[-1]), dtype=torch.float64 if prec == 'fp64' else torch.float32, pin_memory=True)
     host = pinned.numpy()
-    for p, (T, ordering) in enumerate(zip(tensors, orders)):
+
+    def _stage(p):
+        T = tensors[p]
         a = T.detach().cpu().numpy() if isinstance(T, torch.Tensor) else np.asarray(T)
-        host[t_off[p]:t_off[p] + N[p]].reshape(shapes[p])[...] = np.transpose(a, ordering)
-    Tbuf = pinned.to(dev, non_blocking=False)
+        host[t_off[p]:t_off[p] + N[p]] = a.reshape(-1)
+    if n >= 64:   # NumPy copies release the GIL
+        from concurrent.futures import ThreadPoolExecutor
+        with ThreadPoolExecutor(max_workers=min(16, os.cpu_count() or 4)) as ex:
+            list(ex.map(_stage, range(n)))
+    else:
+        for p in range(n):
+            _stage(p)
+    _mark('stage_host')
+    Traw = pinned.to(dev, non_blocking=False)
+    Tbuf = torch.empty_like(Traw)
+    _mark('h2d')
     work = torch.empty(int(w_off[-1]), dtype=dt, device=dev)
     Ubuf = torch.empty(int(u_off[-1]), dtype=dt, device=dev)
     Cbuf = torch.empty(max(1, int(c_off[-1])), dtype=dt, device=dev)
@@ -174,12 +233,20 @@ def cpd_batch(tensors, ranks, options=None):
     if tol < 0:
         raise NotImplementedError("cpd_batch compresses every problem (tol_mlsvd >= 0)")
     st = ctypes.c_void_p(_dev.stream())
+    perm = torch.from_numpy(np.concatenate([np.asarray(od, dtype=np.int32) for od in orders])).to(dev)
+    srcp = torch.from_numpy((Traw.data_ptr() + t_off[:-1] * es).astype(np.uint64).view(np.int64)).to(dev)
+    lib.tfx_batch_permute.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p,
+                                      ctypes.c_void_p, ctypes.c_void_p]
+    _lib.check(lib.tfx_batch_permute(_dev.lib_dtype(prec), ctypes.c_void_p(bd.ctypes.data),
+                                     ctypes.c_void_p(d_bd.data_ptr()), n, ctypes.c_void_p(srcp.data_ptr()),
+                                     ctypes.c_void_p(perm.data_ptr()), st))
     lib.tfx_batch_mlsvd.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_double,
                                     ctypes.c_int, ctypes.c_void_p]
     _lib.check(lib.tfx_batch_mlsvd(_dev.lib_dtype(prec), ctypes.c_void_p(bd.ctypes.data),
                                    ctypes.c_void_p(d_bd.data_ptr()), n, float(tol),
                                    int(o.svd_n_components or 0), st))
     core_dims = cdims.cpu().numpy()
+    _mark('mlsvd')
     # starting points (host RNG, problem order) and engine descriptors
     nx = np.array([int(Rs[p]) * int(core_dims[p].sum()) for p in range(n)], dtype=np.int64)
     x_off = np.concatenate([[0], np.cumsum([_al(v) for v in nx])])
@@ -231,8 +298,26 @@ def cpd_batch(tensors, ranks, options=None):
     opt.symm = 1 if o.symm else 0
     opt.factors_norm = float(o.factors_norm)
     cl = int(o.cluster or 1)
-    _lib.check(lib.tfx_dgn_solve(_dev.lib_dtype(prec), ctypes.cast(dd.ctypes.data, ctypes.POINTER(_lib.DgnProblem)),
-                                 ctypes.c_void_p(d_dd.data_ptr()), n, ctypes.byref(opt), cl, st))
+    _mark('starts_and_descriptors')
+
+    def _launch(desc, tile):
+        opt.tile = int(tile)
+        desc = np.ascontiguousarray(desc)
+        _lib.check(lib.tfx_dgn_solve(_dev.lib_dtype(prec), ctypes.cast(desc.ctypes.data, ctypes.POINTER(_lib.DgnProblem)),
+                                     ctypes.c_void_p(d_dd.data_ptr()), len(desc), ctypes.byref(opt), cl, st))
+    work = np.prod(core_dims.astype(np.float64), axis=1) * Rs
+    forced = getattr(o, 'tile', None)
+    if forced:
+        tile, order = int(forced), 'largest_first'
+    elif not tune or cl != 1:
+        tile, order = 0, 'given'
+    else:
+        tile, order = _tuned_launch(prec, L, core_dims, Rs, work, dd, _launch)
+    perm = tuner.order_largest_first(work) if order == 'largest_first' else np.arange(n)
+    _launch(dd[perm], tile)
+    if timings is not None:
+        timings['engine_config'] = (tile, order)
+    _mark('dgn_engine')
     # decompression and final errors
     f_sz = [int(Rs[p]) * sum(shapes[p]) for p in range(n)]
     f_off = np.concatenate([[0], np.cumsum([_al(v) for v in f_sz])])
@@ -254,6 +339,7 @@ def cpd_batch(tensors, ranks, options=None):
     st_h = stats.cpu().numpy()
     rs_h = result.cpu().numpy()
     _lib.check_solve_status(rs_h)
+    _mark('decompress_residual_d2h')
     out = []
     for p in range(n):
         R = int(Rs[p])
@@ -278,4 +364,5 @@ def cpd_batch(tensors, ranks, options=None):
         op.matvecs = int(info_h[p, 4])
         op.core_dims = [int(d) for d in core_dims[p]]
         out.append((factors, op))
+    _mark('assemble')
     return out

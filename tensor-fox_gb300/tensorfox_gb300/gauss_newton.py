@@ -127,6 +127,7 @@ class _Batch:
         o.use_damp_sched = 1 if sched is not None else 0
         o.symm = 1 if options.symm else 0
         o.factors_norm = float(options.factors_norm)
+        o.tile = int(getattr(options, 'tile', None) or 0)
         self.opts = o
 
     def launch(self, cluster, stream=None):

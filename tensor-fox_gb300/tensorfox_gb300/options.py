@@ -1,17 +1,19 @@
 """Options object with Tensor Fox's defaults (Auxiliar.py:242-362).
 
 ``make_options`` copies every attribute the caller's object defines over the
-defaults, exactly like the reference.  Two fields are added by this package and
+defaults, exactly like the reference.  Three fields are added by this package and
 ignored by the reference: ``precision`` ('fp64', 'fp32' or None for the input's
 own type, 'mixed' = FP32 data with TF32 tensor-core contractions for the
-compression) and ``cluster`` (CTAs per problem in the device engine, None = auto).
+compression), ``cluster`` (CTAs per problem in the device engine, None = auto)
+and ``tile`` (the engine's register tile, 1, 2 or 4; None = chosen by size, or by
+the autotuner in ``cpd_batch``).
 """
 
 _DEFAULTS = dict(maxiter=200, tol=1e-16, tol_step=1e-6, tol_improv=1e-6, tol_grad=1e-6, tol_jump=10,
                  method='dGN', inner_method='cg', cg_maxiter=100, cg_factor=1, cg_tol=1e-16,
                  initialization='random', trunc_dims=0, mlsvd_method='seq', tol_mlsvd=1e-16, init_damp=1,
                  refine=False, symm=False, factors_norm=0, trials=3, display=0, epochs=1, gpu=False,
-                 mkl_dot=True, svd_n_components=None, precision=None, cluster=None)
+                 mkl_dot=True, svd_n_components=None, precision=None, cluster=None, tile=None)
 
 
 class Options:

@@ -61,3 +61,26 @@ def test_batch_agrees_with_serial_cpd_statistically():
     es = np.array([o.rel_error for _, o in outs])
     # same algorithm, different random starts: same quality on well-posed problems
     assert np.median(eb) < 3 * np.median(es) + 1e-6
+
+
+def test_engine_tile_and_order_do_not_change_results():
+    """The autotuner's choices (register tile 1/2/4, problem order) only change
+    speed: every problem's trajectory stays the same."""
+    Ts, _, Rs = problems(40, 5)
+    ref = None
+    for tile in (None, 1, 2, 4):
+        o = tfx.make_options(None)
+        o.tile = tile
+        o.maxiter = 40
+        np.random.seed(6)
+        tm = {}
+        out = tfx.cpd_batch(Ts, Rs, o, timings=tm, tune=(tile is None))
+        errs = [np.asarray(op.errors[0]) for _, op in out]
+        if ref is None:
+            ref = errs
+            assert tm['engine_config'][1] in ('given', 'largest_first')
+        else:
+            assert tm['engine_config'] == (tile, 'largest_first')
+            for a, b in zip(errs, ref):
+                assert len(a) == len(b)
+                np.testing.assert_allclose(a, b, rtol=1e-10, atol=1e-15)
