@@ -265,25 +265,39 @@ struct TcGram2Smem {
 };
 
 __global__ void __launch_bounds__(128, 1)
-    k_gram_tc2(const __grid_constant__ CUtensorMap tmap, int D, long long P, int qchunks, int ksplit, float* part,
-               int* err) {
+    k_gram_tc2(const __grid_constant__ CUtensorMap tmap, int D, long long P, int qchunks, int ks_d, int ks_o,
+               float* part, int* err) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   TcGram2Smem& S = *reinterpret_cast<TcGram2Smem*>((((uintptr_t)smem_raw) + 1023) & ~(uintptr_t)1023);
   const int nt = (D + TCG_BM - 1) / TCG_BM;
   const int ns = (nt + 1) / 2;
-  int t = blockIdx.x, I = 0;
-  while (t >= ns - I) {
-    t -= ns - I;
-    ++I;
+  // CTAs [0, ns*ks_d): diagonal super-blocks (I, I), ks_d splits each; then the
+  // off-diagonal ones (I < J), ks_o splits each -- split counts in proportion to
+  // the blocks computed (3 vs 4), so every CTA carries about the same work
+  int I, J, split, ksplit;
+  if ((int)blockIdx.x < ns * ks_d) {
+    I = J = blockIdx.x / ks_d;
+    split = blockIdx.x - I * ks_d;
+    ksplit = ks_d;
+  } else {
+    const int v = blockIdx.x - ns * ks_d;
+    int t = v / ks_o;
+    split = v - t * ks_o;
+    ksplit = ks_o;
+    I = 0;
+    while (t >= ns - 1 - I) {
+      t -= ns - 1 - I;
+      ++I;
+    }
+    J = I + 1 + t;
   }
-  const int J = I + t;
   const bool diag = I == J;
   // accumulator p: (A slot, B slot, block row tile, block column tile)
   const int npair = diag ? 3 : 4;
   const int pa[4] = {0, 0, diag ? 1 : 1, 1};
   const int pb[4] = {diag ? 0 : 2, diag ? 1 : 3, diag ? 1 : 2, 3};
   const long long nchunk = P * qchunks;
-  const long long c0 = nchunk * blockIdx.y / ksplit, c1 = nchunk * (blockIdx.y + 1) / ksplit;
+  const long long c0 = nchunk * split / ksplit, c1 = nchunk * (split + 1) / ksplit;
   const int nit = (int)(c1 - c0);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
@@ -368,7 +382,7 @@ __global__ void __launch_bounds__(128, 1)
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const bool ok_all = !*(volatile int*)&S.abort;
-  float* out = part + (size_t)blockIdx.y * D * D;
+  float* out = part + (size_t)split * D * D;
   for (int pp = 0; pp < npair; ++pp) {
     const int bi = (pa[pp] == 0 ? 2 * I : 2 * I + 1);
     const int bj = (pb[pp] == 0 ? 2 * I : pb[pp] == 1 ? 2 * I + 1 : pb[pp] == 2 ? 2 * J : 2 * J + 1);
@@ -409,11 +423,16 @@ __global__ void __launch_bounds__(128, 1)
   }
 }
 
-__global__ void k_gram_tc_reduce(const float* __restrict__ part, int D, int ksplit, float* __restrict__ G) {
+// G from the split-K partials of the upper blocks.  ks_d partials for blocks of
+// the diagonal 256 x 256 super-blocks, ks_o for the others (super2 == 0: one
+// count, ks_d, for every block).
+__global__ void k_gram_tc_reduce(const float* __restrict__ part, int D, int ks_d, int ks_o, int super2,
+                                 float* __restrict__ G) {
   const long long n = (long long)D * D;
   for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x) {
     const int i = (int)(e / D), j = (int)(e - (long long)i * D);
     const long long src = (i / TCG_BM <= j / TCG_BM) ? e : (long long)j * D + i;
+    const int ksplit = (!super2 || (i / (2 * TCG_BM)) == (j / (2 * TCG_BM))) ? ks_d : ks_o;
     // compensated FP32 sum of the partials, in split order (FP64 adds are slow on GB300)
     Acc<float> s;
     for (int k = 0; k < ksplit; ++k) s.add(__ldcs(part + (size_t)k * n + src));
@@ -455,18 +474,39 @@ static int sm_count() {
 // the 2 x 2 super-block kernel serves Grams with at least two row tiles
 static bool tc_use2(int D) { return (D + TCG_BM - 1) / TCG_BM >= 2; }
 
-static int tc_splits(long long P, int D, long long Q) {
+// Split-K counts.  Every kernel keeps one CTA per SM, so the grid is sized to
+// fit one wave: the single-block kernel splits each of its blocks evenly; the
+// 2 x 2 kernel gives diagonal super-blocks (3 blocks computed) and
+// off-diagonal ones (4 blocks) split counts in the ratio 3 : 4.
+struct TcSplits {
+  int ks_d, ks_o;
+};
+static TcSplits tc_splits(long long P, int D, long long Q) {
   const int nt = (D + TCG_BM - 1) / TCG_BM;
-  const int ns = (nt + 1) / 2;
-  const long long tiles = tc_use2(D) ? (long long)ns * (ns + 1) / 2 : (long long)nt * (nt + 1) / 2;
   const long long chunks = P * ((Q + TCG_BK - 1) / TCG_BK);
-  long long ks = (sm_count() + tiles - 1) / tiles;
-  ks = std::min<long long>(ks, std::max<long long>(1, chunks / 8));
-  return (int)std::max<long long>(1, std::min<long long>(ks, 64));
+  const long long cap = std::max<long long>(1, std::min<long long>(64, chunks / 8));
+  const int sms = sm_count();
+  TcSplits r;
+  if (!tc_use2(D)) {
+    const long long tiles = (long long)nt * (nt + 1) / 2;
+    const long long ks = std::max<long long>(1, std::min<long long>(cap, sms / tiles));
+    r.ks_d = r.ks_o = (int)ks;
+    return r;
+  }
+  const int ns = (nt + 1) / 2;
+  const long long noff = (long long)ns * (ns - 1) / 2;
+  const double x = (double)sms / (3.0 * ns + 4.0 * noff);
+  long long kd = std::max<long long>(1, (long long)(3.0 * x));
+  long long ko = std::max<long long>(1, (long long)(4.0 * x));
+  if (noff == 0) kd = std::max<long long>(1, sms / ns);
+  r.ks_d = (int)std::min<long long>(cap, kd);
+  r.ks_o = (int)std::min<long long>(cap, ko);
+  return r;
 }
 
 extern "C" size_t tfx_mode_gram_tc_scratch_bytes(long long P, int D, long long Q) {
-  return (size_t)tc_splits(P, D, Q) * D * D * 4 + 16;
+  const TcSplits k = tc_splits(P, D, Q);
+  return (size_t)std::max(k.ks_d, k.ks_o) * D * D * 4 + 16;
 }
 
 extern "C" int tfx_mode_gram_tc(const float* S, long long P, int D, long long Q, float* G, void* scratch,
@@ -478,10 +518,11 @@ extern "C" int tfx_mode_gram_tc(const float* S, long long P, int D, long long Q,
   if (P > 0x7fffffffLL || Q > 0x7fffffffLL) return tfx_set_error(TFX_STATUS_ERR_ARG, "mode_gram_tc extent");
   EncodeTiledFn enc = encode_fn();
   if (!enc) return tfx_set_error(TFX_STATUS_ERR_UNSUPPORTED, "cuTensorMapEncodeTiled unavailable");
-  int ks = tc_splits(P, D, Q);
+  TcSplits kk = tc_splits(P, D, Q);
   const size_t per = (size_t)D * D * 4;
   if (scratch_bytes < per) return tfx_set_error(TFX_STATUS_ERR_ARG, "mode_gram_tc scratch too small");
-  ks = (int)std::min<size_t>((size_t)ks, scratch_bytes / per);
+  kk.ks_d = (int)std::min<size_t>((size_t)kk.ks_d, scratch_bytes / per);
+  kk.ks_o = (int)std::min<size_t>((size_t)kk.ks_o, scratch_bytes / per);
   CUtensorMap map;
   const cuuint64_t gdim[3] = {(cuuint64_t)Q, (cuuint64_t)D, (cuuint64_t)P};
   const cuuint64_t gstride[2] = {(cuuint64_t)Q * 4, (cuuint64_t)Q * D * 4};
@@ -497,24 +538,24 @@ extern "C" int tfx_mode_gram_tc(const float* S, long long P, int D, long long Q,
   cudaError_t e;
   if (tc_use2(D)) {
     const int ns = (nt + 1) / 2;
-    const int tiles = ns * (ns + 1) / 2;
+    const int ncta = ns * kk.ks_d + (ns * (ns - 1) / 2) * kk.ks_o;
     const size_t sm = sizeof(TcGram2Smem) + 1024;
     e = cudaFuncSetAttribute(k_gram_tc2, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     if (e != cudaSuccess) return tfx_set_cuda_error(e, "mode_gram_tc smem");
-    k_gram_tc2<<<dim3(tiles, ks), 128, sm, st>>>(map, D, P, qchunks, ks, (float*)scratch, err);
+    k_gram_tc2<<<ncta, 128, sm, st>>>(map, D, P, qchunks, kk.ks_d, kk.ks_o, (float*)scratch, err);
   } else {
     const int tiles = nt * (nt + 1) / 2;
     const size_t sm = sizeof(TcGramSmem) + 1024;
     e = cudaFuncSetAttribute(k_gram_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     if (e != cudaSuccess) return tfx_set_cuda_error(e, "mode_gram_tc smem");
-    k_gram_tc<<<dim3(tiles, ks), 128, sm, st>>>(map, D, P, qchunks, ks, (float*)scratch, err);
+    k_gram_tc<<<dim3(tiles, kk.ks_d), 128, sm, st>>>(map, D, P, qchunks, kk.ks_d, (float*)scratch, err);
   }
   e = cudaGetLastError();
   if (e != cudaSuccess) return tfx_set_cuda_error(e, "mode_gram_tc launch");
   tfx_count_launch(1);
   const long long n = (long long)D * D;
   const int rb = (int)std::max<long long>(1, std::min<long long>((n + 255) / 256, 4LL * sm_count()));
-  k_gram_tc_reduce<<<rb, 256, 0, st>>>((const float*)scratch, D, ks, G);
+  k_gram_tc_reduce<<<rb, 256, 0, st>>>((const float*)scratch, D, kk.ks_d, kk.ks_o, tc_use2(D) ? 1 : 0, G);
   e = cudaGetLastError();
   if (e != cudaSuccess) return tfx_set_cuda_error(e, "mode_gram_tc reduce");
   tfx_count_launch(1);
