@@ -761,16 +761,133 @@ def clean_zeros(init_factors, dims, R):
     return init_factors
 
 
+def smart_sample(S, dims, R):
+    """One draw of Initialization.py:139-183: per mode an index i taken with
+    probability proportional to d - i (arr = [d, d-1, ..., 1], one integer in
+    [0, sum(arr)) per column), a unit entry at that index in every factor, and
+    the core's value at the chosen position in the first factor."""
+    L = len(dims)
+    f = [np.zeros((dims[l], R)) for l in range(L)]
+    arr = [dims[l] * np.ones(dims[l]) - np.arange(dims[l]) for l in range(L)]
+    high = [np.sum(arr[l]) for l in range(L)]
+    C = [np.random.randint(high[l], size=R) for l in range(L)]
+    cum = [np.cumsum(arr[l]) for l in range(L)]
+    for r in range(R):
+        idx = [int(np.searchsorted(cum[l], C[l][r], side='right')) for l in range(L)]
+        for l in range(L):
+            f[l][idx[l], r] = 1
+        f[0][idx[0], r] = S[tuple(idx)]
+    return f
+
+
+def smart_random(S, dims, R):
+    """Best of 1 + int(sqrt(prod(dims))) smart samples by relative error to S
+    (Initialization.py:97-136), the first one kept on ties."""
+    samples = 1 + int(np.sqrt(np.prod(np.array(dims))))
+    S1 = unfold(S, 1)
+    Ssize = norm(S)
+    best, best_error = None, np.inf
+    for _ in range(samples):
+        f = smart_sample(S, dims, R)
+        e = norm(S1 - cpd2unfold1(f)) / Ssize
+        if e < best_error:
+            best_error, best = e, [w.copy() for w in f]
+    return best
+
+
+def join_rank1(idx):
+    """Initialization.py:289-342: groups of chosen positions that differ in one
+    coordinate only (one rank-one term each), with the reference's scan order --
+    removals inside the scans shift the lists under the running indices."""
+    R, L = len(idx), len(idx[0])
+    count = 0
+    pool = list(idx)
+    groups = [[] for _ in range(L * R)]
+    g = 0
+    for l in range(L):
+        keep = [j for j in range(L) if j != l]
+        r = 0
+        while r < len(pool):
+            key = tuple(pool[r][j] for j in keep)
+            rr = r + 1
+            while rr < len(pool):
+                if tuple(pool[rr][j] for j in keep) == key:
+                    groups[g].append(pool[rr])
+                    pool.remove(pool[rr])
+                    count += 1
+                rr += 1
+            if groups[g]:
+                groups[g].append(pool[r])
+                pool.remove(pool[r])
+            g += 1
+            r += 1
+    return count, [x for x in groups if x]
+
+
+def find_pivot(x):
+    """The coordinate that varies inside a group (Initialization.py:345-358)."""
+    if len(x) == 1:
+        return 0
+    for l in range(len(x[0])):
+        if x[0][l] != x[1][l]:
+            return l
+
+
+def smart(S, dims, R):
+    """Deterministic start from the R largest-magnitude core entries, merged
+    into rank-one terms where they share all coordinates but one, and extended
+    by the next entries while merges free terms (Initialization.py:186-286)."""
+    L = len(dims)
+    flat = np.argsort(-np.abs(S).ravel(), kind='stable')
+    order = [tuple(int(v) for v in np.unravel_index(k, S.shape)) for k in flat]
+    chosen, rest = order[:R], order[R:]
+    prev = 0
+    joined = []
+    for _ in range(100):
+        count, joined = join_rank1(chosen)
+        if count - prev <= 0:
+            break
+        chosen = chosen + rest[:count - prev]
+        rest = rest[count - prev:]
+        prev = count
+    terms = [[] for _ in range(R)]
+    r = 0
+    for grp in joined:
+        for y in grp:
+            terms[r].append(y)
+            chosen.remove(y)
+        r += 1
+    for x in chosen:
+        terms[r].append(x)
+        r += 1
+    f = [np.zeros((dims[l], R)) for l in range(L)]
+    for r in range(R):
+        m = find_pivot(terms[r])
+        for x in terms[r]:
+            for l in range(L):
+                if l == m:
+                    f[l][x[l], r] += S[x]
+                else:
+                    f[l][x[l], r] = 1
+    return f
+
+
 def starting_point(S, U, R, ordering, options):
-    """'random' or user-list initial factors in the compressed space (Initialization.py:20-94)."""
+    """User list, 'random', 'smart_random' or 'smart' initial factors in the
+    compressed space (Initialization.py:20-94)."""
     init = options.initialization
     dims = S.shape
     L = len(dims)
     if type(init) == list:
         return [U[l].T @ init[ordering[l]] for l in range(L)]
-    if init != 'random':
+    if init == 'random':
+        f = [np.random.randn(dims[l], R) for l in range(L)]
+    elif init == 'smart_random':
+        f = smart_random(S, dims, R)
+    elif init == 'smart':
+        f = smart(S, dims, R)
+    else:
         raise NotImplementedError("initialization " + repr(init))
-    f = [np.random.randn(dims[l], R) for l in range(L)]
     f = clean_zeros(f, dims, R)
     f = equalize(f, R)
     return transform(f, options.symm, options.factors_norm)

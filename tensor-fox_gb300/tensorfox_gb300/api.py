@@ -121,6 +121,20 @@ def starting_point_random(dims, R, options, vectorized=False):
     return f
 
 
+def starting_point_core(S, core, R, options, vectorized=False):
+    """'random', 'smart_random' or 'smart' start in the compressed space
+    (Initialization.py:20-94); S is the device core."""
+    init = options.initialization
+    if init == 'random':
+        return starting_point_random(core, R, options, vectorized=vectorized)
+    if init in ('smart_random', 'smart'):
+        from .initialization import clean_and_balance, smart, smart_random
+        Sh = S.double().cpu().numpy()
+        f = smart_random(Sh, R) if init == 'smart_random' else smart(Sh, R)
+        return clean_and_balance(f, R, options, vectorized=vectorized)
+    sys.exit('Error with init parameter initialization.')
+
+
 def _flat_dev(factors, dtype, device):
     return torch.from_numpy(_dev.flat_factors(factors)).to(device=device, dtype=dtype)
 
@@ -191,10 +205,8 @@ def tricpd(T, R, options):
         for l in range(L):
             W = torch.from_numpy(np.asarray(o.initialization[ordering[l]], dtype=np.float64)).to(Td.device, dt)
             init.append(kernels.matmul(Uts[l], W).double().cpu().numpy())
-    elif o.initialization == 'random':
-        init = starting_point_random(core, R, o, vectorized=(prec == 'fp32'))
     else:
-        raise NotImplementedError("initialization %r is outside the dGN path" % (o.initialization,))
+        init = starting_point_core(S, core, R, o, vectorized=(prec == 'fp32'))
     x0 = _flat_dev(init, dt, Td.device)
     best, ss, er, im, gr, st = solve(S, x0, R, o, prec)
     Wf = _decompress(Uts, best, core, R)

@@ -161,7 +161,7 @@ def mlsvd_sparse_device(X, R, options):
 
 def tricpd_sparse(T, R, options):
     """``tricpd`` for ``[data, idxs, dims]`` (TensorFox.py:424-655, sparse branches)."""
-    from .api import Output, starting_point_random, _decompress, _run_dgn, _run_als, unsort_dims
+    from .api import Output, starting_point_core, _decompress, _run_dgn, _run_als, unsort_dims
     o = options
     if o.method not in ('dGN', 'als'):
         raise NotImplementedError("method %r is outside the damped Gauss-Newton and ALS paths" % (o.method,))
@@ -183,7 +183,7 @@ def tricpd_sparse(T, R, options):
             W = torch.from_numpy(np.asarray(o.initialization[ordering[l]], dtype=np.float64)).to(S.device, dt)
             init.append(kernels.matmul(Uts[l], W).double().cpu().numpy())
     else:
-        init = starting_point_random(core, R, o)
+        init = starting_point_core(S, core, R, o)
     x0 = torch.from_numpy(_dev.flat_factors(init)).to(device=S.device, dtype=dt)
     best, ss, er, im, gr, st = (_run_als if o.method == 'als' else _run_dgn)(S, x0, R, o, prec)
     Wf = _decompress(Uts, best, core, R)

@@ -33,7 +33,7 @@ import numpy as np
 import torch
 
 from . import _dev, kernels
-from .api import _decompress, _flat_dev, _precision, _run_als, consistency, sort_dims, starting_point_random, cpd
+from .api import _decompress, _flat_dev, _precision, _run_als, consistency, sort_dims, starting_point_core, cpd
 from .compression import mlsvd_device
 from .gauss_newton import _Batch, _inner_of, auto_cluster
 from .options import make_options
@@ -91,17 +91,15 @@ class _Dense:
             core = [Rm] * L
         return S, Uts, [int(c) for c in core]
 
-    def start(self, R, o, Uts, core):
+    def start(self, R, o, Uts, core, S):
         L = len(self.dims)
         if isinstance(o.initialization, list):
             init = []
             for l in range(L):
                 W = torch.from_numpy(np.asarray(o.initialization[self.ordering[l]], dtype=np.float64))
                 init.append(kernels.matmul(Uts[l], W.to(self.Td.device, self.dt)).double().cpu().numpy())
-        elif o.initialization == 'random':
-            init = starting_point_random(core, R, o, vectorized=(self.prec == 'fp32'))
         else:
-            raise NotImplementedError("initialization %r" % (o.initialization,))
+            init = starting_point_core(S, core, R, o, vectorized=(self.prec == 'fp32'))
         return _flat_dev(init, self.dt, self.Td.device)
 
     def solve(self, problems, o):
@@ -172,7 +170,7 @@ def stats(T, R, options=False, num_samples=100):
         raise NotImplementedError("method %r" % (o.method,))
     X = _Dense(T, o)
     S, Uts, core = X.compress(R, o)
-    probs = [(S, Uts, core, R, X.start(R, o, Uts, core)) for _ in range(n)]
+    probs = [(S, Uts, core, R, X.start(R, o, Uts, core, S)) for _ in range(n)]
     res = X.solve(probs, o)
     torch.cuda.synchronize()
     wall = time.perf_counter() - t0
@@ -244,7 +242,7 @@ def rank(T, options=False, plot=True, trials=3):
         for q in ranks:
             S, Uts, core = X.compress(q, o)
             for _ in range(trials):
-                probs.append((S, Uts, core, q, X.start(q, o, Uts, core)))
+                probs.append((S, Uts, core, q, X.start(q, o, Uts, core, S)))
                 owner.append(q)
         res = X.solve(probs, o)
         best = {q: np.inf for q in ranks}

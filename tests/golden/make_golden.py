@@ -28,6 +28,7 @@ import TensorFox.Critical as crt  # noqa: E402
 import TensorFox.Compression as cmpr  # noqa: E402
 import TensorFox.MultilinearAlgebra as mla  # noqa: E402
 import TensorFox.Alternating_Least_Squares as alsm  # noqa: E402
+import TensorFox.Initialization as ini  # noqa: E402
 
 
 def save(name, **arrays):
@@ -286,7 +287,40 @@ def rank_tables(L, n, trials, seed):
     return tabs
 
 
+def init_case(name, seed):
+    """starting_point (Initialization.py:20-94) with 'smart_random' and 'smart' on
+    seeded cores (Gaussian, and integer-valued with ties), with the RNG state it
+    leaves (np.random.rand() drawn right after)."""
+    rng = np.random.default_rng(seed)
+    rows = []
+    cores = [((5, 4, 3), 3, rng.standard_normal((5, 4, 3))),
+             ((6, 5, 4), 4, rng.standard_normal((6, 5, 4))),
+             ((4, 4, 3, 3), 2, rng.standard_normal((4, 4, 3, 3))),
+             ((5, 4, 3), 4, rng.integers(-3, 4, size=(5, 4, 3)).astype(np.float64)),
+             ((4, 3, 3), 6, np.arange(36, dtype=np.float64).reshape(4, 3, 3) % 5 - 2.0)]
+    out = {}
+    for k, (dims, R, S) in enumerate(cores):
+        for method in ("smart_random", "smart"):
+            o = Opt()
+            o.initialization = method
+            o = tfx.make_options(o)
+            np.random.seed(seed + k)
+            f = ini.starting_point(S, 1.0, S, [np.eye(d) for d in dims], R, list(range(len(dims))), o)
+            after = np.random.rand()
+            out["S%d" % k] = S
+            out["R%d" % k] = R
+            out["%s%d" % (method, k)] = np.concatenate([w.flatten('F') for w in f])
+            out["%s_after%d" % (method, k)] = after
+    out["n"] = len(cores)
+    out["seed"] = seed
+    save(name, **out)
+
+
 CASES = {
+    "init_smart": lambda: init_case("init_smart", 61),
+    "cpd_smart": lambda: cpd_case("cpd_smart", [14, 12, 10], 3, 62, 1e-5, initialization='smart'),
+    "cpd_smart_random": lambda: cpd_case("cpd_smart_random", [14, 12, 10], 3, 63, 1e-5,
+                                         initialization='smart_random'),
     "units_L3": lambda: units("units_L3", [7, 5, 4], 3, 1),
     "units_L4": lambda: units("units_L4", [5, 4, 3, 3], 2, 2),
     "units_L3_big": lambda: units("units_L3_big", [12, 10, 9], 4, 3, damp=0.2, cg_iters=9),

@@ -129,7 +129,7 @@ def _opts(g):
     return o
 
 
-@pytest.mark.parametrize("name", ["cpd_c1_small", "cpd_L4", "cpd_refine"])
+@pytest.mark.parametrize("name", ["cpd_c1_small", "cpd_L4", "cpd_refine", "cpd_smart", "cpd_smart_random"])
 def test_cpd_matches_reference(name):
     g = load_golden(name)
     T, R = g["T"], int(g["R"])

@@ -32,7 +32,7 @@ def test_batched_samples_equal_single_solves():
     np.random.seed(0)
     X = sweeps._Dense(T, o)
     S, Uts, core = X.compress(3, o)
-    probs = [(S, Uts, core, 3, X.start(3, o, Uts, core)) for _ in range(5)]
+    probs = [(S, Uts, core, 3, X.start(3, o, Uts, core, S)) for _ in range(5)]
     res = X.solve(probs, o)
     for p, r in zip(probs, res):
         best, ss, er, im, gr, st = _run_dgn(S, p[4], 3, o, X.prec)

@@ -219,3 +219,30 @@ def test_rank_rules_match_reference(name):
         assert fr == int(g["final_rank"][k])
         np.testing.assert_array_equal(epr, g["errors"][s:s + n])
         s += n
+
+
+def test_smart_starts_match_reference():
+    """Initialization.py:20-94 with 'smart_random' and 'smart' (Gaussian cores,
+    integer cores with ties), including the RNG state left behind."""
+    g = load_golden("init_smart")
+    for k in range(int(g["n"])):
+        S, R = g["S%d" % k], int(g["R%d" % k])
+        for method in ("smart_random", "smart"):
+            o = orc.Options()
+            o.initialization = method
+            o = orc.make_options(o)
+            np.random.seed(int(g["seed"]) + k)
+            f = orc.starting_point(S, [np.eye(d) for d in S.shape], R, list(range(S.ndim)), o)
+            assert np.random.rand() == float(g["%s_after%d" % (method, k)])
+            np.testing.assert_allclose(orc.cpd2flat(f), g["%s%d" % (method, k)], rtol=1e-12, atol=1e-15)
+
+
+@pytest.mark.parametrize("name", ["cpd_smart", "cpd_smart_random"])
+def test_cpd_smart_matches_reference(name):
+    g = load_golden(name)
+    o = _opts(g)
+    np.random.seed(int(g["seed"]))
+    f, out = orc.cpd(g["T"], int(g["R"]), o)
+    assert out.num_steps == int(g["num_steps"])
+    assert list(out.stop) == list(g["stop"])
+    np.testing.assert_allclose(out.rel_error, float(g["rel_error"]), rtol=1e-6)
