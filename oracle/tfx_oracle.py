@@ -477,11 +477,15 @@ def dGN(T, factors, R, options, budgets=None, trace=None):
     return best_factors, step_sizes[:n], errors[:n], improv[:n], gradients[:n], stop
 
 
-def als_iteration(Tl, factors):
-    """One ALS sweep (Alternating_Least_Squares.py:204-235, general case): mode by
-    mode, ``W_l = T_(l) · pinv(KR_l^T)`` with the freshly updated factors."""
+def als_iteration(Tl, factors, fix_mode=-1):
+    """One ALS sweep (Alternating_Least_Squares.py:204-264): mode by mode,
+    ``W_l = T_(l) · pinv(KR_l^T)`` with the freshly updated factors; a fixed
+    mode (third order, bicpd) is skipped -- the reference's explicit branches
+    update the two other modes in the same order with the same products."""
     L = len(factors)
     for l in range(L):
+        if l == fix_mode:
+            continue
         order = [m for m in reversed(range(L)) if m != l]
         M = kr_chain([factors[m] for m in order])
         factors[l] = Tl[l] @ np.linalg.pinv(M.T)
@@ -498,6 +502,12 @@ def als(T, factors, R, options):
     maxiter = o.maxiter
     tol, tol_step, tol_improv, tol_grad = o.tol, o.tol_step, o.tol_improv, o.tol_grad
     L = len(factors)
+    fix_mode, orig = -1, None
+    for l in range(L):                      # [W, l] marks a fixed factor (bicpd)
+        if type(factors[l]) == list:
+            fix_mode = l
+            factors[l] = factors[l][0]
+            orig = np.array(factors[l], dtype=np.float64)
     factors = [np.array(W, dtype=np.float64) for W in factors]
     Tsize = norm(T)
     error = 1
@@ -510,9 +520,11 @@ def als(T, factors, R, options):
     it = 0
     for it in range(maxiter):
         old_x, old_error = x, error
-        factors = als_iteration(Tl, factors)
+        factors = als_iteration(Tl, factors, fix_mode)
         x = cpd2flat(factors)
         factors = transform(factors, o.symm, o.factors_norm)
+        if L == 3 and fix_mode >= 0:
+            factors[fix_mode] = orig.copy()
         error = fastnorm(Tl[0], cpd2unfold1(factors)) / Tsize
         step_sizes[it] = norm(x - old_x)
         errors[it] = error
@@ -918,6 +930,150 @@ class Output:
     pass
 
 
+# ----------------------------------------------------------------------------
+# tensor-train CPD (TensorFox.py:256-421, 658-817, 1042-1065; Auxiliar.py:365-527;
+# Conversion.py:460-494)
+# ----------------------------------------------------------------------------
+def tt_core(V, dims, r1, r2, l):
+    """One core of the TT-SVD (Auxiliar.py:365-380).  The reference takes a
+    randomized SVD at full rank (scikit-learn, no power iteration): an exact SVD
+    up to rounding, whose Gaussian block it draws from NumPy's global RNG; the
+    block is drawn here too, so the RNG stays in step, and the SVD is LAPACK's.
+    Signs: the largest |entry| of every left singular vector is positive."""
+    V = np.asarray(V).reshape(r1 * dims[l], int(np.prod(dims[l + 1:])), order='F')
+    low = min(V.shape)
+    np.random.normal(size=(low, low + 10))
+    U, sv, Vt = sp_svd(V, full_matrices=False)
+    U, Vt = U[:, :low], Vt[:low]
+    for j in range(low):
+        k = np.argmax(np.abs(U[:, j]))
+        if U[k, j] < 0:
+            U[:, j] *= -1
+            Vt[j] *= -1
+    U = U[:, :r2]
+    Vn = (sv[:low, None] * Vt)[:r2, :]
+    g = U.reshape(dims[l], r2, order='F') if r1 == 1 else U.reshape(r1, dims[l], r2, order='F')
+    return Vn, g
+
+
+def cpdtt(T, R):
+    """TT cores d_0 x R -> R x d_1 x R -> ... -> R x d_{L-1} (TensorFox.py:1042-1065)."""
+    dims = np.array(T.shape)
+    L = len(dims)
+    G = []
+    r1, r2 = 1, R
+    V = T
+    for l in range(L - 1):
+        V, g = tt_core(V, dims, r1, r2, l)
+        r1, r2 = R, R
+        G.append(g)
+    G.append(V)
+    return G
+
+
+def inflate(T, R, dims):
+    """Pads every mode shorter than R with 1e-12 * randn entries (Conversion.py:460-480)."""
+    new = [d if d >= R else R for d in dims]
+    out = 1e-12 * np.random.randn(*new)
+    out[tuple(slice(d) for d in dims)] = T
+    return out
+
+
+def bicpd(T, R, fixed, options):
+    """Third-order CPD with one factor fixed (TensorFox.py:658-817): MLSVD of T,
+    a random start whose fixed factor is replaced by the projection of the given
+    one, ALS (bi_method 'als') on the core, decompression.  Returns
+    (X, Y, Z, output) in T's own mode order (no sort_dims)."""
+    o = options
+    if o.bi_method_parameters[0] != 'als':
+        raise NotImplementedError("bicpd with bi_method " + repr(o.bi_method_parameters[0]))
+    Tsize = norm(T)
+    S, U, T1, _ = mlsvd(T, Tsize, R, o)
+    f = starting_point(S, U, R, [0, 1, 2], o)
+    W, fl = fixed
+    f[fl] = [U[fl].T @ W, fl]
+    f, ss, er, im, gr, st = als(S, f, R, o)
+    out = [None, None, None]
+    for l in range(3):
+        out[l] = W if l == fl else U[l] @ f[l]
+    rel = fastnorm(T1, cpd2unfold1(out)) / Tsize
+    res = Output()
+    res.num_steps = len(ss)
+    res.rel_error = rel
+    res.stop = [st, 5]
+    return out[0], out[1], out[2], res
+
+
+def cpd_cores(G, max_trials, epochs, R, options):
+    """CPDs of the TT cores (Auxiliar.py:413-527): the first inner core by
+    tricpd (best of the trials, early exit below 1e-4), then sweeps of bicpd with
+    the factor shared with the neighbouring core fixed to pinv of the
+    neighbour's factor."""
+    L = len(G)
+    if epochs % 2 == 0:
+        epochs += 1
+    cpd_list = list(range(L - 2))
+    outputs = list(range(L - 2))
+    best_error = np.inf
+    for _ in range(max_trials):
+        f, out = _tricpd(G[1], R, options)
+        if out.rel_error < best_error:
+            best_out, best_error = out, out.rel_error
+            bX, bY, bZ = f
+            if best_error < 1e-4:
+                break
+    outputs[0] = best_out
+    cpd_list[0] = [bX, bY, bZ]
+    low, upp = 2, L - 2
+    for epoch in range(epochs):
+        if epoch % 2 == 0:
+            for l in range(low, L - 1):
+                best_error = np.inf
+                fX = np.linalg.pinv(bZ.T)
+                for _ in range(max_trials):
+                    X, Y, Z, out = bicpd(G[l], R, [fX, 0], options)
+                    if out.rel_error < best_error:
+                        best_out, best_error = out, out.rel_error
+                        bX, bY, bZ = fX, Y, Z
+                        if best_error < 1e-4:
+                            break
+                if epoch == epochs - 1:
+                    outputs[l - 1] = best_out
+                    cpd_list[l - 1] = [fX, bY, bZ]
+        else:
+            if L == 3:
+                low, upp = 1, L - 1
+            for l in reversed(range(1, upp)):
+                best_error = np.inf
+                fZ = np.linalg.pinv(bX.T)
+                for _ in range(max_trials):
+                    X, Y, Z, out = bicpd(G[l], R, [fZ, 2], options)
+                    if out.rel_error < best_error:
+                        best_out, best_error = out, out.rel_error
+                        bX, bY, bZ = X, Y, fZ
+                        if best_error < 1e-4:
+                            break
+                if epoch == epochs - 2:
+                    outputs[l - 1] = best_out
+                    cpd_list[l - 1] = [bX, bY, fZ]
+    return cpd_list, outputs, bZ
+
+
+def highcpd(T, R, options):
+    """TT cores, their CPDs, and the factors of T (TensorFox.py:368-421)."""
+    L = T.ndim
+    options.refine = False
+    G = cpdtt(T, R)
+    cpd_list, outputs, bZ = cpd_cores(G, options.trials, options.epochs, R, options)
+    factors = [G[0] @ cpd_list[0][0]]
+    for l in range(L - 2):
+        factors.append(cpd_list[l][1])
+    factors.append(G[-1].T @ bZ)
+    return equalize(factors, R), outputs
+
+
+
+
 def cpd(T, R, options=None, timings=None):
     """``cpd`` → ``tricpd`` for methods 'dGN' and 'als' (TensorFox.py:69-255, 424-655).
 
@@ -936,6 +1092,8 @@ def cpd(T, R, options=None, timings=None):
         _t[0] = now
 
     o = make_options(options)
+    if o.method == 'ttcpd':
+        return cpd_tt(T, R, o)
     sparse_in = isinstance(T, list)
     if sparse_in:
         data_orig = np.asarray(T[0], dtype=np.float64)
@@ -980,4 +1138,43 @@ def cpd(T, R, options=None, timings=None):
     out.stop = [st, st2]
     out.options = o
     _mark('final')
+    return factors, out
+
+
+def _tricpd(T, R, options):
+    """tricpd on a dense third-order tensor with the caller's options object
+    (TensorFox.py:424-655): the method is dGN unless it is 'als'."""
+    o = options
+    saved = o.method
+    o.method = 'als' if saved == 'als' else 'dGN'
+    try:
+        f, out = cpd(T, R, o)
+    finally:
+        o.method = saved
+    return f, out
+
+
+def cpd_tt(T, R, o):
+    """cpd with method 'ttcpd' on a dense tensor (TensorFox.py:256-365)."""
+    Ts, ordering = sort_dims(T)
+    Ts = np.asarray(Ts, dtype=np.float64)
+    Tsize = norm(Ts)
+    S, U, T1, _ = mlsvd(Ts, Tsize, R, o)
+    S_dims = S.shape
+    infl = R > min(S_dims)
+    if infl:
+        S = inflate(S, R, S_dims)
+    o.trunc_dims = 0
+    factors, outputs = highcpd(S, R, o)
+    if infl:
+        factors = [factors[l][:S_dims[l], :] for l in range(len(S_dims))]
+    factors = [U[l] @ factors[l] for l in range(len(factors))]
+    rel_error = fastnorm(unfold(Ts, 1), cpd2unfold1(factors)) / Tsize
+    factors = unsort_dims(factors, ordering)
+    out = Output()
+    out.num_steps = sum(x.num_steps for x in outputs)
+    out.rel_error = rel_error
+    out.accuracy = max(0, 100 * (1 - rel_error))
+    out.cpd_output = outputs
+    out.options = o
     return factors, out

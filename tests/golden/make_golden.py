@@ -316,7 +316,47 @@ def init_case(name, seed):
     save(name, **out)
 
 
+def tt_case(name, shapes, seed):
+    """cpdtt (TensorFox.py:1042-1065, tt_core Auxiliar.py:365-380): the TT cores
+    of seeded tensors and the RNG state the randomized SVDs leave behind."""
+    tf_mod = sys.modules["TensorFox.TensorFox"]
+    rng = np.random.default_rng(seed)
+    out = {"n": len(shapes), "seed": seed}
+    for k, (dims, R) in enumerate(shapes):
+        T = rng.standard_normal(dims)
+        np.random.seed(seed + k)
+        G = tf_mod.cpdtt(T, R)
+        out["T%d" % k] = T
+        out["R%d" % k] = R
+        out["ncores%d" % k] = len(G)
+        for j, g in enumerate(G):
+            out["G%d_%d" % (k, j)] = g
+        out["after%d" % k] = np.random.rand()
+    save(name, **out)
+
+
+def cpd_tt_case(name, dims, R, seed, noise, **opts):
+    """cpd with method='ttcpd' (TensorFox.py:256-421 highcpd, 658-817 bicpd,
+    Auxiliar.py:413-527 cpd_cores)."""
+    T, W = planted(dims, R, noise, seed)
+    o = Opt()
+    o.method = 'ttcpd'
+    for k, v in opts.items():
+        setattr(o, k, v)
+    np.random.seed(seed)
+    f, out = tfx.cpd(T, R, o)
+    save(name, T=T, R=R, seed=seed, planted=np.concatenate([w.flatten('F') for w in W]),
+         factors=np.concatenate([w.flatten('F') for w in f]), rel_error=out.rel_error,
+         num_steps=out.num_steps, core_steps=np.array([c.num_steps for c in out.cpd_output]),
+         core_errors=np.array([c.rel_error for c in out.cpd_output]), after=np.random.rand(),
+         opt_names=np.array(list(opts.keys())), opt_values=np.array([repr(v) for v in opts.values()]))
+
+
 CASES = {
+    "tt_cores": lambda: tt_case("tt_cores", [((6, 5, 4, 3), 2), ((5, 4, 4, 3, 3), 2), ((7, 6, 5, 4), 3)], 71),
+    "cpd_tt_L4": lambda: cpd_tt_case("cpd_tt_L4", [9, 8, 7, 6], 3, 72, 1e-5),
+    "cpd_tt_L5": lambda: cpd_tt_case("cpd_tt_L5", [7, 6, 6, 5, 5], 2, 73, 1e-5),
+    "cpd_tt_L3": lambda: cpd_tt_case("cpd_tt_L3", [10, 9, 8], 3, 74, 1e-5),
     "init_smart": lambda: init_case("init_smart", 61),
     "cpd_smart": lambda: cpd_case("cpd_smart", [14, 12, 10], 3, 62, 1e-5, initialization='smart'),
     "cpd_smart_random": lambda: cpd_case("cpd_smart_random", [14, 12, 10], 3, 63, 1e-5,

@@ -7,6 +7,8 @@ installed here, so this module registers minimal stand-ins:
   ``@njit`` kernels then run as plain Python with identical arithmetic);
 * plotting and display modules become empty namespaces.
 
+The pandas stand-in is removed from ``sys.modules`` again once the reference is
+imported (scikit-learn, which the tensor-train path calls, probes for pandas).
 It also removes the one-second ``time.sleep`` in ``Auxiliar.consistency``
 (Auxiliar.py:76) and replaces ``Compression.sparse_dot_mkl_call``
 (Compression.py:240-258) by the SciPy product ``(Tl @ Tl.T).toarray()``, which is
@@ -75,5 +77,10 @@ def load_reference():
         return (Tl @ Tl.T).toarray()
 
     cmpr.sparse_dot_mkl_call = _dense_gram
+    # the stand-ins for plotting and tables are only needed while the reference
+    # imports; scikit-learn (the reference's randomized SVD of the tensor-train
+    # path) probes sys.modules for a real pandas, so drop the stand-in again
+    for name in ("pandas",):
+        sys.modules.pop(name, None)
     _TFX = tfx
     return tfx

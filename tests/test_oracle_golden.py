@@ -246,3 +246,45 @@ def test_cpd_smart_matches_reference(name):
     assert out.num_steps == int(g["num_steps"])
     assert list(out.stop) == list(g["stop"])
     np.testing.assert_allclose(out.rel_error, float(g["rel_error"]), rtol=1e-6)
+
+
+def test_tt_cores_match_reference():
+    """cpdtt (TensorFox.py:1042-1065) cores and the RNG state after them."""
+    g = load_golden("tt_cores")
+    for k in range(int(g["n"])):
+        T, R = g["T%d" % k], int(g["R%d" % k])
+        np.random.seed(int(g["seed"]) + k)
+        G = orc.cpdtt(T, R)
+        assert np.random.rand() == float(g["after%d" % k])
+        assert len(G) == int(g["ncores%d" % k])
+        for j, c in enumerate(G):
+            np.testing.assert_allclose(c, g["G%d_%d" % (k, j)], rtol=1e-9, atol=1e-11)
+
+
+def congruence(A, B):
+    """Smallest over matched columns of the product over modes of |cos|."""
+    from scipy.optimize import linear_sum_assignment
+    R = A[0].shape[1]
+    C = np.ones((R, R))
+    for a, b in zip(A, B):
+        C *= np.abs((a / np.linalg.norm(a, axis=0)).T @ (b / np.linalg.norm(b, axis=0)))
+    r, c = linear_sum_assignment(-C)
+    return C[r, c].min()
+
+
+@pytest.mark.parametrize("name", ["cpd_tt_L3", "cpd_tt_L4", "cpd_tt_L5"])
+def test_cpd_tt_matches_reference(name):
+    """End to end, the tensor-train path is pinned by its result: the inner TT
+    cores have orthonormal unfoldings, so the MLSVD basis of those modes is
+    arbitrary and last-bit differences in a core rotate the compressed problem
+    (the reference itself lands on the same solution with its columns permuted
+    when a core changes by 1e-15).  The TT-SVD is pinned exactly above."""
+    g = load_golden(name)
+    o = _opts(g)
+    o.method = 'ttcpd'
+    np.random.seed(int(g["seed"]))
+    f, out = orc.cpd(g["T"], int(g["R"]), o)
+    assert abs(out.rel_error - float(g["rel_error"])) <= 1e-2 * float(g["rel_error"])
+    T, R = g["T"], int(g["R"])
+    assert congruence(f, split_x(g["factors"], T.shape, R)) > 0.999
+    assert congruence(f, split_x(g["planted"], T.shape, R)) > 0.999
