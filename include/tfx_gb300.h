@@ -45,13 +45,15 @@ int tfx_dgn_solve(int dtype, const tfx_dgn_problem* h_probs, tfx_dgn_problem* d_
  * step sizes, improvements, gradients; result: [4] stop code, iterations,
  * status, pseudo-inverse fallbacks; info: [5] |T|, best error, 0, sum|T|, 0.
  * options: maxiter, tol, tol_step, tol_improv, tol_grad, symm, factors_norm.
+ * fix_mode: -1, or the mode whose factor stays as given (bicpd of the tensor-
+ * train path, TensorFox.py:658-817; Alternating_Least_Squares.py:64-71, 236-264).
  * The whole solve is one CUDA-graph launch on `stream` (a while-node repeats
  * one iteration until the stop tests fire); work: tfx_als_workspace_bytes()
  * bytes, 256-byte aligned. */
 size_t tfx_als_workspace_bytes(int dtype, int L, const int* dims, int R);
 int tfx_als_solve(int dtype, const void* T, int L, const int* dims, int R, void* x, void* best, double* stats,
-                  int* result, double* info, const tfx_dgn_options* options, void* work, size_t work_bytes,
-                  void* stream);
+                  int* result, double* info, const tfx_dgn_options* options, int fix_mode, void* work,
+                  size_t work_bytes, void* stream);
 
 /* ---- batches of small problems (the rank/stats sweeps, TensorFox.py:820-1039,
  * run cpd on many small tensors): one CTA per problem.

@@ -54,7 +54,7 @@ struct State {
 };
 
 struct Layout {
-  size_t state, G, Hinv, M, gpart, xo, mtt, res, total;
+  size_t state, G, Hinv, M, gpart, xo, xfix, mtt, res, total;
   size_t mtt_bytes;
 };
 
@@ -79,6 +79,7 @@ static Layout layout(int dtype, int L, const int* dims, int R) {
   y.M = o;      o += up256((size_t)maxd * R * es);
   y.gpart = o;  o += up256(nblk * R * R * 8);
   y.xo = o;     o += up256((size_t)nx * es);
+  y.xfix = o;   o += up256((size_t)nx * es);
   y.mtt = o;    o += up256(mtt);
   y.mtt_bytes = mtt;
   y.res = o;    o += up256(tfx_cp_residual_scratch_bytes());
@@ -295,7 +296,8 @@ struct Dims {
 
 template <class T>
 __global__ void __launch_bounds__(NT) k_als_post(T* __restrict__ x, T* __restrict__ xo, Dims sh, int symm,
-                                                 double factors_norm, State* st) {
+                                                 double factors_norm, int fix, const T* __restrict__ xfix,
+                                                 State* st) {
   __shared__ double red[NT / 32];
   __shared__ double nrm[TFX_MAX_ORDER];
   const int tid = threadIdx.x;
@@ -348,6 +350,13 @@ __global__ void __launch_bounds__(NT) k_als_post(T* __restrict__ x, T* __restric
       const int n = sh.d[l] * sh.R;
       for (int e = tid; e < n; e += NT) x[sh.off[l] + e] = sc * x[sh.off[l] + e];
     }
+  }
+  if (fix >= 0 && (symm || factors_norm > 0.0)) {
+    // the fixed factor is restored after the transform
+    // (Alternating_Least_Squares.py:116-121)
+    __syncthreads();
+    const int n = sh.d[fix] * sh.R;
+    for (int e = tid; e < n; e += NT) x[sh.off[fix] + e] = xfix[sh.off[fix] + e];
   }
 }
 
@@ -469,8 +478,8 @@ static int grams_all(const T* x, const Dims& sh, const Layout& y, char* w, cudaS
 // One iteration's launches (the body of the graph's while-node).
 template <class T>
 static int body(int dtype, const T* Tt, const int* dims, T* x, T* best, const Dims& sh, const tfx_dgn_options& op,
-                double* stats, int* result, double* info, const Layout& y, char* w, cudaGraphConditionalHandle cond,
-                cudaStream_t s) {
+                int fix, double* stats, int* result, double* info, const Layout& y, char* w,
+                cudaGraphConditionalHandle cond, cudaStream_t s) {
   const int L = sh.L, R = sh.R;
   State* st = (State*)(w + y.state);
   double* G = (double*)(w + y.G);
@@ -478,6 +487,7 @@ static int body(int dtype, const T* Tt, const int* dims, T* x, T* best, const Di
   T* M = (T*)(w + y.M);
   double* gp = (double*)(w + y.gpart);
   for (int l = 0; l < L; ++l) {
+    if (l == fix) continue;  // bicpd: this factor stays as given
     int r = tfx_mttkrp(dtype, Tt, L, dims, R, x, l, M, w + y.mtt, y.mtt_bytes, s);
     if (r) return r;
     k_als_inv<T><<<1, NT, inv_smem(R), s>>>(G, L, l, R, Hinv, st);
@@ -489,7 +499,7 @@ static int body(int dtype, const T* Tt, const int* dims, T* x, T* best, const Di
     k_als_gram_sum<<<(R * R + 255) / 256, 256, 0, s>>>(gp, nb, R, G + (size_t)l * R * R);
     if ((r = check("als gram sum"))) return r;
   }
-  k_als_post<T><<<1, NT, 0, s>>>(x, (T*)(w + y.xo), sh, op.symm, op.factors_norm, st);
+  k_als_post<T><<<1, NT, 0, s>>>(x, (T*)(w + y.xo), sh, op.symm, op.factors_norm, fix, (const T*)(w + y.xfix), st);
   if (int r = check("als post")) return r;
   if (op.symm || op.factors_norm > 0.0)
     if (int r = grams_all<T>(x, sh, y, w, s)) return r;
@@ -500,7 +510,7 @@ static int body(int dtype, const T* Tt, const int* dims, T* x, T* best, const Di
 
 template <class T>
 static int solve(int dtype, const T* Tt, int L, const int* dims, int R, T* x, T* best, double* stats, int* result,
-                 double* info, const tfx_dgn_options& op, char* w, const Layout& y, cudaStream_t s) {
+                 double* info, const tfx_dgn_options& op, int fix, char* w, const Layout& y, cudaStream_t s) {
   Dims sh;
   sh.L = L;
   sh.R = R;
@@ -522,6 +532,10 @@ static int solve(int dtype, const T* Tt, int L, const int* dims, int R, T* x, T*
   // set-up on the caller's stream: state, x_old, best, |T|, Gramians
   k_als_init<T><<<(int)((sh.nx + 255) / 256), 256, 0, s>>>(x, (T*)(w + y.xo), best, sh.nx, st);
   if (int r = check("als init")) return r;
+  if (fix >= 0) {
+    cudaError_t ce = cudaMemcpyAsync(w + y.xfix, x, (size_t)sh.nx * sizeof(T), cudaMemcpyDeviceToDevice, s);
+    if (ce != cudaSuccess) return tfx_set_cuda_error(ce, "als fixed factor copy");
+  }
   if (int r = tfx_tensor_norms(dtype, Tt, N, st->tn, w + y.res, s)) return r;
   if (int r = grams_all<T>(x, sh, y, w, s)) return r;
 
@@ -548,7 +562,7 @@ static int solve(int dtype, const T* Tt, int L, const int* dims, int R, T* x, T*
         cudaSuccess)
       break;
     capturing = true;
-    status = body<T>(dtype, Tt, dims, x, best, sh, op, stats, result, info, y, w, cond, cs);
+    status = body<T>(dtype, Tt, dims, x, best, sh, op, fix, stats, result, info, y, w, cond, cs);
     cudaGraph_t captured = nullptr;
     e = cudaStreamEndCapture(cs, &captured);
     capturing = false;
@@ -580,8 +594,8 @@ extern "C" size_t tfx_als_workspace_bytes(int dtype, int L, const int* dims, int
 }
 
 extern "C" int tfx_als_solve(int dtype, const void* T, int L, const int* dims, int R, void* x, void* best,
-                             double* stats, int* result, double* info, const tfx_dgn_options* options, void* work,
-                             size_t work_bytes, void* stream) {
+                             double* stats, int* result, double* info, const tfx_dgn_options* options, int fix_mode,
+                             void* work, size_t work_bytes, void* stream) {
   if (!T || !dims || !x || !best || !stats || !result || !info || !options || !work)
     return tfx_set_error(TFX_STATUS_ERR_ARG, "als: null argument");
   if (dtype != TFX_F32 && dtype != TFX_F64) return tfx_set_error(TFX_STATUS_ERR_ARG, "als: dtype");
@@ -590,6 +604,7 @@ extern "C" int tfx_als_solve(int dtype, const void* T, int L, const int* dims, i
   for (int l = 0; l < L; ++l)
     if (dims[l] < 1) return tfx_set_error(TFX_STATUS_ERR_ARG, "als: dimension < 1");
   if (R > als::RMAX) return tfx_set_error(TFX_STATUS_ERR_UNSUPPORTED, "als: rank above 96");
+  if (fix_mode < -1 || fix_mode >= L) return tfx_set_error(TFX_STATUS_ERR_ARG, "als: fix_mode out of range");
   if (options->symm)
     for (int l = 1; l < L; ++l)
       if (dims[l] != dims[0]) return tfx_set_error(TFX_STATUS_ERR_ARG, "als: symm needs equal dimensions");
@@ -599,7 +614,7 @@ extern "C" int tfx_als_solve(int dtype, const void* T, int L, const int* dims, i
   cudaStream_t s = (cudaStream_t)stream;
   if (dtype == TFX_F32)
     return als::solve<float>(dtype, (const float*)T, L, dims, R, (float*)x, (float*)best, stats, result, info,
-                             *options, (char*)work, y, s);
+                             *options, fix_mode, (char*)work, y, s);
   return als::solve<double>(dtype, (const double*)T, L, dims, R, (double*)x, (double*)best, stats, result, info,
-                            *options, (char*)work, y, s);
+                            *options, fix_mode, (char*)work, y, s);
 }

@@ -110,7 +110,7 @@ _EXTRA_SIGNATURES = {
     "tfx_sparse_residual": [_I, _P, _P, _LL, _I, POINTER(c_int), _I, _P, _P, _P, _P],
     "tfx_coo_gram": [_I, _P, _P, _LL, _P, _P, _I, POINTER(c_int), _I, _P, _P, _SZ, _P, _P],
     "tfx_sparse_ttmc": [_I, _P, _P, _LL, _I, POINTER(c_int), POINTER(c_int), _P, _P, _P, _SZ, _P],
-    "tfx_als_solve": [_I, _P, _I, POINTER(c_int), _I, _P, _P, _P, _P, _P, POINTER(DgnOptions), _P, _SZ, _P],
+    "tfx_als_solve": [_I, _P, _I, POINTER(c_int), _I, _P, _P, _P, _P, _P, POINTER(DgnOptions), _I, _P, _SZ, _P],
 }
 _SIZE_FUNCS = {
     "tfx_mode_gram_scratch_bytes": [_I, _LL, _I, _LL],

@@ -26,8 +26,9 @@ def _opts_struct(o):
     return s
 
 
-def als_device(Td, x0, R, options, precision):
-    """ALS on device-resident inputs.  ``x0`` (flat layout) is not modified.
+def als_device(Td, x0, R, options, precision, fix_mode=-1):
+    """ALS on device-resident inputs.  ``x0`` (flat layout) is not modified;
+    ``fix_mode`` >= 0 keeps that factor as given (bicpd).
     Returns ``(x_last, best, stats, result, info)``: device vectors and NumPy
     arrays (stats = errors | step sizes | improvements | gradients)."""
     lib = _lib.load()
@@ -49,7 +50,8 @@ def als_device(Td, x0, R, options, precision):
     _lib.check(lib.tfx_als_solve(dt, ctypes.c_void_p(_dev.ptr(Td)), L, cd, int(R), ctypes.c_void_p(_dev.ptr(x)),
                                  ctypes.c_void_p(_dev.ptr(best)), ctypes.c_void_p(_dev.ptr(stats)),
                                  ctypes.c_void_p(_dev.ptr(result)), ctypes.c_void_p(_dev.ptr(info)),
-                                 ctypes.byref(opt), ctypes.c_void_p(base), nb, ctypes.c_void_p(_dev.stream())))
+                                 ctypes.byref(opt), int(fix_mode), ctypes.c_void_p(base), nb,
+                                 ctypes.c_void_p(_dev.stream())))
     res = result.cpu().numpy()
     _lib.check_solve_status(res)
     return x, best, stats.cpu().numpy(), res, info.cpu().numpy()
@@ -74,8 +76,13 @@ def als(T, factors, R, options=None, precision=None):
     dt = _dev.torch_dtype(prec)
     Td = _dev.to_device(T, dt)
     dims = tuple(int(d) for d in Td.shape)
+    factors = list(factors)
+    fix = -1
+    for l in range(len(factors)):        # [W, l] marks a fixed factor, as in the reference
+        if isinstance(factors[l], list):
+            fix, factors[l] = l, factors[l][0]
     x0 = torch.from_numpy(_dev.flat_factors(factors)).to(device=Td.device, dtype=dt)
-    x, best, stats, res, info = als_device(Td, x0, R, options, prec)
+    x, best, stats, res, info = als_device(Td, x0, R, options, prec, fix)
     n = int(res[1])
     ss, er, im, gr = split_stats(stats, int(options.maxiter), n)
     f = _dev.unflat(x.double().cpu().numpy(), dims, R)

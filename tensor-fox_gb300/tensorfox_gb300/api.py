@@ -234,7 +234,8 @@ def tricpd(T, R, options):
 
 
 def cpd(T, R, options=False):
-    """Drop-in for TensorFox.cpd (TensorFox.py:69-255), methods 'dGN' and 'als'."""
+    """Drop-in for TensorFox.cpd (TensorFox.py:69-255): methods 'dGN', 'als' and
+    (dense tensors) 'ttcpd'."""
     _dev.require_cuda()
     if isinstance(T, list):
         dims_orig = T[2]
@@ -244,4 +245,9 @@ def cpd(T, R, options=False):
     consistency(R, dims_orig, o)
     if o.method in ('dGN', 'als'):
         return tricpd(T, R, o)
-    raise NotImplementedError("method %r is outside the damped Gauss-Newton path" % (o.method,))
+    if o.method == 'ttcpd':
+        if isinstance(T, list):
+            raise NotImplementedError("method 'ttcpd' takes dense tensors on this path")
+        from .tt import cpd_tt
+        return cpd_tt(T, R, o)
+    raise NotImplementedError("method %r" % (o.method,))
