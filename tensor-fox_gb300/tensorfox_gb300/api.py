@@ -235,7 +235,7 @@ def tricpd(T, R, options):
 
 def cpd(T, R, options=False):
     """Drop-in for TensorFox.cpd (TensorFox.py:69-255): methods 'dGN', 'als' and
-    (dense tensors) 'ttcpd'."""
+    'ttcpd'."""
     _dev.require_cuda()
     if isinstance(T, list):
         dims_orig = T[2]
@@ -246,8 +246,6 @@ def cpd(T, R, options=False):
     if o.method in ('dGN', 'als'):
         return tricpd(T, R, o)
     if o.method == 'ttcpd':
-        if isinstance(T, list):
-            raise NotImplementedError("method 'ttcpd' takes dense tensors on this path")
         from .tt import cpd_tt
         return cpd_tt(T, R, o)
     raise NotImplementedError("method %r" % (o.method,))

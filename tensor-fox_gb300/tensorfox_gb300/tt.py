@@ -235,21 +235,42 @@ def highcpd(S, R, options, prec):
 
 
 def cpd_tt(T, R, options):
-    """cpd with method 'ttcpd' on a dense tensor (TensorFox.py:256-365)."""
+    """cpd with method 'ttcpd' (TensorFox.py:256-365), dense or
+    ``[data, idxs, dims]`` input (sparse: the reference's sparse MLSVD, and the
+    final error on the stored entries)."""
     from .api import Output, _precision, sort_dims, unsort_dims
     o = options
-    prec = _precision(T, o)
-    dt = _dev.torch_dtype(prec)
-    shape = tuple(int(d) for d in T.shape)
-    ordering = sort_dims(shape)
-    if isinstance(T, torch.Tensor):
-        Td = T.to(device=_dev.device(), dtype=dt).permute(*[int(i) for i in ordering]).contiguous()
+    sparse_in = isinstance(T, list)
+    if sparse_in:
+        from .sparse import DeviceCOO, mlsvd_sparse_device, sparse_residual_sq
+        data, idxs, dims0 = T
+        data = np.asarray(data, dtype=np.float64)
+        dims0 = np.asarray(dims0)
+        idxs = np.asarray(idxs, dtype=np.int64).reshape(len(data), -1)
+        prec = o.precision if o.precision in ('fp64', 'fp32') else 'fp64'
+        dt = _dev.torch_dtype(prec)
+        ordering = np.argsort(-dims0)
+        dims = [int(d) for d in dims0[ordering]]
+        X = DeviceCOO(data, idxs[:, ordering], dims, dt)
+        Tsize = float(np.linalg.norm(data))
+        tol = o.tol_mlsvd[0] if isinstance(o.tol_mlsvd, list) else o.tol_mlsvd
+        if tol < 0:            # TensorFox.py:275-280
+            o.tol_mlsvd = 1e-16
+        S, Uts, sigmas = mlsvd_sparse_device(X, R, o)
+        core = [int(u.shape[0]) for u in Uts]
     else:
-        Td = _dev.to_device(np.transpose(np.asarray(T), ordering), dt)
-    dims = [int(d) for d in Td.shape]
-    Tsize = float(np.sqrt(kernels.tensor_norms(Td).cpu().numpy()[0]))
-    S, Uts, sigmas, core = mlsvd_device(Td, R, o)
-    core = [int(c) for c in core]
+        prec = _precision(T, o)
+        dt = _dev.torch_dtype(prec)
+        shape = tuple(int(d) for d in T.shape)
+        ordering = sort_dims(shape)
+        if isinstance(T, torch.Tensor):
+            Td = T.to(device=_dev.device(), dtype=dt).permute(*[int(i) for i in ordering]).contiguous()
+        else:
+            Td = _dev.to_device(np.transpose(np.asarray(T), ordering), dt)
+        dims = [int(d) for d in Td.shape]
+        Tsize = float(np.sqrt(kernels.tensor_norms(Td).cpu().numpy()[0]))
+        S, Uts, sigmas, core = mlsvd_device(Td, R, o)
+        core = [int(c) for c in core]
     infl = R > min(core)
     if infl:
         S = _inflate(S, R, core)
@@ -261,8 +282,12 @@ def cpd_tt(T, R, options):
     for l in range(len(dims)):
         U = Uts[l].double().cpu().numpy().T                 # d_l x n_l
         full.append(U @ factors[l])
-    flat = torch.from_numpy(_dev.flat_factors(full)).to(Td.device, dt)
-    r2 = float(kernels.cp_residual_sq(Td, dims, flat, R).cpu().numpy()[0])
+    if sparse_in:            # error on the stored entries (Auxiliar.py:155-159)
+        frm = [torch.from_numpy(np.ascontiguousarray(f)).to(S.device, dt) for f in full]
+        r2 = float(sparse_residual_sq(X, frm).cpu().numpy()[0])
+    else:
+        flat = torch.from_numpy(_dev.flat_factors(full)).to(Td.device, dt)
+        r2 = float(kernels.cp_residual_sq(Td, dims, flat, R).cpu().numpy()[0])
     rel = float(np.sqrt(max(r2, 0.0))) / Tsize
     full = unsort_dims(full, ordering)
     out = Output()

@@ -352,7 +352,27 @@ def cpd_tt_case(name, dims, R, seed, noise, **opts):
          opt_names=np.array(list(opts.keys())), opt_values=np.array([repr(v) for v in opts.values()]))
 
 
+def cpd_tt_sparse_case(name, dims, R, nnz, seed):
+    """cpd with method='ttcpd' on a COO tensor sampled from a planted model."""
+    rng = np.random.default_rng(seed)
+    L = len(dims)
+    lin = rng.choice(int(np.prod(dims)), size=nnz, replace=False)
+    idxs = np.stack(np.unravel_index(lin, dims), axis=1).astype(np.int64)
+    W = [rng.standard_normal((d, R)) for d in dims]
+    model = np.ones((nnz, R))
+    for l in range(L):
+        model *= W[l][idxs[:, l]]
+    data = model.sum(1) + 1e-3 * rng.standard_normal(nnz)
+    o = Opt()
+    o.method = 'ttcpd'
+    np.random.seed(seed)
+    f, out = tfx.cpd([data, idxs, np.array(dims)], R, o)
+    save(name, dims=np.array(dims), R=R, seed=seed, idxs=idxs, data=data,
+         factors=np.concatenate([w.flatten('F') for w in f]), rel_error=out.rel_error, num_steps=out.num_steps)
+
+
 CASES = {
+    "cpd_tt_sparse": lambda: cpd_tt_sparse_case("cpd_tt_sparse", [8, 7, 6, 5], 2, 1680, 75),
     "tt_cores": lambda: tt_case("tt_cores", [((6, 5, 4, 3), 2), ((5, 4, 4, 3, 3), 2), ((7, 6, 5, 4), 3)], 71),
     "cpd_tt_L4": lambda: cpd_tt_case("cpd_tt_L4", [9, 8, 7, 6], 3, 72, 1e-5),
     "cpd_tt_L5": lambda: cpd_tt_case("cpd_tt_L5", [7, 6, 6, 5, 5], 2, 73, 1e-5),

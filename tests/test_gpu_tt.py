@@ -83,3 +83,17 @@ def test_als_fixed_mode_matches_oracle():
         assert st1 == st0 and len(er1) == len(er0)
         np.testing.assert_allclose(er1, er0, rtol=1e-8)
         np.testing.assert_allclose(f1[fl], W[fl], rtol=0, atol=0)
+
+
+def test_cpd_tt_sparse_matches_reference():
+    """method='ttcpd' on [data, idxs, dims] (every entry stored): the sparse
+    MLSVD, the TT path on the dense core, the error on the stored entries."""
+    g = load_golden("cpd_tt_sparse")
+    dims, R = [int(d) for d in g["dims"]], int(g["R"])
+    o = tfx.Options()
+    o.method = 'ttcpd'
+    np.random.seed(int(g["seed"]))
+    f, out = tfx.cpd([g["data"], g["idxs"], np.array(dims)], R, o)
+    ref = float(g["rel_error"])
+    assert abs(out.rel_error - ref) <= 1e-2 * ref
+    assert congruence(f, split_x(g["factors"], dims, R)) > 0.999
