@@ -371,7 +371,31 @@ def cpd_tt_sparse_case(name, dims, R, nnz, seed):
          factors=np.concatenate([w.flatten('F') for w in f]), rel_error=out.rel_error, num_steps=out.num_steps)
 
 
+def consistency_case(name):
+    """Auxiliar.py:24-78: the reference's SystemExit message for each invalid
+    input (an empty string where the input is accepted)."""
+    aux = sys.modules["TensorFox.Auxiliar"]
+    cases = [((3, 3, 3), 2, {}), ((2,) * 13, 2, {}), ((4, 1, 3), 2, {}), ((4, 3, 3), 0, {}), ((4, 3, 3), 2.0, {}),
+             ((4, 3, 3), 10, {}), ((4, 3, 3), 9, {}), ((4, 3, 3, 2), 1, {}), ((4, 4, 4), 2, {"symm": True}),
+             ((4, 3, 4), 2, {"symm": True}), ((4, 3, 3), 2, {"method": "foo"}), ((2,) * 12, 2, {})]
+    msgs = []
+    for dims, R, opts in cases:
+        o = Opt()
+        for k, v in opts.items():
+            setattr(o, k, v)
+        o = tfx.make_options(o)
+        try:
+            aux.consistency(R, dims, o)
+            msgs.append("")
+        except SystemExit as e:
+            msgs.append(str(e))
+    save(name, dims=np.array([repr(c[0]) for c in cases]), ranks=np.array([repr(c[1]) for c in cases]),
+         opts=np.array([repr(c[2]) for c in cases]), msgs=np.array(msgs))
+
+
 CASES = {
+    "consistency": lambda: consistency_case("consistency"),
+    "cpd_overrank": lambda: cpd_case("cpd_overrank", [6, 5, 4], 7, 76, 1e-4),
     "cpd_tt_sparse": lambda: cpd_tt_sparse_case("cpd_tt_sparse", [8, 7, 6, 5], 2, 1680, 75),
     "tt_cores": lambda: tt_case("tt_cores", [((6, 5, 4, 3), 2), ((5, 4, 4, 3, 3), 2), ((7, 6, 5, 4), 3)], 71),
     "cpd_tt_L4": lambda: cpd_tt_case("cpd_tt_L4", [9, 8, 7, 6], 3, 72, 1e-5),

@@ -129,7 +129,8 @@ def _opts(g):
     return o
 
 
-@pytest.mark.parametrize("name", ["cpd_c1_small", "cpd_L4", "cpd_refine", "cpd_smart", "cpd_smart_random"])
+@pytest.mark.parametrize("name", ["cpd_c1_small", "cpd_L4", "cpd_refine", "cpd_smart", "cpd_smart_random",
+                                  "cpd_overrank"])
 def test_cpd_matches_reference(name):
     g = load_golden(name)
     T, R = g["T"], int(g["R"])

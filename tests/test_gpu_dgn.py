@@ -95,3 +95,21 @@ def test_dgn_larger_core_vs_oracle():
         _, ss1, er1, _, _, st1 = tfx.dGN(T, [w.copy() for w in init], R, o)
         assert st1 == st0
         np.testing.assert_allclose(er1, er0, rtol=1e-7)
+
+
+def test_dgn_order12_vs_oracle():
+    """The largest order the reference accepts (12): a 2^12 tensor at rank 2."""
+    rng = np.random.default_rng(12)
+    dims, R = (2,) * 12, 2
+    W = [rng.standard_normal((d, R)) for d in dims]
+    T = orc.cpd2tens(W) + 1e-4 * rng.standard_normal(dims)
+    init = [w + 0.2 * rng.standard_normal(w.shape) for w in W]
+
+    class O:
+        inner_method = 'cg_static'
+        cg_maxiter = 6
+        maxiter = 15
+    _, ss0, er0, _, _, st0 = orc.dGN(T, [w.copy() for w in init], R, orc.make_options(O))
+    _, ss1, er1, _, _, st1 = tfx.dGN(T, [w.copy() for w in init], R, tfx.make_options(O))
+    assert st1 == st0 and len(er1) == len(er0)
+    np.testing.assert_allclose(er1, er0, rtol=1e-7)
