@@ -23,6 +23,13 @@ extern "C" {
 #endif
 
 /* ---- library ------------------------------------------------------------ */
+/* Host memory staging (no reference counterpart: the reference's rank/stats
+ * sweeps hand one tensor at a time to cpd): copies n host buffers src[i] of
+ * bytes[i] bytes to dst + dst_off[i] (dst: host memory, e.g. pinned), split
+ * over `threads` host threads.  Used to send a batch of tensors to the device
+ * in one copy. */
+int tfx_host_gather(const void* const* src, const long long* bytes, const long long* dst_off, int n, void* dst,
+                    int threads);
 const char* tfx_last_error(void);
 long long tfx_launch_count(void); /* kernels enqueued by this library so far */
 int tfx_version(void);

@@ -168,45 +168,65 @@ def cpd_batch(tensors, ranks, options=None, timings=None, tune=True):
     es = 8 if prec == 'fp64' else 4
     dev = _dev.device()
     L = len(tensors[0].shape)
-    shapes, orders = [], []
-    for T, R in zip(tensors, ranks):
-        consistency(int(R), T.shape, o)
-        if len(T.shape) != L:
-            raise ValueError("all tensors of a batch must have the same order")
-        ordering = sort_dims(T.shape)
-        orders.append(ordering)
-        shapes.append([int(T.shape[i]) for i in ordering])
-    if max(max(s) for s in shapes) > 64:
-        raise ValueError("cpd_batch handles dimensions up to 64; use cpd for larger tensors")
-    N = np.array([int(np.prod(s)) for s in shapes], dtype=np.int64)
+    if any(len(T.shape) != L for T in tensors):
+        raise ValueError("all tensors of a batch must have the same order")
+    D = np.array([T.shape for T in tensors], dtype=np.int64)              # (n, L)
     Rs = np.array([int(r) for r in ranks], dtype=np.int64)
-    mins = [[min(int(R), d) for d in s] for s, R in zip(shapes, Rs)]
+    # the input checks of Auxiliar.py:24-78, vectorised; the first problem that
+    # fails is passed to consistency() for the reference's message
+    bad = np.any(D == 1, axis=1) | (Rs < 1) | np.array([type(r) != int and not isinstance(r, np.integer)
+                                                        for r in ranks])
+    if L == 3:
+        bad |= Rs > np.min(np.stack([D[:, 0] * D[:, 1], D[:, 0] * D[:, 2], D[:, 1] * D[:, 2]]), axis=0)
+    if L > 3:
+        bad |= Rs == 1
+    if o.symm:
+        bad |= np.any(D != D[:, :1], axis=1)
+    consistency(int(Rs[0]) if not np.any(bad) else ranks[int(np.argmax(bad))],
+                tuple(int(v) for v in D[int(np.argmax(bad)) if np.any(bad) else 0]), o)
+    if np.any(bad):     # consistency() above raised unless the vector test was stricter
+        raise ValueError("problem %d failed the input checks" % int(np.argmax(bad)))
+    # sort_dims per problem (stable order on ties, as NumPy's argsort of a short array)
+    order_arr = np.argsort(-D, axis=1, kind='stable')
+    S_arr = np.take_along_axis(D, order_arr, axis=1)
+    orders = list(order_arr)
+    shapes = S_arr.tolist()
+    if int(S_arr.max()) > 64:
+        raise ValueError("cpd_batch handles dimensions up to 64; use cpd for larger tensors")
+    N = np.prod(S_arr, axis=1)
+    M_arr = np.minimum(Rs[:, None], S_arr)                                # min(R, d_l)
+    mins = M_arr.tolist()
+
+    def _offsets(sizes, a=64):
+        al = (sizes + a - 1) // a * a
+        return np.concatenate([[0], np.cumsum(al)]).astype(np.int64)
     # one allocation per field, per-problem offsets (elements)
-    t_off = np.concatenate([[0], np.cumsum([_al(v) for v in N])])
-    w_off = np.concatenate([[0], np.cumsum([_al(2 * v) for v in N])])
-    u_sz = [sum(m * d for m, d in zip(mm, s)) for mm, s in zip(mins, shapes)]
-    u_off = np.concatenate([[0], np.cumsum([_al(v) for v in u_sz])])
-    c_sz = [int(np.prod(mm)) for mm in mins]
-    c_off = np.concatenate([[0], np.cumsum([_al(v) for v in c_sz])])
-    s_sz = [sum(mm) for mm in mins]
-    s_off = np.concatenate([[0], np.cumsum([_al(v, 8) for v in s_sz])])
+    t_off = _offsets(N)
+    w_off = _offsets(2 * N)
+    u_off = _offsets(np.sum(M_arr * S_arr, axis=1))
+    c_off = _offsets(np.prod(M_arr, axis=1))
+    s_off = _offsets(np.sum(M_arr, axis=1), 8)
     # pinned staging buffer: each tensor copied as it is (contiguous copies,
     # several host threads), one H2D copy, then the mode permutation of every
     # problem on the device (tfx_batch_permute)
     pinned = torch.empty(int(t_off[-1]), dtype=torch.float64 if prec == 'fp64' else torch.float32, pin_memory=True)
     host = pinned.numpy()
 
-    def _stage(p):
-        T = tensors[p]
+    hd = host.dtype
+    arrs = []
+    for T in tensors:
         a = T.detach().cpu().numpy() if isinstance(T, torch.Tensor) else np.asarray(T)
-        host[t_off[p]:t_off[p] + N[p]] = a.reshape(-1)
-    if n >= 64:   # NumPy copies release the GIL
-        from concurrent.futures import ThreadPoolExecutor
-        with ThreadPoolExecutor(max_workers=min(16, os.cpu_count() or 4)) as ex:
-            list(ex.map(_stage, range(n)))
-    else:
-        for p in range(n):
-            _stage(p)
+        if a.dtype != hd or not a.flags.c_contiguous:
+            a = np.ascontiguousarray(a, dtype=hd)
+        arrs.append(a)
+    srcp = np.array([a.ctypes.data for a in arrs], dtype=np.uint64)
+    nbytes = (N * hd.itemsize).astype(np.int64)
+    doff = (t_off[:-1] * hd.itemsize).astype(np.int64)
+    lib.tfx_host_gather.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p,
+                                    ctypes.c_int]
+    _lib.check(lib.tfx_host_gather(ctypes.c_void_p(srcp.ctypes.data), ctypes.c_void_p(nbytes.ctypes.data),
+                                   ctypes.c_void_p(doff.ctypes.data), n, ctypes.c_void_p(host.ctypes.data),
+                                   min(32, os.cpu_count() or 4)))
     _mark('stage_host')
     Traw = pinned.to(dev, non_blocking=False)
     Tbuf = torch.empty_like(Traw)
@@ -219,8 +239,7 @@ def cpd_batch(tensors, ranks, options=None, timings=None, tune=True):
     bd = np.zeros(n, dtype=_BATCH_DT)
     bd['L'] = L
     bd['R'] = Rs
-    for p in range(n):
-        bd['dims'][p, :L] = shapes[p]
+    bd['dims'][:, :L] = S_arr
     bd['tensor'] = Tbuf.data_ptr() + t_off[:-1] * es
     bd['work'] = work.data_ptr() + w_off[:-1] * es
     bd['work_elems'] = w_off[1:] - w_off[:-1]
@@ -254,10 +273,14 @@ def cpd_batch(tensors, ranks, options=None, timings=None, tune=True):
     _random_starts(core_dims, Rs, x_off, xh)
     X0 = torch.from_numpy(xh).to(device=dev, dtype=dt)
     best = torch.empty_like(X0)
-    ws_b = []
-    for p in range(n):
-        dims_c = (ctypes.c_int * L)(*[int(d) for d in core_dims[p]])
-        ws_b.append(int(lib.tfx_dgn_workspace_bytes(_dev.lib_dtype(prec), L, dims_c, int(Rs[p]))))
+    ws_b, ws_cache = [], {}
+    for p in range(n):       # one query per distinct (core dims, rank)
+        key = (tuple(int(d) for d in core_dims[p]), int(Rs[p]))
+        v = ws_cache.get(key)
+        if v is None:
+            dims_c = (ctypes.c_int * L)(*key[0])
+            v = ws_cache[key] = int(lib.tfx_dgn_workspace_bytes(_dev.lib_dtype(prec), L, dims_c, key[1]))
+        ws_b.append(v)
     ws_off = np.concatenate([[0], np.cumsum([_al(v, 256) for v in ws_b])])
     WS = torch.empty(int(ws_off[-1]), dtype=torch.uint8, device=dev)
     m = int(o.maxiter)
