@@ -296,9 +296,13 @@ __global__ void __launch_bounds__(128, 1)
   const int npair = diag ? 3 : 4;
   const int pa[4] = {0, 0, diag ? 1 : 1, 1};
   const int pb[4] = {diag ? 0 : 2, diag ? 1 : 3, diag ? 1 : 2, 3};
+  // chunks split, split + ksplit, ...: every CTA sweeps the whole contraction
+  // range at the same pace, so the diagonal and off-diagonal super-blocks that
+  // share row tiles read each chunk at about the same time and the second
+  // reader finds it in L2 (contiguous ranges of different lengths per class
+  // read the shared tiles far apart and fetch them from DRAM twice)
   const long long nchunk = P * qchunks;
-  const long long c0 = nchunk * split / ksplit, c1 = nchunk * (split + 1) / ksplit;
-  const int nit = (int)(c1 - c0);
+  const int nit = split < nchunk ? (int)((nchunk - split + ksplit - 1) / ksplit) : 0;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
   if (threadIdx.x == 0) {
@@ -334,7 +338,7 @@ __global__ void __launch_bounds__(128, 1)
         }
       }
       if (*(volatile int*)&S.abort) break;
-      const long long c = c0 + it;
+      const long long c = split + (long long)it * ksplit;
       const int p = (int)(c / qchunks);
       const int q = (int)(c - (long long)p * qchunks) * TCG_BK;
       mbar_expect_tx(&S.full[s2], tx);
