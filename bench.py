@@ -546,6 +546,15 @@ def run_case(case):
             b.launch(gauss_newton.auto_cluster(tuple(S.shape), RANK))
         torch.cuda.synchronize()
         print(json.dumps({"case": case, "result": b.result[0].cpu().numpy().tolist()}))
+    elif case == "residual_tc":
+        # the full-tensor residual of the headline tensor (tcgen05 path), five launches
+        T, W = make_problem()
+        Td = torch.from_numpy(T).cuda()
+        flat = torch.from_numpy(_dev.flat_factors([w.astype(np.float32) for w in W])).cuda().float()
+        for _ in range(5):
+            r = kernels.cp_residual_sq(Td, list(DIMS), flat, RANK)
+        torch.cuda.synchronize()
+        print(json.dumps({"case": case, "res": float(r.cpu()[0])}))
     elif case == "c3_autograd":
         # the c3 CP fit loss, forward + backward, three times
         res = run_autograd(None)
@@ -567,7 +576,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-sparse", action="store_true")
-    ap.add_argument("--case", default=None, help="tc_gram_small | engine_core | c3_autograd | sparse_c5 (profiling workloads)")
+    ap.add_argument("--case", default=None, help="tc_gram_small | engine_core | residual_tc | c3_autograd | sparse_c5 (profiling workloads)")
     args = ap.parse_args()
     if args.case:
         run_case(args.case)

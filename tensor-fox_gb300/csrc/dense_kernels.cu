@@ -1035,6 +1035,14 @@ extern "C" int tfx_flip_signs(int dtype, void* U, int D, int n, void* stream) {
 
 extern "C" size_t tfx_cp_residual_scratch_bytes(void) { return (size_t)8 * (8 * 1024 + 8); }
 
+namespace tfx {
+__global__ void k_nan_if_flag(const int* err, double* out) {
+  if (*err) *out = nan("");
+}
+}  // namespace tfx
+int tfx_cp_residual_tc_launch(const float* T, const int* dims, int R, const float* W, double* partial,
+                              int max_partials, int* err, int* nblocks, cudaStream_t st);
+
 // ---------------------------------------------------------------------------
 // FP32 ||T - [[W]]||^2 as a register-tiled GEMM with the Khatri-Rao operand
 // generated on the fly.  A block owns 256 columns q of the other modes: it
@@ -1180,6 +1188,23 @@ extern "C" int tfx_cp_residual(int dtype, const void* T, int L, const int* dims,
   }
   cudaStream_t st = (cudaStream_t)stream;
   double* partial = (double*)scratch;
+  if (dtype == TFX_F32 && L == 3 && R <= 64) {
+    // tensor-core path (residual_tc.cu); its bounded-wait flag sits in the
+    // scratch's last slot and turns the result into NaN if a wait ran out
+    int* err = (int*)((char*)scratch + tfx_cp_residual_scratch_bytes() - sizeof(double));
+    cudaError_t ce = cudaMemsetAsync(err, 0, sizeof(int), st);
+    if (ce != cudaSuccess) return tfx_set_cuda_error(ce, "cp_residual flag");
+    int nb = 0;
+    const int r = tfx_cp_residual_tc_launch((const float*)T, dims, R, (const float*)W, partial, 8 * 1024, err, &nb, st);
+    if (r == TFX_STATUS_OK) {
+      k_sum_partials<<<1, 32, 0, st>>>(partial, nb, 1, out);
+      int c = check_launch("sum_partials");
+      if (c) return c;
+      k_nan_if_flag<<<1, 1, 0, st>>>(err, out);
+      return check_launch("cp_residual flag");
+    }
+    if (r != TFX_STATUS_ERR_UNSUPPORTED) return r;
+  }
   if (dtype == TFX_F32 && Q0 >= RES_BN && R <= RES_RMAX) {
     const int rows = dims[0] < 64 ? dims[0] : 64;
     const int nw = (rows + 7) / 8;

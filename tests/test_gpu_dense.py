@@ -240,3 +240,17 @@ def test_matmul_f32(M, K, N, tA, tB):
     got = kernels.matmul(dev(A, torch.float32), dev(B, torch.float32), transA=tA, transB=tB).double().cpu().numpy()
     ref = (A.T if tA else A).astype(np.float64) @ (B.T if tB else B).astype(np.float64)
     np.testing.assert_allclose(got, ref, rtol=0, atol=2e-6 * np.sqrt(K) * np.abs(ref).max())
+
+
+@pytest.mark.parametrize("dims,R", [((257, 131, 128), 50), ((129, 129, 256), 64), ((300, 140, 100), 1)])
+def test_cp_residual_tensor_core_path(dims, R):
+    """Large FP32 third-order tensors take the tcgen05 residual (3xTF32 products,
+    partial row and column tiles here): FP32-level agreement with FP64."""
+    rng = np.random.default_rng(8)
+    W = [rng.standard_normal((d, R)).astype(np.float32) for d in dims]
+    M = np.einsum('ir,jr,kr->ijk', *[w.astype(np.float64) for w in W])
+    T = (M + 1e-2 * rng.standard_normal(dims)).astype(np.float32)
+    ref = float(np.sum((T.astype(np.float64) - M) ** 2))
+    x = np.concatenate([w.flatten('F') for w in W]).astype(np.float32)
+    got = float(kernels.cp_residual_sq(dev(T, torch.float32), list(dims), dev(x, torch.float32), R).cpu().numpy()[0])
+    assert abs(got - ref) <= 2e-5 * ref
