@@ -126,9 +126,13 @@ def transform(factors, symm, factors_norm):
     """Symmetrisation / fixed-norm rescaling (Conversion.py:412-444); both default off."""
     L = len(factors)
     if symm:
+        # in place, as in the reference: ``s`` IS factors[0], and afterwards every
+        # entry of the list is the same array.  When the list already holds one
+        # array L times (any dGN iteration after the first), ``s += factors[l]``
+        # doubles it L - 1 times, so the result is 2^(L-1)/L times the array.
         s = factors[0]
         for l in range(1, L):
-            s = s + factors[l]
+            s += factors[l]
         factors[0] = s / L
         for l in range(1, L):
             factors[l] = factors[0]
@@ -314,6 +318,60 @@ def cg_budget(it, L, cg_factor):
     return 1 + (L - 2) * int(cg_factor * np.random.randint(1 + it ** 0.4, 2 + it ** 0.9))
 
 
+def hessian(factors, P1, P2, exact=False):
+    """The reference's Gauss-Newton matrix in the flat point's order
+    (GaussNewton.py:656-701).
+
+    Diagonal blocks ``kron(P1[l], I_{d_l})``; block (l, m), l > m, entry
+    ((l, r, i), (m, s, j)) = ``P2[l, m][r, s] * W_l[i, s] * W_m[j, r]``, where
+    (l, r, i) is position ``sum_dims[l] + r d_l + i`` of the flat point, and
+    block (m, l) its transpose.  That is ``J^T J`` -- except that the reference
+    fills block (l, m) through ``mlinalg.hadamard`` (MultilinearAlgebra.py:276-289),
+    which loops over ``A.shape[0]`` in BOTH indices: only the leading R d_l
+    columns of the block are written, the rest keep the zeros ``H`` starts
+    with.  This truncation is reproduced (``exact=False``).  With d_l > d_m
+    (modes not in decreasing order) the reference indexes past the block; the
+    full block is used then."""
+    L = len(factors)
+    R = factors[0].shape[1]
+    dims = [W.shape[0] for W in factors]
+    sd = sum_dims_of(dims, R)
+    H = np.zeros((sd[-1], sd[-1]))
+    for l in range(L):
+        H[sd[l]:sd[l + 1], sd[l]:sd[l + 1]] = np.kron(P1[l], np.eye(dims[l]))
+        for m in range(l):
+            blk = np.einsum('rs,is,jr->risj', P2[l, m], factors[l], factors[m])
+            blk = blk.reshape(R * dims[l], R * dims[m])
+            if not exact and dims[l] < dims[m]:
+                blk[:, R * dims[l]:] = 0.0
+            H[sd[l]:sd[l + 1], sd[m]:sd[m + 1]] = blk
+            H[sd[m]:sd[m + 1], sd[l]:sd[l + 1]] = blk.T
+    return H
+
+
+def direct(Tl, factors, damp):
+    """The 'direct' inner method (GaussNewton.py:630-653): the damped system
+    ``(J^T J + damp diag(Gamma)) y = grad`` row-scaled by ``M^2`` and solved by a
+    QR factorisation and a triangular solve; ``y = 0`` when that raises."""
+    L = len(factors)
+    R = factors[0].shape[1]
+    dims = [W.shape[0] for W in factors]
+    Gr, P1, P2 = gramians(factors)
+    Gamma, gamma = regularization(P1, dims, R)
+    M = precond(Gamma, gamma, damp, dims)
+    grad = -compute_grad(Tl, factors, P1)
+    H = hessian(factors, P1, P2)
+    Hd = H + damp * np.diag(Gamma)
+    MHd = ((Hd.T) * (M ** 2)).T
+    Mgrad = (M ** 2) * grad
+    try:
+        q, r = np.linalg.qr(MHd)
+        y = np.linalg.solve(r, q.T @ Mgrad)
+    except np.linalg.LinAlgError:
+        y = np.zeros(len(grad))
+    return y, grad
+
+
 def update_gain_ratio(damp, old_error, error, Tsize, old_x, x, grad):
     """Gain ratio (GaussNewton.py:472-487)."""
     num = (Tsize ** 2) * (old_error ** 2 - error ** 2)
@@ -399,7 +457,18 @@ def dGN(T, factors, R, options, budgets=None, trace=None):
     init_damp, maxiter = o.init_damp, o.maxiter
     tol, tol_step, tol_improv, tol_grad = o.tol, o.tol_step, o.tol_improv, o.tol_grad
     L = len(factors)
-    factors = [np.array(W, dtype=np.float64) for W in factors]
+    fix_mode, orig = -1, None
+    factors = list(factors)
+    for l in range(L):           # [W] marks a fixed factor (bicpd), GaussNewton.py:92-99
+        if type(factors[l]) == list:
+            fix_mode = l
+            factors[l] = factors[l][0]
+            orig = np.array(factors[l], dtype=np.float64)
+    # float64 copies that keep the list's aliasing: a list holding one array L
+    # times (a symmetric start) stays that way, which matters to ``x2cpd`` and
+    # ``transform`` (both work in place, as in the reference)
+    copies = {}
+    factors = [copies.setdefault(id(W), np.array(W, dtype=np.float64)) for W in factors]
     dims = T.shape
     Tsize = norm(T)
     error = 1
@@ -419,20 +488,32 @@ def dGN(T, factors, R, options, budgets=None, trace=None):
     for it in range(maxiter):
         old_x, old_error = x, error
         inner = o.inner_method[it] if type(o.inner_method) == list else o.inner_method
-        if budgets is not None:
-            cgmax = int(budgets[it])
-        elif inner == 'cg':
-            cgmax = cg_budget(it, L, o.cg_factor)
-        elif inner == 'cg_static':
-            cgmax = o.cg_maxiter
+        cgmax, itn = 0, 0
+        if inner == 'als':
+            # GaussNewton.py:275-278: one ALS sweep, x = the swept factors, no step
+            factors = als_iteration(Tl, factors, fix_mode)
+            x = cpd2flat(factors)
+            y = np.zeros(R * sum(dims))
+            grad = np.array([np.nan])
+        elif inner == 'direct':
+            y, grad = direct(Tl, factors, damp)
         else:
-            raise NotImplementedError("inner_method " + repr(inner))
-        y, grad, JT_J_grad, itn, residualnorm = cg(Tl, factors, damp, cgmax, o.cg_tol)
+            if budgets is not None:
+                cgmax = int(budgets[it])
+            elif inner == 'cg':
+                cgmax = cg_budget(it, L, o.cg_factor)
+            elif inner == 'cg_static':
+                cgmax = o.cg_maxiter
+            else:
+                raise NotImplementedError("inner_method " + repr(inner))
+            y, grad, JT_J_grad, itn, residualnorm = cg(Tl, factors, damp, cgmax, o.cg_tol)
         x = x + y
         factors = x2cpd(x, factors)
         factors = transform(factors, o.symm, o.factors_norm)
+        if L == 3 and fix_mode >= 0:     # GaussNewton.py:293-297
+            factors[fix_mode] = orig.copy()
         error = fastnorm(Tl[0], cpd2unfold1(factors)) / Tsize
-        if it > 3 and error > o.tol_jump * old_error:
+        if inner in ('cg', 'cg_static') and it > 3 and error > o.tol_jump * old_error:
             x = x - y
             factors, x, y, error = compute_dogleg_steps(Tsize, Tl[0], factors, grad, JT_J_grad,
                                                         x, y, error, damp, o.symm, o.factors_norm)

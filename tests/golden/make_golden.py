@@ -84,8 +84,9 @@ class Opt:
     pass
 
 
-def dgn_case(name, dims, R, seed, noise=1e-3, **opts):
-    """dGN trajectory from an explicit start; 'cg' budgets replayed from a fixed seed."""
+def dgn_case(name, dims, R, seed, noise=1e-3, fix=-1, **opts):
+    """dGN trajectory from an explicit start; 'cg' budgets replayed from a fixed seed.
+    ``fix`` >= 0 passes that factor as ``[W]`` (kept fixed, as bicpd does)."""
     T, W = planted(dims, R, noise, seed)
     rng = np.random.default_rng(seed + 1000)
     init = [w + 0.3 * rng.standard_normal(w.shape) for w in W]
@@ -94,8 +95,11 @@ def dgn_case(name, dims, R, seed, noise=1e-3, **opts):
         setattr(o, k, v)
     o = tfx.make_options(o)
     np.random.seed(seed)
-    bf, ss, er, im, gr, st = gn.dGN(T, [w.copy() for w in init], R, o)
-    save(name, T=T, init_x=np.concatenate([w.flatten('F') for w in init]), R=R, seed=seed,
+    start = [w.copy() for w in init]
+    if fix >= 0:
+        start[fix] = [start[fix]]
+    bf, ss, er, im, gr, st = gn.dGN(T, start, R, o)
+    save(name, T=T, init_x=np.concatenate([w.flatten('F') for w in init]), R=R, seed=seed, fix=fix,
          dims=np.array(dims), best_x=np.concatenate([w.flatten('F') for w in bf]),
          step_sizes=ss, errors=er, improv=im, gradients=gr, stop=st,
          opt_names=np.array(list(opts.keys())), opt_values=np.array([repr(v) for v in opts.values()]))
@@ -417,6 +421,19 @@ CASES = {
     "dgn_cg_L4": lambda: dgn_case("dgn_cg_L4", [6, 5, 5, 4], 3, 13, maxiter=50),
     "dgn_dogleg_L3": lambda: dgn_case("dgn_dogleg_L3", [8, 7, 6], 3, 14, noise=0.2, tol_jump=0.99, maxiter=30),
     "dgn_small_L3": lambda: dgn_case("dgn_small_L3", [4, 4, 3], 2, 15, maxiter=80),
+    "dgn_als_L3": lambda: dgn_case("dgn_als_L3", [9, 8, 7], 3, 16, inner_method='als', maxiter=40),
+    "dgn_als_L4": lambda: dgn_case("dgn_als_L4", [6, 5, 5, 4], 3, 17, inner_method='als', maxiter=40),
+    "dgn_als_fix_L3": lambda: dgn_case("dgn_als_fix_L3", [8, 7, 6], 3, 18, fix=0, inner_method='als', maxiter=30),
+    "dgn_direct_L3": lambda: dgn_case("dgn_direct_L3", [9, 8, 7], 3, 19, inner_method='direct', maxiter=30),
+    "dgn_direct_L4": lambda: dgn_case("dgn_direct_L4", [6, 5, 5, 4], 3, 20, inner_method='direct', maxiter=30),
+    "dgn_direct_fix_L3": lambda: dgn_case("dgn_direct_fix_L3", [8, 7, 6], 3, 24, fix=1, inner_method='direct',
+                                          maxiter=25),
+    "dgn_direct_symm_L3": lambda: dgn_case("dgn_direct_symm_L3", [6, 6, 6], 2, 25, inner_method='direct',
+                                           maxiter=20, symm=True),
+    "dgn_direct_big_L3": lambda: dgn_case("dgn_direct_big_L3", [20, 18, 16], 6, 26, noise=1e-2,
+                                          inner_method='direct', maxiter=15),
+    "dgn_mixed_L3": lambda: dgn_case("dgn_mixed_L3", [9, 8, 7], 3, 27, inner_method=['direct'] * 4 + ['als'] * 26,
+                                     maxiter=30),
     "mlsvd_seq": lambda: mlsvd_case("mlsvd_seq", [20, 15, 12], 4, 21),
     "mlsvd_classic": lambda: mlsvd_case("mlsvd_classic", [18, 14, 11], 3, 22, method='classic'),
     "mlsvd_seq_L4": lambda: mlsvd_case("mlsvd_seq_L4", [10, 9, 8, 7], 3, 23),

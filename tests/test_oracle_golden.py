@@ -72,6 +72,74 @@ def test_dgn_trajectory_matches_reference(name):
     np.testing.assert_allclose(orc.cpd2flat(bf), g["best_x"], rtol=1e-5, atol=1e-8)
 
 
+INNER_CASES = ["dgn_als_L3", "dgn_als_L4", "dgn_als_fix_L3", "dgn_direct_L3", "dgn_direct_L4", "dgn_direct_fix_L3",
+               "dgn_direct_symm_L3", "dgn_direct_big_L3", "dgn_mixed_L3"]
+
+
+def start_of(g):
+    """The starting factors of a golden dGN case, the fixed one wrapped as [W]."""
+    dims, R = [int(d) for d in g["dims"]], int(g["R"])
+    f = split_x(g["init_x"], dims, R)
+    fix = int(g.get("fix", -1))
+    if fix >= 0:
+        f[fix] = [f[fix]]
+    return f
+
+
+@pytest.mark.parametrize("name", INNER_CASES)
+def test_dgn_inner_als_direct_match_reference(name):
+    """dGN with the 'als' and 'direct' inner methods (GaussNewton.py:275-281,
+    630-653), fixed factors included, against the reference's trajectories."""
+    g = load_golden(name)
+    R = int(g["R"])
+    o = _opts(g)
+    bf, ss, er, im, gr, st = orc.dGN(g["T"], start_of(g), R, o)
+    assert st == int(g["stop"])
+    assert len(er) == len(g["errors"])
+    np.testing.assert_allclose(er, g["errors"], rtol=1e-7, atol=1e-13)
+    np.testing.assert_allclose(ss, g["step_sizes"], rtol=1e-6, atol=1e-13)
+    np.testing.assert_allclose(gr, g["gradients"], rtol=1e-6, atol=1e-12)   # NaN for 'als' steps
+    np.testing.assert_allclose(orc.cpd2flat(bf), g["best_x"], rtol=1e-6, atol=1e-9)
+
+
+def test_hessian_is_jtj():
+    """``hessian`` equals J^T J of the CP map, J formed by finite differences."""
+    rng = np.random.default_rng(3)
+    dims, R = (4, 3, 5), 2
+    W = [rng.standard_normal((d, R)) for d in dims]
+    _, P1, P2 = orc.gramians(W)
+    H = orc.hessian(W, P1, P2, exact=True)
+    x = orc.cpd2flat(W)
+    n = len(x)
+    J = np.empty((int(np.prod(dims)), n))
+    for k in range(n):
+        e = np.zeros(n)
+        e[k] = 1.0
+        fp = orc.cpd2tens(split_x(x + 1e-6 * e, dims, R)).ravel()
+        fm = orc.cpd2tens(split_x(x - 1e-6 * e, dims, R)).ravel()
+        J[:, k] = (fp - fm) / 2e-6
+    np.testing.assert_allclose(H, J.T @ J, rtol=1e-6, atol=1e-6)
+
+
+def test_hessian_truncation_rule():
+    """The reference's blocks (l, m), l > m, keep only their leading R d_l
+    columns; with equal dimensions nothing is truncated."""
+    rng = np.random.default_rng(4)
+    R = 2
+    for dims in [(5, 4, 3), (4, 4, 4), (4, 3, 3, 2)]:
+        W = [rng.standard_normal((d, R)) for d in dims]
+        _, P1, P2 = orc.gramians(W)
+        H, J = orc.hessian(W, P1, P2), orc.hessian(W, P1, P2, exact=True)
+        sd = orc.sum_dims_of(dims, R)
+        want = J.copy()
+        for l in range(len(dims)):
+            for m in range(l):
+                want[sd[l]:sd[l + 1], sd[m] + R * dims[l]:sd[m + 1]] = 0.0
+                want[sd[m] + R * dims[l]:sd[m + 1], sd[l]:sd[l + 1]] = 0.0
+        np.testing.assert_array_equal(H, want)
+        assert np.array_equal(H, J) == (len(set(dims)) == 1)
+
+
 def test_dgn_until_first_dogleg():
     """Past a dogleg fallback the reference's path depends on last-bit rounding of
     the error (its first trial re-evaluates the rejected point, so the gain ratio
