@@ -62,6 +62,35 @@ int tfx_als_solve(int dtype, const void* T, int L, const int* dims, int R, void*
                   int* result, double* info, const tfx_dgn_options* options, int fix_mode, void* work,
                   size_t work_bytes, void* stream);
 
+/* One ALS iteration in place on x (flat layout), no error and no stop tests:
+ * the 'als' inner method of dGN (GaussNewton.py:275-278 ->
+ * Alternating_Least_Squares.py:204-264).  work: tfx_als_workspace_bytes(). */
+int tfx_als_sweep(int dtype, const void* T, int L, const int* dims, int R, void* x, int fix_mode, void* work,
+                  size_t work_bytes, void* stream);
+
+/* ---- dGN inner methods outside the engine ('direct', and the update after
+ * every inner step), one host-driven iteration at a time
+ * (GaussNewton.py:254-312 compute_step).
+ * tfx_dgn_direct_step: GaussNewton.py:630-653 direct(): y (FP64, n = R*sum(dims))
+ * solves (H + damp diag(Gamma)) y = grad, H the reference's Gauss-Newton matrix
+ * (GaussNewton.py:656-701, its truncated off-diagonal blocks included), grad
+ * (FP64, flat layout) = -compute_grad at the factors W; LU with partial
+ * pivoting, y = 0 when a pivot is zero.  n <= 24576.  work:
+ * tfx_dgn_direct_workspace_bytes() (about 8 n^2 bytes), 256-byte aligned.
+ * tfx_dgn_step_update: GaussNewton.py:284-297: x += y (from_W = 0) or x = W
+ * (from_W = 1, after tfx_als_sweep); W = x2cpd(x) balanced (Conversion.py:
+ * 21-49, 361-387) and transformed (Conversion.py:412-444); the fix_mode factor
+ * copied back from Wfix.  aliased = 1: the factor list holds one array L times
+ * (after a symmetrising transform), whose in-place semantics are reproduced.
+ * out[4] (device): ||x_new - x||^2, ||x||^2, (x_new - x).(grad + damp (x_new - x))
+ * and max|grad| (the last two NaN when grad is NULL). */
+size_t tfx_dgn_direct_workspace_bytes(int dtype, int L, const int* dims, int R);
+int tfx_dgn_direct_step(int dtype, const void* T, int L, const int* dims, int R, const void* W, double damp,
+                        double* y, double* grad, void* work, size_t work_bytes, void* stream);
+int tfx_dgn_step_update(int dtype, int L, const int* dims, int R, void* x, void* W, const double* y,
+                        const double* grad, double damp, int from_W, int symm, double factors_norm, int aliased,
+                        int fix_mode, const void* Wfix, double* out, void* stream);
+
 /* ---- batches of small problems (the rank/stats sweeps, TensorFox.py:820-1039,
  * run cpd on many small tensors): one CTA per problem.
  * tfx_batch_mlsvd: Compression.py:141-156 (mlsvd 'seq') per problem, modes <= 64;

@@ -475,11 +475,11 @@ static int grams_all(const T* x, const Dims& sh, const Layout& y, char* w, cudaS
   return TFX_STATUS_OK;
 }
 
-// One iteration's launches (the body of the graph's while-node).
+// The mode-by-mode factor updates of one ALS iteration (Alternating_Least_Squares.py:
+// 204-264); G must hold every mode's Gramian on entry and holds them on exit.
 template <class T>
-static int body(int dtype, const T* Tt, const int* dims, T* x, T* best, const Dims& sh, const tfx_dgn_options& op,
-                int fix, double* stats, int* result, double* info, const Layout& y, char* w,
-                cudaGraphConditionalHandle cond, cudaStream_t s) {
+static int sweep(int dtype, const T* Tt, const int* dims, T* x, const Dims& sh, int fix, const Layout& y, char* w,
+                 cudaStream_t s) {
   const int L = sh.L, R = sh.R;
   State* st = (State*)(w + y.state);
   double* G = (double*)(w + y.G);
@@ -499,36 +499,73 @@ static int body(int dtype, const T* Tt, const int* dims, T* x, T* best, const Di
     k_als_gram_sum<<<(R * R + 255) / 256, 256, 0, s>>>(gp, nb, R, G + (size_t)l * R * R);
     if ((r = check("als gram sum"))) return r;
   }
+  return TFX_STATUS_OK;
+}
+
+// One iteration's launches (the body of the graph's while-node).
+template <class T>
+static int body(int dtype, const T* Tt, const int* dims, T* x, T* best, const Dims& sh, const tfx_dgn_options& op,
+                int fix, double* stats, int* result, double* info, const Layout& y, char* w,
+                cudaGraphConditionalHandle cond, cudaStream_t s) {
+  State* st = (State*)(w + y.state);
+  if (int r = sweep<T>(dtype, Tt, dims, x, sh, fix, y, w, s)) return r;
   k_als_post<T><<<1, NT, 0, s>>>(x, (T*)(w + y.xo), sh, op.symm, op.factors_norm, fix, (const T*)(w + y.xfix), st);
   if (int r = check("als post")) return r;
   if (op.symm || op.factors_norm > 0.0)
     if (int r = grams_all<T>(x, sh, y, w, s)) return r;
-  if (int r = tfx_cp_residual(dtype, Tt, L, dims, R, x, &st->res2, w + y.res, s)) return r;
+  if (int r = tfx_cp_residual(dtype, Tt, sh.L, dims, sh.R, x, &st->res2, w + y.res, s)) return r;
   k_als_control<T><<<1, NT, 0, s>>>(x, best, sh.nx, op, stats, result, info, st, cond);
   return check("als control");
+}
+
+static Dims dims_of(int L, const int* dims, int R, long long* N) {
+  Dims sh;
+  sh.L = L;
+  sh.R = R;
+  long long n = 1, acc = 0;
+  for (int l = 0; l < L; ++l) {
+    sh.d[l] = dims[l];
+    sh.off[l] = (int)acc;
+    acc += (long long)dims[l] * R;
+    n *= dims[l];
+  }
+  sh.nx = acc;
+  *N = n;
+  return sh;
+}
+
+template <class T>
+static int set_attributes(int R) {
+  cudaError_t e = cudaFuncSetAttribute(k_als_inv<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)inv_smem(R));
+  if (e != cudaSuccess) return tfx_set_cuda_error(e, "als inverse attribute");
+  const size_t asm_ = ((size_t)R * R + 2 * (size_t)ROWS * R) * sizeof(T);
+  e = cudaFuncSetAttribute(k_als_apply<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)asm_);
+  if (e != cudaSuccess) return tfx_set_cuda_error(e, "als apply attribute");
+  return TFX_STATUS_OK;
+}
+
+// One ALS iteration in place, without the error and the stop tests (the
+// 'als' inner method of dGN, GaussNewton.py:275-278).
+template <class T>
+static int sweep_once(int dtype, const T* Tt, int L, const int* dims, int R, T* x, int fix, char* w, const Layout& y,
+                      cudaStream_t s) {
+  long long N;
+  const Dims sh = dims_of(L, dims, R, &N);
+  if (int r = set_attributes<T>(R)) return r;
+  cudaError_t e = cudaMemsetAsync(w + y.state, 0, sizeof(State), s);
+  if (e != cudaSuccess) return tfx_set_cuda_error(e, "als sweep state");
+  if (int r = grams_all<T>(x, sh, y, w, s)) return r;
+  return sweep<T>(dtype, Tt, dims, x, sh, fix, y, w, s);
 }
 
 template <class T>
 static int solve(int dtype, const T* Tt, int L, const int* dims, int R, T* x, T* best, double* stats, int* result,
                  double* info, const tfx_dgn_options& op, int fix, char* w, const Layout& y, cudaStream_t s) {
-  Dims sh;
-  sh.L = L;
-  sh.R = R;
-  long long N = 1, acc = 0;
-  for (int l = 0; l < L; ++l) {
-    sh.d[l] = dims[l];
-    sh.off[l] = (int)acc;
-    acc += (long long)dims[l] * R;
-    N *= dims[l];
-  }
-  sh.nx = acc;
+  long long N;
+  const Dims sh = dims_of(L, dims, R, &N);
   State* st = (State*)(w + y.state);
-  const size_t ism = inv_smem(R);
-  cudaError_t e = cudaFuncSetAttribute(k_als_inv<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ism);
-  if (e != cudaSuccess) return tfx_set_cuda_error(e, "als inverse attribute");
-  const size_t asm_ = ((size_t)R * R + 2 * (size_t)ROWS * R) * sizeof(T);
-  e = cudaFuncSetAttribute(k_als_apply<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)asm_);
-  if (e != cudaSuccess) return tfx_set_cuda_error(e, "als apply attribute");
+  if (int r = set_attributes<T>(R)) return r;
+  cudaError_t e = cudaSuccess;
   // set-up on the caller's stream: state, x_old, best, |T|, Gramians
   k_als_init<T><<<(int)((sh.nx + 255) / 256), 256, 0, s>>>(x, (T*)(w + y.xo), best, sh.nx, st);
   if (int r = check("als init")) return r;
@@ -617,4 +654,23 @@ extern "C" int tfx_als_solve(int dtype, const void* T, int L, const int* dims, i
                              *options, fix_mode, (char*)work, y, s);
   return als::solve<double>(dtype, (const double*)T, L, dims, R, (double*)x, (double*)best, stats, result, info,
                             *options, fix_mode, (char*)work, y, s);
+}
+
+extern "C" int tfx_als_sweep(int dtype, const void* T, int L, const int* dims, int R, void* x, int fix_mode,
+                             void* work, size_t work_bytes, void* stream) {
+  if (!T || !dims || !x || !work) return tfx_set_error(TFX_STATUS_ERR_ARG, "als sweep: null argument");
+  if (dtype != TFX_F32 && dtype != TFX_F64) return tfx_set_error(TFX_STATUS_ERR_ARG, "als sweep: dtype");
+  if (L < 2 || L > TFX_MAX_ORDER || R < 1) return tfx_set_error(TFX_STATUS_ERR_ARG, "als sweep: order or rank");
+  for (int l = 0; l < L; ++l)
+    if (dims[l] < 1) return tfx_set_error(TFX_STATUS_ERR_ARG, "als sweep: dimension < 1");
+  if (R > als::RMAX) return tfx_set_error(TFX_STATUS_ERR_UNSUPPORTED, "als sweep: rank above 96");
+  if (fix_mode < -1 || fix_mode >= L) return tfx_set_error(TFX_STATUS_ERR_ARG, "als sweep: fix_mode out of range");
+  if (((uintptr_t)work & 255) != 0)
+    return tfx_set_error(TFX_STATUS_ERR_ARG, "als sweep: workspace not 256-byte aligned");
+  const als::Layout y = als::layout(dtype, L, dims, R);
+  if (work_bytes < y.total) return tfx_set_error(TFX_STATUS_ERR_ARG, "als sweep: workspace too small");
+  cudaStream_t s = (cudaStream_t)stream;
+  if (dtype == TFX_F32)
+    return als::sweep_once<float>(dtype, (const float*)T, L, dims, R, (float*)x, fix_mode, (char*)work, y, s);
+  return als::sweep_once<double>(dtype, (const double*)T, L, dims, R, (double*)x, fix_mode, (char*)work, y, s);
 }

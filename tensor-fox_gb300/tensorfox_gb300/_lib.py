@@ -111,6 +111,9 @@ _EXTRA_SIGNATURES = {
     "tfx_coo_gram": [_I, _P, _P, _LL, _P, _P, _I, POINTER(c_int), _I, _P, _P, _SZ, _P, _P],
     "tfx_sparse_ttmc": [_I, _P, _P, _LL, _I, POINTER(c_int), POINTER(c_int), _P, _P, _P, _SZ, _P],
     "tfx_als_solve": [_I, _P, _I, POINTER(c_int), _I, _P, _P, _P, _P, _P, POINTER(DgnOptions), _I, _P, _SZ, _P],
+    "tfx_als_sweep": [_I, _P, _I, POINTER(c_int), _I, _P, _I, _P, _SZ, _P],
+    "tfx_dgn_direct_step": [_I, _P, _I, POINTER(c_int), _I, _P, _D, _P, _P, _P, _SZ, _P],
+    "tfx_dgn_step_update": [_I, _I, POINTER(c_int), _I, _P, _P, _P, _P, _D, _I, _I, _D, _I, _I, _P, _P, _P],
 }
 _SIZE_FUNCS = {
     "tfx_mode_gram_scratch_bytes": [_I, _LL, _I, _LL],
@@ -121,6 +124,7 @@ _SIZE_FUNCS = {
     "tfx_coo_gram_scratch_bytes": [_LL, _I],
     "tfx_sparse_ttmc_scratch_bytes": [_I, _LL, _I, POINTER(c_int)],
     "tfx_als_workspace_bytes": [_I, _I, POINTER(c_int), _I],
+    "tfx_dgn_direct_workspace_bytes": [_I, _I, POINTER(c_int), _I],
 }
 
 

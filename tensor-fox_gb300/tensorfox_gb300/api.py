@@ -139,7 +139,13 @@ def _flat_dev(factors, dtype, device):
     return torch.from_numpy(_dev.flat_factors(factors)).to(device=device, dtype=dtype)
 
 
-def _run_dgn(Td, x0, R, options, prec):
+def _run_dgn(Td, x0, R, options, prec, aliased=False):
+    """dGN on device inputs: the persistent engine for the 'cg'/'cg_static'
+    inner methods, the stepped loop for 'als'/'direct'.  ``aliased``: the
+    reference would hand dGN one factor array L times (a symmetric start)."""
+    from .stepped import uses_stepped, dgn_stepped
+    if uses_stepped(options):
+        return dgn_stepped(Td, x0, R, options, prec, aliased=aliased)
     b = _Batch([Td], [x0], [R], options, prec)
     c = options.cluster or auto_cluster(tuple(Td.shape), R)
     b.launch(c)
@@ -208,7 +214,12 @@ def tricpd(T, R, options):
     else:
         init = starting_point_core(S, core, R, o, vectorized=(prec == 'fp32'))
     x0 = _flat_dev(init, dt, Td.device)
-    best, ss, er, im, gr, st = solve(S, x0, R, o, prec)
+    if o.method == 'als':
+        best, ss, er, im, gr, st = solve(S, x0, R, o, prec)
+    else:
+        # Initialization.py:83: a symmetrising transform leaves one array L times
+        alias = bool(o.symm) and float(o.factors_norm) <= 0 and not isinstance(o.initialization, list)
+        best, ss, er, im, gr, st = solve(S, x0, R, o, prec, aliased=alias)
     Wf = _decompress(Uts, best, core, R)
     if o.refine:
         Wf, ss2, er2, im2, gr2, st2 = solve(Td, Wf, R, o, prec)

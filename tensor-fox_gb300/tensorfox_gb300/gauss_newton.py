@@ -181,7 +181,20 @@ def dGN(T, factors, R, options=None, precision=None):
     dt = _dev.torch_dtype(prec)
     Td = _dev.to_device(T, dt)
     dims = tuple(Td.shape)
+    factors = list(factors)
+    L = len(factors)
+    aliased = L > 1 and all(f is factors[0] for f in factors)   # one array L times (symmetric start)
+    fix = -1
+    for l in range(L):        # [W] marks a fixed factor (bicpd), GaussNewton.py:92-99
+        if isinstance(factors[l], list):
+            fix, factors[l] = l, factors[l][0]
     x0 = torch.from_numpy(_dev.flat_factors(factors)).to(device=Td.device, dtype=dt)
+    from .stepped import uses_stepped, dgn_stepped
+    if uses_stepped(options):
+        best, ss, er, im, gr, st = dgn_stepped(Td, x0, R, options, prec, fix_mode=fix, aliased=aliased)
+        return (_dev.unflat(best.double().cpu().numpy(), dims, R), ss, er, im, gr, st)
+    if fix >= 0:
+        raise NotImplementedError("a fixed factor with the 'cg'/'cg_static' inner methods")
     b = dGN_device(Td, x0, R, options, prec)
     res = b.result[0].cpu().numpy()
     _lib.check_solve_status(res)

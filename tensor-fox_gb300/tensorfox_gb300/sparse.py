@@ -185,7 +185,11 @@ def tricpd_sparse(T, R, options):
     else:
         init = starting_point_core(S, core, R, o)
     x0 = torch.from_numpy(_dev.flat_factors(init)).to(device=S.device, dtype=dt)
-    best, ss, er, im, gr, st = (_run_als if o.method == 'als' else _run_dgn)(S, x0, R, o, prec)
+    if o.method == 'als':
+        best, ss, er, im, gr, st = _run_als(S, x0, R, o, prec)
+    else:
+        alias = bool(o.symm) and float(o.factors_norm) <= 0 and not isinstance(o.initialization, list)
+        best, ss, er, im, gr, st = _run_dgn(S, x0, R, o, prec, aliased=alias)
     Wf = _decompress(Uts, best, core, R)
     factors = _dev.unflat(Wf.double().cpu().numpy(), [int(d) for d in sdims], R)
     # final error on the stored entries (Auxiliar.py:155-159), sorted order

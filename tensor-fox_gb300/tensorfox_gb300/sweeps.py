@@ -33,7 +33,7 @@ import numpy as np
 import torch
 
 from . import _dev, kernels
-from .api import _decompress, _flat_dev, _precision, _run_als, consistency, sort_dims, starting_point_core, cpd
+from .api import _decompress, _flat_dev, _precision, _run_als, _run_dgn, consistency, sort_dims, starting_point_core, cpd
 from .compression import mlsvd_device
 from .gauss_newton import _Batch, _inner_of, auto_cluster
 from .options import make_options
@@ -107,11 +107,17 @@ class _Dense:
         (rel_error, num_steps, factors_flat_device)."""
         n = len(problems)
         L = len(self.dims)
-        if o.method == 'als':
+        from .stepped import uses_stepped
+        stepped = o.method != 'als' and uses_stepped(o)
+        if o.method == 'als' or stepped:
             bests = []
             steps = []
+            alias = stepped and bool(o.symm) and float(o.factors_norm) <= 0 and not isinstance(o.initialization, list)
             for (S, Uts, core, R, x0) in problems:
-                x, ss, er, im, gr, st = _run_als(S, x0, R, o, self.prec)
+                if stepped:
+                    x, ss, er, im, gr, st = _run_dgn(S, x0, R, o, self.prec, aliased=alias)
+                else:
+                    x, ss, er, im, gr, st = _run_als(S, x0, R, o, self.prec)
                 bests.append(x)
                 steps.append(len(ss))
         else:
@@ -128,8 +134,9 @@ class _Dense:
         out = []
         full = [_decompress(p[1], bests[k], p[2], p[3]) for k, p in enumerate(problems)]
         if o.refine:
-            if o.method == 'als':
-                ref = [_run_als(self.Td, f, p[3], o, self.prec) for f, p in zip(full, problems)]
+            if o.method == 'als' or stepped:
+                run = _run_dgn if stepped else _run_als
+                ref = [run(self.Td, f, p[3], o, self.prec) for f, p in zip(full, problems)]
                 for k, r in enumerate(ref):
                     out.append((float(r[2][-1]), steps[k] + len(r[1]), r[0]))
                 return out
