@@ -89,6 +89,9 @@ typedef struct tfx_dgn_options {
   int tile;           /* engine register tile of the small contractions: 1, 2 or 4
                          (16*tile rows and columns per CTA tile); 0 = chosen from
                          the largest dimension or rank of the batch */
+  int aliased;        /* 1: the start's factor list holds one array L times (a
+                         symmetric start, Initialization.py:83); the reference's
+                         in-place x2cpd / transform then act on that one array */
 } tfx_dgn_options;
 
 #ifdef __cplusplus

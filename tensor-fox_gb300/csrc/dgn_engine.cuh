@@ -570,6 +570,9 @@ struct Engine {
   T* sScale;
   double damp, Tsize;
   tfx_dgn_options op;
+  // The reference's factor list holds ONE array L times (after a symmetrising
+  // transform, or a symmetric start); see to_factors.
+  bool aliased;
   // staged operands: full search direction and factors, owned P1/P2 columns
   int stage;
   T *sQf, *sWf, *sP1o, *sP2o;
@@ -1102,7 +1105,42 @@ struct Engine {
   // then transform (Conversion.py:412-444).  Owned columns only, except the
   // factors_norm rescaling which needs a team-wide norm per mode.
   __device__ void to_factors(const T* src, T* dst, bool eq) {
-    if (eq) {
+    if (aliased) {
+      // The reference's x2cpd writes every block of x into the one shared
+      // array, which ends holding the LAST block; balancing then scales it once
+      // per mode (all its column norms are equal), and transform's in-place sum
+      // adds the array to itself L - 1 times before dividing by L
+      // (Conversion.py:21-49, 361-387, 432-437).
+      const int dl = d[L - 1];
+      if (eq) {
+        const int lane = tid & 31, wid = tid >> 5;
+        for (int c = wid; c < ncol; c += TFX_THREADS / 32) {
+          const T* col = src + off[L - 1] + (c0 + c) * dl;
+          Acc<T> s;
+          for (int i = lane; i < dl; i += 32) s.fma_(col[i], col[i]);
+          s.warp_reduce();
+          if (lane == 0) {
+            const double nr = sqrt(s.value());
+            double prod = 1.0;
+            for (int m = 0; m < L; ++m) prod *= nr;
+            sScale[c] = prod != 0.0 ? (T)(pow(prod, 1.0 / (double)L) / nr) : T(1);
+          }
+        }
+        __syncthreads();
+      }
+      for_own([&](int e, int l, int c) {
+        const int i = e - off[l] - (c0 + c) * d[l];
+        T v = src[off[L - 1] + (c0 + c) * dl + i];
+        if (eq)
+          for (int m = 0; m < L; ++m) v = sScale[c] * v;
+        if (op.symm) {
+          for (int m = 1; m < L; ++m) v = v + v;
+          v = v / (T)L;
+        }
+        dst[e] = v;
+      });
+      __syncthreads();
+    } else if (eq) {
       const int lane = tid & 31, wid = tid >> 5;
       for (int p = wid; p < L * ncol; p += TFX_THREADS / 32) {
         const int l = p / ncol, c = p - l * ncol;
@@ -1130,7 +1168,7 @@ struct Engine {
       for_own([&](int e, int l, int c) { dst[e] = src[e]; });
     }
     __syncthreads();
-    if (op.symm) {
+    if (op.symm && !aliased) {
       // all dims equal: W_0 = mean_l W_l, then every mode copies W_0
       const int dd = d[0];
       for (int e = tid; e < ncol * dd; e += TFX_THREADS) {
@@ -1160,6 +1198,8 @@ struct Engine {
       });
       __syncthreads();
     }
+    // symmetrising leaves one array; the fixed-norm rescaling gives each mode its own
+    aliased = (op.symm || aliased) && !(op.factors_norm > 0.0);
   }
 
   // ||T - [[W]]|| / ||T|| (Conversion.py:117-141 + Critical.py:14-22), fused:
@@ -1547,6 +1587,7 @@ __device__ void solve_problem(const tfx_dgn_problem& pb, const tfx_dgn_options& 
   E.cgo.wsl = sp.wsl;
   E.rs1b = (RedScratch<1>*)(smem + sp.rs1b);
   E.sScale = (T*)(smem + sp.sScale);
+  E.aliased = op.aliased != 0;
   // third-order gradient path: every mode <= 64 (the plan), 16-byte slabs
   E.sG3 = (sp.sG3 && pb.L == 3 && ((size_t)pb.dims[1] * pb.dims[2]) % 4 == 0 &&
            (((unsigned long long)pb.tensor) & 15) == 0)

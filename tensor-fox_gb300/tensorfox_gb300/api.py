@@ -146,7 +146,7 @@ def _run_dgn(Td, x0, R, options, prec, aliased=False):
     from .stepped import uses_stepped, dgn_stepped
     if uses_stepped(options):
         return dgn_stepped(Td, x0, R, options, prec, aliased=aliased)
-    b = _Batch([Td], [x0], [R], options, prec)
+    b = _Batch([Td], [x0], [R], options, prec, aliased=aliased)
     c = options.cluster or auto_cluster(tuple(Td.shape), R)
     b.launch(c)
     res = b.result[0].cpu().numpy()

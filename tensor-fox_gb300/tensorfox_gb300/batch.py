@@ -320,6 +320,8 @@ def cpd_batch(tensors, ranks, options=None, timings=None, tune=True):
     opt.init_damp = float(o.init_damp)
     opt.symm = 1 if o.symm else 0
     opt.factors_norm = float(o.factors_norm)
+    # Initialization.py:83: a symmetrising transform of the start leaves one array L times
+    opt.aliased = 1 if (o.symm and float(o.factors_norm) <= 0 and not isinstance(o.initialization, list)) else 0
     cl = int(o.cluster or 1)
     _mark('starts_and_descriptors')
 

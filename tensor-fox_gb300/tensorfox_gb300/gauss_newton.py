@@ -68,7 +68,7 @@ def _cluster_candidates(c, R):
 class _Batch:
     """Device buffers for a set of dGN problems solved in one engine launch."""
 
-    def __init__(self, tensors, xs, R_list, options, precision, budgets=None):
+    def __init__(self, tensors, xs, R_list, options, precision, budgets=None, aliased=False):
         self.precision = precision
         dt = _dev.torch_dtype(precision)
         self.es = 8 if precision == "fp64" else 4
@@ -128,6 +128,7 @@ class _Batch:
         o.symm = 1 if options.symm else 0
         o.factors_norm = float(options.factors_norm)
         o.tile = int(getattr(options, 'tile', None) or 0)
+        o.aliased = 1 if aliased else 0
         self.opts = o
 
     def launch(self, cluster, stream=None):
@@ -159,9 +160,9 @@ def _precision_of(T, options):
     return 'fp64' if np.asarray(T).dtype == np.float64 else 'fp32'
 
 
-def dGN_device(Td, x0d, R, options, precision, cluster=None):
+def dGN_device(Td, x0d, R, options, precision, cluster=None, aliased=False):
     """Runs the engine on device-resident inputs; returns device results."""
-    b = _Batch([Td], [x0d], [R], options, precision)
+    b = _Batch([Td], [x0d], [R], options, precision, aliased=aliased)
     c = cluster if cluster is not None else (options.cluster or auto_cluster(Td.shape, R))
     b.launch(c)
     return b
@@ -195,7 +196,9 @@ def dGN(T, factors, R, options=None, precision=None):
         return (_dev.unflat(best.double().cpu().numpy(), dims, R), ss, er, im, gr, st)
     if fix >= 0:
         raise NotImplementedError("a fixed factor with the 'cg'/'cg_static' inner methods")
-    b = dGN_device(Td, x0, R, options, prec)
+    if aliased and len(set(dims)) != 1:
+        raise ValueError("one factor array for every mode needs equal dimensions")
+    b = dGN_device(Td, x0, R, options, prec, aliased=aliased)
     res = b.result[0].cpu().numpy()
     _lib.check_solve_status(res)
     stats = b.stats[0].cpu().numpy()

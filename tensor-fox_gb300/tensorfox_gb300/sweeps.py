@@ -122,8 +122,9 @@ class _Dense:
                 steps.append(len(ss))
         else:
             caps = _draw_caps(o, L, n)
+            alias = bool(o.symm) and float(o.factors_norm) <= 0 and not isinstance(o.initialization, list)
             b = _Batch([p[0] for p in problems], [p[4] for p in problems], [p[3] for p in problems], o, self.prec,
-                       budgets=list(caps))
+                       budgets=list(caps), aliased=alias)
             c = o.cluster or min(auto_cluster(tuple(p[2]), p[3]) for p in problems)
             b.launch(c)
             res = b.result.cpu().numpy()

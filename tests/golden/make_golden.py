@@ -84,22 +84,29 @@ class Opt:
     pass
 
 
-def dgn_case(name, dims, R, seed, noise=1e-3, fix=-1, **opts):
+def dgn_case(name, dims, R, seed, noise=1e-3, fix=-1, alias=False, symmetric=False, **opts):
     """dGN trajectory from an explicit start; 'cg' budgets replayed from a fixed seed.
-    ``fix`` >= 0 passes that factor as ``[W]`` (kept fixed, as bicpd does)."""
+    ``fix`` >= 0 passes that factor as ``[W]`` (kept fixed, as bicpd does);
+    ``alias`` passes ONE array for every mode (as a symmetric start is);
+    ``symmetric`` plants a symmetric tensor."""
     T, W = planted(dims, R, noise, seed)
+    if symmetric:
+        T = cnv.cpd2tens([W[0]] * len(dims)) + noise * np.random.default_rng(seed + 7).standard_normal(dims)
+        W = [W[0]] * len(dims)
     rng = np.random.default_rng(seed + 1000)
     init = [w + 0.3 * rng.standard_normal(w.shape) for w in W]
+    if alias:
+        init = [init[0]] * len(dims)
     o = Opt()
     for k, v in opts.items():
         setattr(o, k, v)
     o = tfx.make_options(o)
     np.random.seed(seed)
-    start = [w.copy() for w in init]
+    start = [init[0].copy()] * len(dims) if alias else [w.copy() for w in init]
     if fix >= 0:
         start[fix] = [start[fix]]
     bf, ss, er, im, gr, st = gn.dGN(T, start, R, o)
-    save(name, T=T, init_x=np.concatenate([w.flatten('F') for w in init]), R=R, seed=seed, fix=fix,
+    save(name, T=T, init_x=np.concatenate([w.flatten('F') for w in init]), R=R, seed=seed, fix=fix, alias=int(alias),
          dims=np.array(dims), best_x=np.concatenate([w.flatten('F') for w in bf]),
          step_sizes=ss, errors=er, improv=im, gradients=gr, stop=st,
          opt_names=np.array(list(opts.keys())), opt_values=np.array([repr(v) for v in opts.values()]))
@@ -117,8 +124,11 @@ def mlsvd_case(name, dims, R, seed, method='seq', noise=1e-2):
          method=method)
 
 
-def cpd_case(name, dims, R, seed, noise, **opts):
+def cpd_case(name, dims, R, seed, noise, symmetric=False, **opts):
     T, W = planted(dims, R, noise, seed)
+    if symmetric:
+        T = cnv.cpd2tens([W[0]] * len(dims)) + noise * np.random.default_rng(seed + 7).standard_normal(dims)
+        W = [W[0]] * len(dims)
     o = Opt()
     for k, v in opts.items():
         setattr(o, k, v)
@@ -432,6 +442,18 @@ CASES = {
                                            maxiter=20, symm=True),
     "dgn_direct_big_L3": lambda: dgn_case("dgn_direct_big_L3", [20, 18, 16], 6, 26, noise=1e-2,
                                           inner_method='direct', maxiter=15),
+    "dgn_symm_L3": lambda: dgn_case("dgn_symm_L3", [7, 7, 7], 3, 28, symmetric=True, inner_method='cg_static',
+                                    cg_maxiter=6, maxiter=25, symm=True),
+    "dgn_symm_alias_L3": lambda: dgn_case("dgn_symm_alias_L3", [7, 7, 7], 3, 29, symmetric=True, alias=True,
+                                          inner_method='cg_static', cg_maxiter=6, maxiter=25, symm=True),
+    "dgn_symm_norm_L3": lambda: dgn_case("dgn_symm_norm_L3", [6, 6, 6], 2, 30, symmetric=True, alias=True,
+                                         inner_method='cg_static', cg_maxiter=6, maxiter=20, symm=True,
+                                         factors_norm=3.0),
+    "dgn_symm_direct_alias_L3": lambda: dgn_case("dgn_symm_direct_alias_L3", [6, 6, 6], 2, 34, symmetric=True,
+                                                 alias=True, inner_method='direct', maxiter=15, symm=True),
+    "cpd_symm": lambda: cpd_case("cpd_symm", [10, 10, 10], 3, 35, 1e-4, symmetric=True, symm=True, maxiter=60),
+    "cpd_symm_direct": lambda: cpd_case("cpd_symm_direct", [8, 8, 8], 2, 36, 1e-4, symmetric=True, symm=True,
+                                        inner_method='direct', maxiter=30),
     "dgn_mixed_L3": lambda: dgn_case("dgn_mixed_L3", [9, 8, 7], 3, 27, inner_method=['direct'] * 4 + ['als'] * 26,
                                      maxiter=30),
     "mlsvd_seq": lambda: mlsvd_case("mlsvd_seq", [20, 15, 12], 4, 21),

@@ -130,7 +130,7 @@ def _opts(g):
 
 
 @pytest.mark.parametrize("name", ["cpd_c1_small", "cpd_L4", "cpd_refine", "cpd_smart", "cpd_smart_random",
-                                  "cpd_overrank"])
+                                  "cpd_overrank", "cpd_symm", "cpd_symm_direct"])
 def test_cpd_matches_reference(name):
     g = load_golden(name)
     T, R = g["T"], int(g["R"])

@@ -113,3 +113,28 @@ def test_dgn_order12_vs_oracle():
     _, ss1, er1, _, _, st1 = tfx.dGN(T, [w.copy() for w in init], R, tfx.make_options(O))
     assert st1 == st0 and len(er1) == len(er0)
     np.testing.assert_allclose(er1, er0, rtol=1e-7)
+
+
+def _start(g):
+    dims, R = [int(d) for d in g["dims"]], int(g["R"])
+    f = split_x(g["init_x"], dims, R)
+    if "alias" in g and int(g["alias"]):
+        return [f[0]] * len(dims)     # one array for every mode
+    return f
+
+
+@pytest.mark.parametrize("name", ["dgn_symm_L3", "dgn_symm_alias_L3", "dgn_symm_norm_L3"])
+@pytest.mark.parametrize("cluster", [1, 2])
+def test_dgn_symm_matches_reference(name, cluster):
+    """symm=True on the engine: the reference's in-place x2cpd / transform on a
+    factor list that holds one array L times (a symmetric start, then every
+    iteration after a symmetrising transform) reproduced, fixed norm included."""
+    g = load_golden(name)
+    dims, R = [int(d) for d in g["dims"]], int(g["R"])
+    o = _opts(g, tfx)
+    o.cluster = cluster
+    bf, ss, er, im, gr, st = tfx.dGN(g["T"], _start(g), R, o)
+    assert st == int(g["stop"])
+    assert len(er) == len(g["errors"])
+    np.testing.assert_allclose(er, g["errors"], rtol=1e-6, atol=1e-12)
+    np.testing.assert_allclose(ss, g["step_sizes"], rtol=1e-5, atol=1e-12)

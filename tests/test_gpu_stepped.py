@@ -11,7 +11,7 @@ pytestmark = pytest.mark.gpu
 tfx = pytest.importorskip("tensorfox_gb300")
 
 INNER_CASES = ["dgn_als_L3", "dgn_als_L4", "dgn_als_fix_L3", "dgn_direct_L3", "dgn_direct_L4", "dgn_direct_fix_L3",
-               "dgn_direct_symm_L3", "dgn_direct_big_L3", "dgn_mixed_L3"]
+               "dgn_direct_symm_L3", "dgn_direct_big_L3", "dgn_mixed_L3", "dgn_symm_direct_alias_L3"]
 
 
 def _opts(g, mod):
@@ -24,6 +24,8 @@ def _opts(g, mod):
 def _start(g):
     dims, R = [int(d) for d in g["dims"]], int(g["R"])
     f = split_x(g["init_x"], dims, R)
+    if "alias" in g and int(g["alias"]):
+        return [f[0]] * len(dims)     # one array for every mode
     fix = int(g["fix"]) if "fix" in g else -1
     if fix >= 0:
         f[fix] = [f[fix]]

@@ -73,13 +73,16 @@ def test_dgn_trajectory_matches_reference(name):
 
 
 INNER_CASES = ["dgn_als_L3", "dgn_als_L4", "dgn_als_fix_L3", "dgn_direct_L3", "dgn_direct_L4", "dgn_direct_fix_L3",
-               "dgn_direct_symm_L3", "dgn_direct_big_L3", "dgn_mixed_L3"]
+               "dgn_direct_symm_L3", "dgn_direct_big_L3", "dgn_mixed_L3", "dgn_symm_direct_alias_L3"]
+SYMM_CASES = ["dgn_symm_L3", "dgn_symm_alias_L3", "dgn_symm_norm_L3"]
 
 
 def start_of(g):
     """The starting factors of a golden dGN case, the fixed one wrapped as [W]."""
     dims, R = [int(d) for d in g["dims"]], int(g["R"])
     f = split_x(g["init_x"], dims, R)
+    if int(g.get("alias", 0)):
+        return [f[0]] * len(dims)     # one array for every mode
     fix = int(g.get("fix", -1))
     if fix >= 0:
         f[fix] = [f[fix]]
@@ -100,6 +103,21 @@ def test_dgn_inner_als_direct_match_reference(name):
     np.testing.assert_allclose(ss, g["step_sizes"], rtol=1e-6, atol=1e-13)
     np.testing.assert_allclose(gr, g["gradients"], rtol=1e-6, atol=1e-12)   # NaN for 'als' steps
     np.testing.assert_allclose(orc.cpd2flat(bf), g["best_x"], rtol=1e-6, atol=1e-9)
+
+
+@pytest.mark.parametrize("name", SYMM_CASES)
+def test_dgn_symm_matches_reference(name):
+    """symm=True with the CG inner method: the reference's in-place transform
+    on a list that holds one array L times (a symmetric start, or any
+    iteration after the first) is part of the trajectory."""
+    g = load_golden(name)
+    R = int(g["R"])
+    np.random.seed(int(g["seed"]))
+    bf, ss, er, im, gr, st = orc.dGN(g["T"], start_of(g), R, _opts(g))
+    assert st == int(g["stop"])
+    assert len(er) == len(g["errors"])
+    np.testing.assert_allclose(er, g["errors"], rtol=1e-7, atol=1e-13)
+    np.testing.assert_allclose(ss, g["step_sizes"], rtol=1e-6, atol=1e-13)
 
 
 def test_hessian_is_jtj():
@@ -187,7 +205,7 @@ def test_mlsvd_matches_reference(name):
     np.testing.assert_allclose(S, g["S"], rtol=1e-8, atol=1e-9)
 
 
-@pytest.mark.parametrize("name", ["cpd_c1_small", "cpd_L4", "cpd_refine"])
+@pytest.mark.parametrize("name", ["cpd_c1_small", "cpd_L4", "cpd_refine", "cpd_symm", "cpd_symm_direct"])
 def test_cpd_matches_reference(name):
     g = load_golden(name)
     o = _opts(g)
