@@ -92,6 +92,9 @@ typedef struct tfx_dgn_options {
   int aliased;        /* 1: the start's factor list holds one array L times (a
                          symmetric start, Initialization.py:83); the reference's
                          in-place x2cpd / transform then act on that one array */
+  int fixed;          /* 1 + the mode whose factor is put back after every step
+                         (bicpd, third order, GaussNewton.py:92-99, 293-297);
+                         0 = none */
 } tfx_dgn_options;
 
 #ifdef __cplusplus

@@ -1063,17 +1063,19 @@ def inflate(T, R, dims):
 def bicpd(T, R, fixed, options):
     """Third-order CPD with one factor fixed (TensorFox.py:658-817): MLSVD of T,
     a random start whose fixed factor is replaced by the projection of the given
-    one, ALS (bi_method 'als') on the core, decompression.  Returns
+    one, ALS (bi_method 'als') or dGN with the options' inner method (any other
+    bi_method, TensorFox.py:762-767) on the core, decompression.  Returns
     (X, Y, Z, output) in T's own mode order (no sort_dims)."""
     o = options
-    if o.bi_method_parameters[0] != 'als':
-        raise NotImplementedError("bicpd with bi_method " + repr(o.bi_method_parameters[0]))
     Tsize = norm(T)
     S, U, T1, _ = mlsvd(T, Tsize, R, o)
     f = starting_point(S, U, R, [0, 1, 2], o)
     W, fl = fixed
     f[fl] = [U[fl].T @ W, fl]
-    f, ss, er, im, gr, st = als(S, f, R, o)
+    if o.bi_method_parameters[0] == 'als':
+        f, ss, er, im, gr, st = als(S, f, R, o)
+    else:
+        f, ss, er, im, gr, st = dGN(S, f, R, o)
     out = [None, None, None]
     for l in range(3):
         out[l] = W if l == fl else U[l] @ f[l]

@@ -31,6 +31,9 @@ extern "C" int tfx_dgn_solve(int dtype, const tfx_dgn_problem* h_probs, tfx_dgn_
       maxd = q.dims[l] > maxd ? q.dims[l] : maxd;
     }
     if (n > (1LL << 40)) return tfx_set_error(TFX_STATUS_ERR_ARG, "tensor too large");
+    if (op->fixed < 0 || op->fixed > q.L) return tfx_set_error(TFX_STATUS_ERR_ARG, "fixed mode out of range");
+    if (op->fixed > 0 && (op->symm || op->aliased))
+      return tfx_set_error(TFX_STATUS_ERR_UNSUPPORTED, "a fixed factor with symm");
     if (op->symm || op->aliased) {
       for (int l = 1; l < q.L; ++l)
         if (q.dims[l] != q.dims[0]) return tfx_set_error(TFX_STATUS_ERR_ARG, "symm (or one factor array for every mode) needs equal dims");

@@ -1681,6 +1681,15 @@ __device__ void solve_problem(const tfx_dgn_problem& pb, const tfx_dgn_options& 
     });
     __syncthreads();
     E.to_factors(E.xn, E.W, true);
+    if (op.fixed > 0 && E.L == 3) {
+      // bicpd: the fixed factor is put back after every step (GaussNewton.py:
+      // 293-297); the dogleg trials do not (GaussNewton.py:737-742)
+      const int fm = op.fixed - 1;
+      E.for_own([&](int e, int l, int c) {
+        if (l == fm) E.W[e] = x0[e];
+      });
+      __syncthreads();
+    }
     E.tm.sync();
     E.stage_W();
     tick(3);

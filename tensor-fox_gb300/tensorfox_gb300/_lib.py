@@ -38,7 +38,7 @@ class DgnOptions(ctypes.Structure):
     _fields_ = [("maxiter", c_int), ("tol", c_double), ("tol_step", c_double), ("tol_improv", c_double),
                 ("tol_grad", c_double), ("tol_jump", c_double), ("cg_tol", c_double),
                 ("init_damp", c_double), ("use_damp_sched", c_int), ("symm", c_int),
-                ("factors_norm", c_double), ("tile", c_int), ("aliased", c_int)]
+                ("factors_norm", c_double), ("tile", c_int), ("aliased", c_int), ("fixed", c_int)]
 
 
 _LIB = None

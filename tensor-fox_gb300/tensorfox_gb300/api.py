@@ -139,14 +139,15 @@ def _flat_dev(factors, dtype, device):
     return torch.from_numpy(_dev.flat_factors(factors)).to(device=device, dtype=dtype)
 
 
-def _run_dgn(Td, x0, R, options, prec, aliased=False):
+def _run_dgn(Td, x0, R, options, prec, aliased=False, fix_mode=-1):
     """dGN on device inputs: the persistent engine for the 'cg'/'cg_static'
     inner methods, the stepped loop for 'als'/'direct'.  ``aliased``: the
-    reference would hand dGN one factor array L times (a symmetric start)."""
+    reference would hand dGN one factor array L times (a symmetric start);
+    ``fix_mode`` >= 0: that factor is put back after every step (bicpd)."""
     from .stepped import uses_stepped, dgn_stepped
     if uses_stepped(options):
-        return dgn_stepped(Td, x0, R, options, prec, aliased=aliased)
-    b = _Batch([Td], [x0], [R], options, prec, aliased=aliased)
+        return dgn_stepped(Td, x0, R, options, prec, fix_mode=fix_mode, aliased=aliased)
+    b = _Batch([Td], [x0], [R], options, prec, aliased=aliased, fix_mode=fix_mode)
     c = options.cluster or auto_cluster(tuple(Td.shape), R)
     b.launch(c)
     res = b.result[0].cpu().numpy()

@@ -68,7 +68,7 @@ def _cluster_candidates(c, R):
 class _Batch:
     """Device buffers for a set of dGN problems solved in one engine launch."""
 
-    def __init__(self, tensors, xs, R_list, options, precision, budgets=None, aliased=False):
+    def __init__(self, tensors, xs, R_list, options, precision, budgets=None, aliased=False, fix_mode=-1):
         self.precision = precision
         dt = _dev.torch_dtype(precision)
         self.es = 8 if precision == "fp64" else 4
@@ -129,6 +129,7 @@ class _Batch:
         o.factors_norm = float(options.factors_norm)
         o.tile = int(getattr(options, 'tile', None) or 0)
         o.aliased = 1 if aliased else 0
+        o.fixed = int(fix_mode) + 1
         self.opts = o
 
     def launch(self, cluster, stream=None):
@@ -160,9 +161,9 @@ def _precision_of(T, options):
     return 'fp64' if np.asarray(T).dtype == np.float64 else 'fp32'
 
 
-def dGN_device(Td, x0d, R, options, precision, cluster=None, aliased=False):
+def dGN_device(Td, x0d, R, options, precision, cluster=None, aliased=False, fix_mode=-1):
     """Runs the engine on device-resident inputs; returns device results."""
-    b = _Batch([Td], [x0d], [R], options, precision, aliased=aliased)
+    b = _Batch([Td], [x0d], [R], options, precision, aliased=aliased, fix_mode=fix_mode)
     c = cluster if cluster is not None else (options.cluster or auto_cluster(Td.shape, R))
     b.launch(c)
     return b
@@ -194,11 +195,9 @@ def dGN(T, factors, R, options=None, precision=None):
     if uses_stepped(options):
         best, ss, er, im, gr, st = dgn_stepped(Td, x0, R, options, prec, fix_mode=fix, aliased=aliased)
         return (_dev.unflat(best.double().cpu().numpy(), dims, R), ss, er, im, gr, st)
-    if fix >= 0:
-        raise NotImplementedError("a fixed factor with the 'cg'/'cg_static' inner methods")
     if aliased and len(set(dims)) != 1:
         raise ValueError("one factor array for every mode needs equal dimensions")
-    b = dGN_device(Td, x0, R, options, prec, aliased=aliased)
+    b = dGN_device(Td, x0, R, options, prec, aliased=aliased, fix_mode=fix)
     res = b.result[0].cpu().numpy()
     _lib.check_solve_status(res)
     stats = b.stats[0].cpu().numpy()

@@ -5,8 +5,9 @@ A tensor of order L is compressed by the MLSVD, split by a TT-SVD into the
 cores d_0 x R, R x d_1 x R, ..., R x d_{L-1}; the first inner core gets a full
 third-order CPD (``tricpd``, best of ``options.trials``), every further core a
 CPD whose first factor is fixed to pinv(Z^T) of the previous core's last factor
-(``bicpd``, ALS with a fixed mode on the device), and the factors of the tensor
-are assembled from the cores' CPDs.
+(``bicpd``: ALS with a fixed mode when bi_method is 'als', else dGN with the
+fixed factor put back after every step), and the factors of the tensor are
+assembled from the cores' CPDs.
 
 The TT-SVD runs on the device.  Every unfolding is kept column-major, so the
 reference's Fortran-order reshapes cost nothing: a column-major (rows x cols)
@@ -102,14 +103,13 @@ def _inflate(S, R, dims):
 
 def bicpd(Td, R, fixed, options, prec):
     """Third-order CPD of the device tensor Td with the factor ``fixed = [W, l]``
-    kept (TensorFox.py:658-817), ALS on the MLSVD core.  Returns
-    (X, Y, Z, output) as NumPy arrays in Td's mode order."""
-    from .api import Output, starting_point_core
+    kept (TensorFox.py:658-817) on the MLSVD core: ALS when bi_method is 'als'
+    (the last iterate), else dGN with the options' inner method (the best
+    iterate).  Returns (X, Y, Z, output) as NumPy arrays in Td's mode order."""
+    from .api import Output, starting_point_core, _run_dgn
     from .als import als_device
     o = options
-    if o.bi_method_parameters[0] != 'als':
-        raise NotImplementedError("bicpd with bi_method %r: the device path solves the cores by ALS"
-                                  % (o.bi_method_parameters[0],))
+    use_als = o.bi_method_parameters[0] == 'als'
     dt = _dev.torch_dtype(prec)
     dims = [int(d) for d in Td.shape]
     Tsize = float(np.sqrt(kernels.tensor_norms(Td).cpu().numpy()[0]))
@@ -119,8 +119,15 @@ def bicpd(Td, R, fixed, options, prec):
     Wd = torch.from_numpy(np.asarray(W, dtype=np.float64)).to(Td.device, dt)
     init[fl] = kernels.matmul(Uts[fl], Wd).double().cpu().numpy()
     x0 = torch.from_numpy(_dev.flat_factors(init)).to(Td.device, dt)
-    x, best, stats, res, info = als_device(S, x0, R, o, prec, fl)
-    n = int(res[1])
+    if use_als:
+        x, best, stats, res, info = als_device(S, x0, R, o, prec, fl)
+        n = int(res[1])
+        m = int(o.maxiter)
+        ss, er, im, gr, st = (stats[m:m + n].copy(), stats[:n].copy(), stats[2 * m:2 * m + n].copy(),
+                              stats[3 * m:3 * m + n].copy(), int(res[0]))
+    else:
+        x, ss, er, im, gr, st = _run_dgn(S, x0, R, o, prec, fix_mode=fl)
+        n = len(er)
     xs = x.double().cpu().numpy()
     out, s = [], 0
     for l in range(3):
@@ -138,12 +145,11 @@ def bicpd(Td, R, fixed, options, prec):
     op.num_steps = n
     op.rel_error = float(np.sqrt(max(r2, 0.0))) / Tsize
     op.accuracy = max(0, 100 * (1 - op.rel_error))
-    m = int(o.maxiter)
-    op.errors = [stats[:n].copy(), np.array([0])]
-    op.step_sizes = [stats[m:m + n].copy(), np.array([0])]
-    op.improv = [stats[2 * m:2 * m + n].copy(), np.array([0])]
-    op.gradients = [stats[3 * m:3 * m + n].copy(), np.array([0])]
-    op.stop = [int(res[0]), 5]
+    op.errors = [er, np.array([0])]
+    op.step_sizes = [ss, np.array([0])]
+    op.improv = [im, np.array([0])]
+    op.gradients = [gr, np.array([0])]
+    op.stop = [st, 5]
     op.options = o
     return out[0], out[1], out[2], op
 

@@ -414,6 +414,11 @@ CASES = {
     "tt_cores": lambda: tt_case("tt_cores", [((6, 5, 4, 3), 2), ((5, 4, 4, 3, 3), 2), ((7, 6, 5, 4), 3)], 71),
     "cpd_tt_L4": lambda: cpd_tt_case("cpd_tt_L4", [9, 8, 7, 6], 3, 72, 1e-5),
     "cpd_tt_L5": lambda: cpd_tt_case("cpd_tt_L5", [7, 6, 6, 5, 5], 2, 73, 1e-5),
+    "cpd_tt_dgn_L4": lambda: cpd_tt_case("cpd_tt_dgn_L4", [9, 8, 7, 6], 3, 76, 1e-5, bi_method='cg_static',
+                                         inner_method='cg_static', cg_maxiter=10, maxiter=60),
+    "dgn_fix_cg_L3": lambda: dgn_case("dgn_fix_cg_L3", [8, 7, 6], 3, 37, fix=2, inner_method='cg_static',
+                                      cg_maxiter=8, maxiter=30),
+    "dgn_fix_cgr_L3": lambda: dgn_case("dgn_fix_cgr_L3", [9, 8, 7], 3, 38, fix=1, maxiter=40),
     "cpd_tt_L3": lambda: cpd_tt_case("cpd_tt_L3", [10, 9, 8], 3, 74, 1e-5),
     "init_smart": lambda: init_case("init_smart", 61),
     "cpd_smart": lambda: cpd_case("cpd_smart", [14, 12, 10], 3, 62, 1e-5, initialization='smart'),

@@ -12,6 +12,7 @@ tfx = pytest.importorskip("tensorfox_gb300")
 
 INNER_CASES = ["dgn_als_L3", "dgn_als_L4", "dgn_als_fix_L3", "dgn_direct_L3", "dgn_direct_L4", "dgn_direct_fix_L3",
                "dgn_direct_symm_L3", "dgn_direct_big_L3", "dgn_mixed_L3", "dgn_symm_direct_alias_L3"]
+FIXED_CG_CASES = ["dgn_fix_cg_L3", "dgn_fix_cgr_L3"]
 
 
 def _opts(g, mod):
@@ -45,6 +46,25 @@ def test_inner_methods_fp64_match_reference(name):
     np.testing.assert_allclose(er, g["errors"], rtol=1e-6, atol=1e-12)
     np.testing.assert_allclose(ss, g["step_sizes"], rtol=1e-5, atol=1e-12)
     np.testing.assert_allclose(gr, g["gradients"], rtol=1e-5, atol=1e-10)    # NaN where the step was 'als'
+    np.testing.assert_allclose(np.concatenate([w.flatten('F') for w in bf]), g["best_x"], rtol=1e-5, atol=1e-8)
+
+
+@pytest.mark.parametrize("name", FIXED_CG_CASES)
+@pytest.mark.parametrize("cluster", [1, 3])
+def test_engine_fixed_factor_matches_reference(name, cluster):
+    """The engine with a fixed factor (bicpd's dGN, GaussNewton.py:92-99,
+    293-297): 'cg' caps from the seeded RNG, the fixed factor put back after
+    every step but not inside the dogleg trials."""
+    g = load_golden(name)
+    dims, R = [int(d) for d in g["dims"]], int(g["R"])
+    o = _opts(g, tfx)
+    o.cluster = cluster
+    np.random.seed(int(g["seed"]))
+    bf, ss, er, im, gr, st = tfx.dGN(g["T"], _start(g), R, o)
+    assert st == int(g["stop"])
+    assert len(er) == len(g["errors"])
+    np.testing.assert_allclose(er, g["errors"], rtol=1e-6, atol=1e-12)
+    np.testing.assert_allclose(ss, g["step_sizes"], rtol=1e-5, atol=1e-12)
     np.testing.assert_allclose(np.concatenate([w.flatten('F') for w in bf]), g["best_x"], rtol=1e-5, atol=1e-8)
 
 

@@ -49,7 +49,7 @@ def test_tt_cores_large_unfoldings_vs_oracle():
         assert a.shape == tuple(b.shape)
 
 
-@pytest.mark.parametrize("name", ["cpd_tt_L3", "cpd_tt_L4", "cpd_tt_L5"])
+@pytest.mark.parametrize("name", ["cpd_tt_L3", "cpd_tt_L4", "cpd_tt_L5", "cpd_tt_dgn_L4"])
 def test_cpd_tt_matches_reference(name):
     g = load_golden(name)
     T, R = g["T"], int(g["R"])

@@ -73,7 +73,8 @@ def test_dgn_trajectory_matches_reference(name):
 
 
 INNER_CASES = ["dgn_als_L3", "dgn_als_L4", "dgn_als_fix_L3", "dgn_direct_L3", "dgn_direct_L4", "dgn_direct_fix_L3",
-               "dgn_direct_symm_L3", "dgn_direct_big_L3", "dgn_mixed_L3", "dgn_symm_direct_alias_L3"]
+               "dgn_direct_symm_L3", "dgn_direct_big_L3", "dgn_mixed_L3", "dgn_symm_direct_alias_L3",
+               "dgn_fix_cg_L3", "dgn_fix_cgr_L3"]
 SYMM_CASES = ["dgn_symm_L3", "dgn_symm_alias_L3", "dgn_symm_norm_L3"]
 
 
@@ -96,6 +97,7 @@ def test_dgn_inner_als_direct_match_reference(name):
     g = load_golden(name)
     R = int(g["R"])
     o = _opts(g)
+    np.random.seed(int(g["seed"]))      # the 'cg' caps draw from the global RNG
     bf, ss, er, im, gr, st = orc.dGN(g["T"], start_of(g), R, o)
     assert st == int(g["stop"])
     assert len(er) == len(g["errors"])
@@ -358,7 +360,7 @@ def congruence(A, B):
     return C[r, c].min()
 
 
-@pytest.mark.parametrize("name", ["cpd_tt_L3", "cpd_tt_L4", "cpd_tt_L5"])
+@pytest.mark.parametrize("name", ["cpd_tt_L3", "cpd_tt_L4", "cpd_tt_L5", "cpd_tt_dgn_L4"])
 def test_cpd_tt_matches_reference(name):
     """End to end, the tensor-train path is pinned by its result: the inner TT
     cores have orthonormal unfoldings, so the MLSVD basis of those modes is
