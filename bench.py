@@ -77,6 +77,14 @@ class Clocks:
         for line in self.proc.stdout:
             self.lines.append(line.strip())
 
+    def mark_start(self):
+        """Samples taken from here on count (the timed region starts)."""
+        self.first = len(self.lines)
+
+    def mark_end(self):
+        """Samples taken after this do not count; at least the newest one is kept."""
+        self.last = max(len(self.lines), getattr(self, "first", 0) + 1)
+
     def __exit__(self, *a):
         if self.proc is not None:
             self.proc.terminate()
@@ -88,7 +96,10 @@ class Clocks:
     def summary(self):
         sm, mx, reasons = [], None, set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for ln in self.lines:
+        first = getattr(self, "first", 0)
+        last = getattr(self, "last", len(self.lines))
+        lines = self.lines[max(0, min(first, last - 1)):last] if self.lines else []
+        for ln in lines:
             parts = [p.strip() for p in ln.split(",")]
             if len(parts) < 7:
                 continue
@@ -202,36 +213,52 @@ def run_ours(args):
             dist.barrier()
         torch.cuda.synchronize()
 
+    # The clock sampler (an nvidia-smi process) starts before the warm-up and
+    # stops after the last timed loop: its start-up and tear-down stall the
+    # driver for a while, so no timed loop may sit next to either.
+    clk = Clocks(local)
+    clk.__enter__()
     # warm-up (also builds the library on first use)
     for _ in range(args.warmup):
         np.random.seed(0)
         tfx.cpd(Td, R, opts)
+    np.random.seed(0)
+    tfx.cpd(Th, R, opts)
     barrier()
     stream = torch.cuda.current_stream()
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     l0 = _lib.launch_count()
     outs = []
-    with Clocks(local) as clk:
-        barrier()
-        ev0.record(stream)
-        for _ in range(args.steps):
-            np.random.seed(0)
-            f, out = tfx.cpd(Td, R, opts)
-            outs.append(out)
-        ev1.record(stream)
-        barrier()
+    barrier()
+    clk.mark_start()
+    ev0.record(stream)
+    for _ in range(args.steps):
+        np.random.seed(0)
+        f, out = tfx.cpd(Td, R, opts)
+        outs.append(out)
+    ev1.record(stream)
+    barrier()
     launches = _lib.launch_count() - l0
     t_dev = ev0.elapsed_time(ev1) / 1e3 / args.steps
     # end to end: pinned host tensor in (H2D inside the call), NumPy factors out
-    np.random.seed(0)
-    tfx.cpd(Th, R, opts)
-    barrier()
     t0 = time.perf_counter()
     for _ in range(args.steps):
         np.random.seed(0)
         f_e2e, out_e2e = tfx.cpd(Th, R, opts)
     barrier()
     t_e2e = (time.perf_counter() - t0) / args.steps
+    clk.mark_end()
+    # the host-to-device copy alone (pinned source, one cudaMemcpyAsync)
+    h0, h1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    h2d = []
+    for _ in range(3):
+        h0.record(stream)
+        xin = Th.to(dev, non_blocking=True)
+        h1.record(stream)
+        barrier()
+        h2d.append(h0.elapsed_time(h1))
+        del xin
+    t_h2d = float(np.median(h2d)) / 1e3
     if world > 1:
         from tensorfox_gb300.distributed import max_over_ranks
         t_dev, t_e2e = max_over_ranks([t_dev, t_e2e], device=dev)
@@ -270,14 +297,17 @@ def run_ours(args):
     c1_leg = run_c1(args) if not args.no_batched else None
     autograd_leg = run_autograd(args) if not args.no_batched else None
     als_leg = run_als(Td, R, args) if not args.no_batched else None
+    inner_leg = run_inner(args) if not args.no_batched else None
+    clk.__exit__(None, None, None)
+    clk_summary = clk.summary()
     flops = 2.0 * DIMS[0] * DIMS[0] * DIMS[1] * DIMS[2]
     hbm, bf16, src = peaks()
     achieved_tf = flops / t_gram / 1e12
     # DRAM traffic of one launch, from the ncu capture of the small case
-    # (profiles/k_gram_tc_mode0_512x128x512.md: 135.97 MB read + 3.58 MB written
+    # (profiles/k_gram_tc2_mode0_512x128x512.md: 134.60 MB read + 3.43 MB written
     # for a 134 MB input) scaled by the input size, which the traffic follows
     # (the tensor crosses HBM once; the partials grow with the split count only)
-    traffic = (135.97e6 + 3.58e6) * (float(np.prod(DIMS)) * 4 / (512 * 128 * 512 * 4))
+    traffic = (134.60e6 + 3.43e6) * (float(np.prod(DIMS)) * 4 / (512 * 128 * 512 * 4))
 
     # congruence with the planted factors and the FP64 oracle error of the result
     fl = outs[-1]
@@ -295,12 +325,13 @@ def run_ours(args):
             "rel_error": float(fl.rel_error), "num_steps": int(fl.num_steps), "stop": [int(s) for s in fl.stop],
             "plain_fp32": {"value": t_plain, "unit": "s", "rel_error": float(out_plain.rel_error)},
             "e2e": {"value": t_e2e, "unit": "s", "h2d_bytes_per_step": int(T.nbytes),
-                    "d2h_bytes_per_step": int(sum(d * R * 8 for d in DIMS))},
+                    "d2h_bytes_per_step": int(sum(d * R * 8 for d in DIMS)),
+                    "h2d_copy_s": t_h2d, "h2d_GBps": float(T.nbytes) / t_h2d / 1e9},
             "roofline": {"bound": "tensor", "kernel": "k_gram_tc2 (tcgen05 TF32 mode-1 Gram, 512 x 262144, 2x2 super-blocks, incl. split-K reduce)",
                          "achieved": achieved_tf, "peak": bf16, "unit": "TFLOP/s", "frac": achieved_tf / bf16,
                          "traffic": traffic, "peak_source": src + " bf16 dense (TF32 tensor rate is half of it)"},
             "gpu_launches": int(launches / max(1, args.steps)) * args.steps,
-            "clocks": clk.summary()}
+            "clocks": clk_summary}
     if cpu is not None:
         line["cpu_baseline"] = cpu
     if batched is not None:
@@ -313,6 +344,8 @@ def run_ours(args):
         line["autograd"] = autograd_leg
     if als_leg is not None:
         line["als"] = als_leg
+    if inner_leg is not None:
+        line["dgn_inner_methods"] = inner_leg
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:
@@ -431,6 +464,41 @@ def run_als(Td, R, args):
     t = a.elapsed_time(b) / 1e3 / reps
     return {"workload": "as the headline, method='als'", "value": t, "unit": "s", "rel_error": float(out.rel_error),
             "num_steps": int(out.num_steps), "stop": [int(s) for s in out.stop]}
+
+
+def run_inner(args, seed=102):
+    """dGN with the 'direct' and 'als' inner methods on a core of the headline's
+    compressed size (50^3, rank 50, FP64, planted + 1e-3 noise): seconds per
+    iteration.  'direct' forms the 7500 x 7500 damped system and factors it by
+    LU every iteration; the FP64 rate of that factorisation (2/3 n^3 flop) is
+    reported as a lower bound (the Hessian and gradient are in the time)."""
+    import torch
+    import tensorfox_gb300 as tfx
+    rng = np.random.default_rng(seed)
+    dims, R = (50, 50, 50), 50
+    W = [rng.standard_normal((d, R)) for d in dims]
+    T = np.einsum('ir,jr,kr->ijk', *W)
+    T += 1e-3 * np.linalg.norm(T) / np.sqrt(T.size) * rng.standard_normal(dims)
+    init = [w + 0.3 * rng.standard_normal(w.shape) for w in W]
+    out = {"workload": "dGN on a 50^3 FP64 core, rank 50 (n = 7500 unknowns)"}
+    for inner, iters in (("direct", 3), ("als", 20)):
+        o = tfx.make_options(None)
+        o.inner_method = inner
+        o.maxiter = iters
+        o.tol = o.tol_step = o.tol_improv = o.tol_grad = 0.0
+        tfx.dGN(T, [w.copy() for w in init], R, o)     # warm-up (workspace, attributes)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        _, ss, er, _, _, st = tfx.dGN(T, [w.copy() for w in init], R, o)
+        torch.cuda.synchronize()
+        t = (time.perf_counter() - t0) / len(er)
+        leg = {"s_per_iteration": t, "iterations": int(len(er)), "error_first": float(er[0]),
+               "error_last": float(er[-1])}
+        if inner == "direct":
+            n = R * sum(dims)
+            leg["lu_fp64_TFLOPs_lower_bound"] = (2.0 / 3.0) * n ** 3 / t / 1e12
+        out[inner] = leg
+    return out
 
 
 def run_c1(args, seed=101):
