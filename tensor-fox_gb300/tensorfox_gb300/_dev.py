@@ -46,6 +46,17 @@ def to_device(a, dtype):
     return t.to(device=device(), dtype=dtype, non_blocking=False).contiguous()
 
 
+def h2d(arr, dtype, dev=None):
+    """NumPy array -> CUDA tensor of ``dtype`` without blocking the host: the
+    values are converted on the host, staged in pinned memory and copied
+    asynchronously on the current stream (a pageable copy would wait for all
+    queued device work first)."""
+    np_dt = np.float64 if dtype == torch.float64 else (np.float32 if dtype == torch.float32 else None)
+    a = np.ascontiguousarray(arr, dtype=np_dt) if np_dt is not None else np.ascontiguousarray(arr)
+    t = torch.from_numpy(a).pin_memory()
+    return t.to(device=dev if dev is not None else device(), non_blocking=True)
+
+
 def flat_factors(factors):
     """concat_l vec_F(W_l) as float64 numpy (GaussNewton.py:125)."""
     return np.concatenate([np.asarray(W, dtype=np.float64).flatten("F") for W in factors])

@@ -136,7 +136,7 @@ def starting_point_core(S, core, R, options, vectorized=False):
 
 
 def _flat_dev(factors, dtype, device):
-    return torch.from_numpy(_dev.flat_factors(factors)).to(device=device, dtype=dtype)
+    return _dev.h2d(_dev.flat_factors(factors), dtype, device)
 
 
 def _run_dgn(Td, x0, R, options, prec, aliased=False, fix_mode=-1):
@@ -199,8 +199,7 @@ def tricpd(T, R, options):
     else:
         Td = _dev.to_device(np.transpose(np.asarray(T), ordering), dt)
     dims = tuple(int(d) for d in Td.shape)
-    nrm = kernels.tensor_norms(Td).cpu().numpy()
-    Tsize = float(np.sqrt(nrm[0]))
+    nrm_dev = kernels.tensor_norms(Td)       # read with the final error (no wait here)
     S, Uts, sigmas, core = mlsvd_device(Td, R, o)
     if o.symm:
         Rm = min(core)
@@ -229,7 +228,9 @@ def tricpd(T, R, options):
     if o.refine:
         rel_error = float(er2[-1])
     else:
-        rel_error = float(np.sqrt(kernels.cp_residual_sq(Td, dims, Wf, R).cpu().numpy()[0])) / Tsize
+        # one transfer: ||T - [[W]]||^2, ||T||^2
+        r2n = torch.cat([kernels.cp_residual_sq(Td, dims, Wf, R), nrm_dev[:1]]).cpu().numpy()
+        rel_error = float(np.sqrt(r2n[0])) / float(np.sqrt(r2n[1]))
     factors = _dev.unflat(Wf.double().cpu().numpy(), dims, R)
     factors = unsort_dims(factors, ordering)
     out = Output()

@@ -34,11 +34,12 @@ def clean_compression(sigma, tol_mlsvd, L):
     return len(sigma)
 
 
-def top_eig(G, n, omega=None):
+def top_eig(G, n, omega=None, host=True):
     """Leading ``n`` eigenpairs of the symmetric D x D device matrix ``G``.
 
     Returns ``(Ut, lam)``: Ut is (n, D) (rows = eigenvectors, signs fixed),
-    lam a float64 NumPy array (descending).
+    lam a float64 NumPy array (descending), or a device tensor with
+    ``host=False`` (no wait for the device).
     """
     D = G.shape[0]
     n = min(n, D)
@@ -50,10 +51,10 @@ def top_eig(G, n, omega=None):
         lam = ev[:n]
     else:
         if omega is not None and omega.shape[0] == D:
-            Yt = torch.from_numpy(np.ascontiguousarray(omega[:, :k].T)).to(device=G.device, dtype=G.dtype)
+            Yt = _dev.h2d(omega[:, :k].T, G.dtype, G.device)
         else:
             rng = np.random.default_rng(D * 7919 + k)
-            Yt = torch.from_numpy(rng.standard_normal((k, D))).to(device=G.device, dtype=G.dtype)
+            Yt = _dev.h2d(rng.standard_normal((k, D)), G.dtype, G.device)
         for _ in range(3):
             Yt = kernels.matmul(Yt, G)          # (G Y)^T, G symmetric
             kernels.orthonormalize(Yt)
@@ -63,6 +64,8 @@ def top_eig(G, n, omega=None):
         Ut = kernels.matmul(V[:n].contiguous(), Yt)
         lam = ev[:n]
     kernels.flip_signs(Ut)
+    if not host:
+        return Ut, lam
     lam = lam.double().cpu().numpy()
     return Ut, lam
 
@@ -103,6 +106,10 @@ def mlsvd_device(Td, R, options):
     Uts, sigmas = [], []
     tc = getattr(o, 'precision', None) == 'mixed'
     if o.mlsvd_method in ('seq', 'gpu'):
+        spec = _seq_speculative(Td, shape, R, o, tol_mlsvd, tc)
+        if spec is not None:
+            S, Uts, sigmas, cur = spec
+            return _finish(S, Uts, sigmas, cur, o, L)
         S, cur = Td, list(shape)
         for l in range(L):
             n = o.svd_n_components if o.svd_n_components is not None else min(R, shape[l])
@@ -121,6 +128,50 @@ def mlsvd_device(Td, R, options):
             S, cur = kernels.ttm(S, cur, l, Uts[l])
     else:
         raise NotImplementedError("mlsvd_method %r" % (o.mlsvd_method,))
+    return _finish(S, Uts, sigmas, cur, o, L)
+
+
+def _seq_speculative(Td, shape, R, o, tol_mlsvd, tc):
+    """The sequential MLSVD issued without waiting for the device: every mode is
+    assumed to keep n = min(R, d_l) singular vectors, the eigenvalues of all
+    modes are read in one transfer at the end, and the energy truncation
+    (``clean_compression``) is applied then.  If it keeps fewer vectors in some
+    mode, the result is discarded, NumPy's RNG is put back, and the caller
+    runs the mode-by-mode path (same draws, same result as the reference's
+    order).  Returns None in that case."""
+    L = len(shape)
+    state = np.random.get_state()
+    S, cur = Td, list(shape)
+    Uts, lams, errs, ns = [], [], [], []
+    for l in range(L):
+        n = o.svd_n_components if o.svd_n_components is not None else min(R, shape[l])
+        omega = _draw_omega(_ref_draw_cols(cur, l), n + 10)
+        if tc and kernels.tc_gram_supported(S, cur, l):
+            G, err = kernels.mode_gram_tc(S, cur, l, check=False)
+            errs.append(err)
+        else:
+            G = kernels.mode_gram(S, cur, l)
+        Ut, lam = top_eig(G, n, omega, host=False)
+        Uts.append(Ut)
+        lams.append(lam.double())
+        ns.append(int(lam.shape[0]))
+        S, cur = kernels.ttm(S, cur, l, Ut)
+    host = torch.cat(lams).cpu().numpy()          # the one wait of the whole MLSVD
+    for err in errs:
+        kernels.check_gram_flag(err)
+    sigmas, off = [], 0
+    for l in range(L):
+        sigma = np.sqrt(np.maximum(host[off:off + ns[l]], 0.0))
+        off += ns[l]
+        if clean_compression(sigma, tol_mlsvd, L) != ns[l]:
+            np.random.set_state(state)
+            return None
+        sigmas.append(sigma)
+    return S, Uts, sigmas, cur
+
+
+def _finish(S, Uts, sigmas, cur, o, L):
+    """User truncation (``trunc_dims``) and the core's final shape."""
     if isinstance(o.trunc_dims, list):
         sl = []
         for l in range(L):

@@ -87,20 +87,26 @@ class _Batch:
             dims_c = (ctypes.c_int * L)(*t.shape)
             nb = lib.tfx_dgn_workspace_bytes(_dev.lib_dtype(precision), L, dims_c, int(R))
             self.ws.append(torch.empty(int(nb), dtype=torch.uint8, device=t.device))
+        # host -> device copies through pinned staging: they queue behind the
+        # device work instead of waiting for it
         if budgets is None:
-            self.budgets = [torch.from_numpy(cg_budgets(options, t.dim())).to(t.device) for t in tensors]
+            self.budgets = [_dev.h2d(cg_budgets(options, t.dim()), None, t.device) for t in tensors]
         else:   # per-problem caps drawn by the caller (maxiter ints each)
-            self.budgets = [torch.from_numpy(np.ascontiguousarray(b, dtype=np.int32)).to(t.device)
+            self.budgets = [_dev.h2d(np.asarray(b, dtype=np.int32), None, t.device)
                             for b, t in zip(budgets, tensors)]
         sched = options.init_damp if isinstance(options.init_damp, list) else None
         self.sched = None
         if sched is not None:
-            self.sched = torch.tensor(np.asarray(sched, dtype=np.float64), device=tensors[0].device)
+            self.sched = _dev.h2d(np.asarray(sched, dtype=np.float64), torch.float64, tensors[0].device)
         self.stats = torch.zeros((self.n, 4 * self.maxiter), dtype=torch.float64, device=tensors[0].device)
         self.result = torch.zeros((self.n, 4), dtype=torch.int32, device=tensors[0].device)
         self.info = torch.zeros((self.n, 8), dtype=torch.float64, device=tensors[0].device)
         self.prof = torch.zeros((self.n, 24), dtype=torch.int64, device=tensors[0].device)
-        self.desc = (_lib.DgnProblem * self.n)()
+        # the descriptors live in pinned memory, so the library's copy of them
+        # to the device is asynchronous (this object keeps the buffer alive
+        # until the results are read)
+        self._desc_host = torch.zeros(ctypes.sizeof(_lib.DgnProblem) * self.n, dtype=torch.uint8).pin_memory()
+        self.desc = (_lib.DgnProblem * self.n).from_address(self._desc_host.data_ptr())
         for p in range(self.n):
             d = self.desc[p]
             d.L = len(self.dims[p])

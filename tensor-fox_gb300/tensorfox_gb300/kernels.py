@@ -46,8 +46,11 @@ def tc_gram_supported(S, shape, l):
     return S.dtype == torch.float32 and Q >= 32 and Q % 4 == 0 and S.data_ptr() % 16 == 0
 
 
-def mode_gram_tc(S, shape, l):
-    """``S_(l) S_(l)^T`` on the tensor cores (tcgen05 kind::tf32, FP32 accumulation)."""
+def mode_gram_tc(S, shape, l, check=True):
+    """``S_(l) S_(l)^T`` on the tensor cores (tcgen05 kind::tf32, FP32 accumulation).
+
+    ``check=False`` returns ``(G, err)`` without reading the kernel's error flag
+    (a read waits for the device); the caller checks ``err`` at its next sync."""
     P = int(np.prod(shape[:l], dtype=np.int64))
     D = int(shape[l])
     Q = int(np.prod(shape[l + 1:], dtype=np.int64))
@@ -57,10 +60,17 @@ def mode_gram_tc(S, shape, l):
     err = torch.zeros(1, dtype=torch.int32, device=S.device)
     G = torch.empty((D, D), dtype=torch.float32, device=S.device)
     _lib.call("tfx_mode_gram_tc", _vp(S), P, D, Q, _vp(G), _vp(scratch), nb, _vp(err), _st())
+    if not check:
+        return G, err
+    check_gram_flag(err)
+    return G
+
+
+def check_gram_flag(err):
+    """Raises when the tensor-core Gram's bounded wait ran out (``err`` != 0)."""
     e = int(err.item())
     if e != 0:
         raise _lib.TfxError("tensor-core Gram: bounded wait expired (code %d)" % e)
-    return G
 
 
 def gemm(A, B, C, M, N, K, batch, strides, alpha=1.0, beta=0.0):
