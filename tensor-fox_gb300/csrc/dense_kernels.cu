@@ -764,12 +764,54 @@ __global__ void k_tensor_norms(const T* __restrict__ Tt, long long N, double* __
   __shared__ double red[2][TFX_THREADS / 32];
   // compensated accumulation in the working precision (FP64 per element would
   // run at GB300's FP64 rate)
-  Acc<T> a2, a1;
-  for (long long e = (long long)blockIdx.x * TFX_THREADS + threadIdx.x; e < N; e += (long long)gridDim.x * TFX_THREADS) {
-    const T t = __ldg(Tt + e);
-    a2.fma_(t, t);
-    a1.add(fabs(t));
+  // 16-byte loads, four of them in flight per thread (independent
+  // accumulators), so the read runs at HBM speed rather than at one
+  // outstanding scalar load per thread
+  Acc<T> a2, a1, b2, b1;
+  constexpr int V = 16 / sizeof(T);  // elements per 16-byte vector
+  const bool vec = (((uintptr_t)Tt) & 15) == 0;
+  const long long nv = vec ? N / V : 0;
+  const long long stride = (long long)gridDim.x * TFX_THREADS;
+  long long e = (long long)blockIdx.x * TFX_THREADS + threadIdx.x;
+  if constexpr (sizeof(T) == 4) {
+    const float4* p = (const float4*)Tt;
+    for (; e + stride < nv; e += 2 * stride) {
+      const float4 u = __ldg(p + e), w = __ldg(p + e + stride);
+      a2.fma_((T)u.x, (T)u.x); a1.add(fabs((T)u.x)); b2.fma_((T)w.x, (T)w.x); b1.add(fabs((T)w.x));
+      a2.fma_((T)u.y, (T)u.y); a1.add(fabs((T)u.y)); b2.fma_((T)w.y, (T)w.y); b1.add(fabs((T)w.y));
+      a2.fma_((T)u.z, (T)u.z); a1.add(fabs((T)u.z)); b2.fma_((T)w.z, (T)w.z); b1.add(fabs((T)w.z));
+      a2.fma_((T)u.w, (T)u.w); a1.add(fabs((T)u.w)); b2.fma_((T)w.w, (T)w.w); b1.add(fabs((T)w.w));
+    }
+    for (; e < nv; e += stride) {
+      const float4 u = __ldg(p + e);
+      a2.fma_((T)u.x, (T)u.x); a1.add(fabs((T)u.x));
+      a2.fma_((T)u.y, (T)u.y); a1.add(fabs((T)u.y));
+      a2.fma_((T)u.z, (T)u.z); a1.add(fabs((T)u.z));
+      a2.fma_((T)u.w, (T)u.w); a1.add(fabs((T)u.w));
+    }
+  } else {
+    const double2* p = (const double2*)Tt;
+    for (; e + stride < nv; e += 2 * stride) {
+      const double2 u = __ldg(p + e), w = __ldg(p + e + stride);
+      a2.fma_((T)u.x, (T)u.x); a1.add(fabs((T)u.x)); b2.fma_((T)w.x, (T)w.x); b1.add(fabs((T)w.x));
+      a2.fma_((T)u.y, (T)u.y); a1.add(fabs((T)u.y)); b2.fma_((T)w.y, (T)w.y); b1.add(fabs((T)w.y));
+    }
+    for (; e < nv; e += stride) {
+      const double2 u = __ldg(p + e);
+      a2.fma_((T)u.x, (T)u.x); a1.add(fabs((T)u.x));
+      a2.fma_((T)u.y, (T)u.y); a1.add(fabs((T)u.y));
+    }
   }
+  // the scalar tail (and the whole tensor when it is not 16-byte aligned)
+  for (long long t = nv * V + (long long)blockIdx.x * TFX_THREADS + threadIdx.x; t < N; t += stride) {
+    const T v = __ldg(Tt + t);
+    a2.fma_(v, v);
+    a1.add(fabs(v));
+  }
+  a2.add(b2.hi_or_v());
+  a2.add(b2.lo_or_0());
+  a1.add(b1.hi_or_v());
+  a1.add(b1.lo_or_0());
   a2.warp_reduce();
   a1.warp_reduce();
   if ((threadIdx.x & 31) == 0) {

@@ -147,9 +147,19 @@ def _run_dgn(Td, x0, R, options, prec, aliased=False, fix_mode=-1):
     from .stepped import uses_stepped, dgn_stepped
     if uses_stepped(options):
         return dgn_stepped(Td, x0, R, options, prec, fix_mode=fix_mode, aliased=aliased)
+    return _engine_collect(_engine_launch(Td, x0, R, options, prec, aliased, fix_mode), options)
+
+
+def _engine_launch(Td, x0, R, options, prec, aliased=False, fix_mode=-1):
+    """Queues one engine solve on the current stream; nothing is read back."""
     b = _Batch([Td], [x0], [R], options, prec, aliased=aliased, fix_mode=fix_mode)
-    c = options.cluster or auto_cluster(tuple(Td.shape), R)
-    b.launch(c)
+    b.launch(options.cluster or auto_cluster(tuple(Td.shape), R))
+    return b
+
+
+def _engine_collect(b, options):
+    """Reads a launched engine solve: (best, step_sizes, errors, improv,
+    gradients, stop), the global RNG advanced past the 'cg' caps' draws."""
     res = b.result[0].cpu().numpy()
     _lib.check_solve_status(res)
     stats = b.stats[0].cpu().numpy()
@@ -200,12 +210,82 @@ def tricpd(T, R, options):
         Td = _dev.to_device(np.transpose(np.asarray(T), ordering), dt)
     dims = tuple(int(d) for d in Td.shape)
     nrm_dev = kernels.tensor_norms(Td)       # read with the final error (no wait here)
-    S, Uts, sigmas, core = mlsvd_device(Td, R, o)
+    # Pipelined path (engine solve, random start): the MLSVD, the start point,
+    # the engine, the decompression and the final residual are all queued
+    # before the first read from the device.
+    pipelined, tried = None, False
+    if o.method == 'dGN' and isinstance(o.initialization, str) and o.initialization == 'random':
+        from .stepped import uses_stepped
+        from .compression import mlsvd_launch
+        if not uses_stepped(o):
+            pend = mlsvd_launch(Td, R, o)
+            if pend is not None:
+                tried = True
+                pipelined = _pipelined(Td, dims, R, o, prec, dt, pend)
+    if pipelined is not None:
+        best, ss, er, im, gr, st, Wf, r2 = pipelined
+    else:
+        # after a failed speculation the MLSVD runs mode by mode straight away
+        best, ss, er, im, gr, st, Wf, r2 = _staged(Td, dims, R, o, prec, dt, ordering, solve, speculate=not tried)
+    if o.refine:
+        Wf, ss2, er2, im2, gr2, st2 = solve(Td, Wf, R, o, prec)
+    else:
+        ss2, er2, im2, gr2, st2 = np.array([0]), np.array([0]), np.array([0]), np.array([0]), 8
+    if o.refine:
+        rel_error = float(er2[-1])
+    else:
+        # one transfer: ||T - [[W]]||^2, ||T||^2
+        r2n = torch.cat([r2, nrm_dev[:1]]).cpu().numpy()
+        rel_error = float(np.sqrt(r2n[0])) / float(np.sqrt(r2n[1]))
+    factors = _dev.unflat(Wf.double().cpu().numpy(), dims, R)
+    factors = unsort_dims(factors, ordering)
+    out = Output()
+    out.num_steps = len(ss) + (len(ss2) if o.refine else 0)
+    out.rel_error = rel_error
+    out.accuracy = max(0, 100 * (1 - rel_error))
+    out.step_sizes = [ss, ss2]
+    out.errors = [er, er2]
+    out.improv = [im, im2]
+    out.gradients = [gr, gr2]
+    out.stop = [st, st2]
+    out.options = o
+    return factors, out
+
+
+def _symm_core(S, Uts, core, L):
+    """TensorFox.py:519-523: with symm the core keeps min(core) in every mode."""
+    Rm = min(core)
+    S = S[tuple(slice(Rm) for _ in range(L))].contiguous()
+    return S, [u[:Rm].contiguous() for u in Uts], [Rm] * L
+
+
+def _pipelined(Td, dims, R, o, prec, dt, pend):
+    """The engine path with no read from the device until everything is queued.
+    Returns None (NumPy's RNG put back) when the MLSVD's energy truncation cuts
+    a mode, so the staged path must run instead."""
+    from .compression import mlsvd_confirm
+    L = len(dims)
+    S, Uts, core = pend.S, pend.Uts, list(pend.cur)
     if o.symm:
-        Rm = min(core)
-        S = S[tuple(slice(Rm) for _ in range(L))].contiguous()
-        Uts = [u[:Rm].contiguous() for u in Uts]
-        core = [Rm] * L
+        S, Uts, core = _symm_core(S, Uts, core, L)
+    init = starting_point_core(S, core, R, o, vectorized=(prec == 'fp32'))
+    x0 = _flat_dev(init, dt, Td.device)
+    alias = bool(o.symm) and float(o.factors_norm) <= 0     # Initialization.py:83
+    b = _engine_launch(S, x0, R, o, prec, aliased=alias)
+    Wf = _decompress(Uts, b.best[0], core, R)
+    r2 = None if o.refine else kernels.cp_residual_sq(Td, dims, Wf, R)
+    if mlsvd_confirm(pend) is None:
+        return None
+    best, ss, er, im, gr, st = _engine_collect(b, o)
+    return best, ss, er, im, gr, st, Wf, r2
+
+
+def _staged(Td, dims, R, o, prec, dt, ordering, solve, speculate=True):
+    """MLSVD, start point, solve, decompression and residual one after the other."""
+    L = len(dims)
+    S, Uts, sigmas, core = mlsvd_device(Td, R, o, speculate=speculate)
+    if o.symm:
+        S, Uts, core = _symm_core(S, Uts, core, L)
     if isinstance(o.initialization, list):
         init = []
         for l in range(L):
@@ -221,29 +301,8 @@ def tricpd(T, R, options):
         alias = bool(o.symm) and float(o.factors_norm) <= 0 and not isinstance(o.initialization, list)
         best, ss, er, im, gr, st = solve(S, x0, R, o, prec, aliased=alias)
     Wf = _decompress(Uts, best, core, R)
-    if o.refine:
-        Wf, ss2, er2, im2, gr2, st2 = solve(Td, Wf, R, o, prec)
-    else:
-        ss2, er2, im2, gr2, st2 = np.array([0]), np.array([0]), np.array([0]), np.array([0]), 8
-    if o.refine:
-        rel_error = float(er2[-1])
-    else:
-        # one transfer: ||T - [[W]]||^2, ||T||^2
-        r2n = torch.cat([kernels.cp_residual_sq(Td, dims, Wf, R), nrm_dev[:1]]).cpu().numpy()
-        rel_error = float(np.sqrt(r2n[0])) / float(np.sqrt(r2n[1]))
-    factors = _dev.unflat(Wf.double().cpu().numpy(), dims, R)
-    factors = unsort_dims(factors, ordering)
-    out = Output()
-    out.num_steps = len(ss) + (len(ss2) if o.refine else 0)
-    out.rel_error = rel_error
-    out.accuracy = max(0, 100 * (1 - rel_error))
-    out.step_sizes = [ss, ss2]
-    out.errors = [er, er2]
-    out.improv = [im, im2]
-    out.gradients = [gr, gr2]
-    out.stop = [st, st2]
-    out.options = o
-    return factors, out
+    r2 = None if o.refine else kernels.cp_residual_sq(Td, dims, Wf, R)
+    return best, ss, er, im, gr, st, Wf, r2
 
 
 def cpd(T, R, options=False):

@@ -92,8 +92,12 @@ def _ref_draw_cols(shape, l):
     return D if D < other else other
 
 
-def mlsvd_device(Td, R, options):
-    """Device MLSVD of a dense C-order tensor. Returns (S, Ut_list, sigmas, shape)."""
+def mlsvd_device(Td, R, options, speculate=True):
+    """Device MLSVD of a dense C-order tensor. Returns (S, Ut_list, sigmas, shape).
+
+    The sequential method is issued as one stream of device work with a single
+    read at the end (``mlsvd_launch`` / ``mlsvd_confirm``); ``speculate=False``,
+    or an energy truncation that cuts a mode, takes the mode-by-mode path."""
     o = options
     shape = [int(d) for d in Td.shape]
     L = len(shape)
@@ -106,10 +110,11 @@ def mlsvd_device(Td, R, options):
     Uts, sigmas = [], []
     tc = getattr(o, 'precision', None) == 'mixed'
     if o.mlsvd_method in ('seq', 'gpu'):
-        spec = _seq_speculative(Td, shape, R, o, tol_mlsvd, tc)
-        if spec is not None:
-            S, Uts, sigmas, cur = spec
-            return _finish(S, Uts, sigmas, cur, o, L)
+        p = mlsvd_launch(Td, R, o) if speculate else None
+        if p is not None:
+            sig = mlsvd_confirm(p)
+            if sig is not None:
+                return _finish(p.S, p.Uts, sig, p.cur, o, L)
         S, cur = Td, list(shape)
         for l in range(L):
             n = o.svd_n_components if o.svd_n_components is not None else min(R, shape[l])
@@ -131,15 +136,30 @@ def mlsvd_device(Td, R, options):
     return _finish(S, Uts, sigmas, cur, o, L)
 
 
-def _seq_speculative(Td, shape, R, o, tol_mlsvd, tc):
-    """The sequential MLSVD issued without waiting for the device: every mode is
-    assumed to keep n = min(R, d_l) singular vectors, the eigenvalues of all
-    modes are read in one transfer at the end, and the energy truncation
-    (``clean_compression``) is applied then.  If it keeps fewer vectors in some
-    mode, the result is discarded, NumPy's RNG is put back, and the caller
-    runs the mode-by-mode path (same draws, same result as the reference's
-    order).  Returns None in that case."""
+class Pending:
+    """A sequential MLSVD issued to the device and not yet checked: the core
+    ``S`` (shape ``cur``) and the bases ``Uts`` assume every mode keeps
+    n = min(R, d_l) singular vectors."""
+
+    def __init__(self, S, Uts, cur, lams, errs, ns, state, tol_mlsvd):
+        self.S, self.Uts, self.cur = S, Uts, cur
+        self.lams, self.errs, self.ns = lams, errs, ns
+        self.state, self.tol_mlsvd = state, tol_mlsvd
+
+
+def mlsvd_launch(Td, R, o):
+    """Issues the sequential MLSVD without waiting for the device, or returns
+    None where that path does not apply (no compression, 'classic', user
+    truncation).  Every mode is assumed to keep n = min(R, d_l) vectors; the
+    eigenvalues stay on the device until ``mlsvd_confirm``."""
+    shape = [int(d) for d in Td.shape]
     L = len(shape)
+    tol_mlsvd = o.tol_mlsvd
+    if isinstance(tol_mlsvd, list):
+        tol_mlsvd = tol_mlsvd[0] if L > 3 else tol_mlsvd[1]
+    if tol_mlsvd == -1 or o.mlsvd_method not in ('seq', 'gpu') or isinstance(o.trunc_dims, list):
+        return None
+    tc = getattr(o, 'precision', None) == 'mixed'
     state = np.random.get_state()
     S, cur = Td, list(shape)
     Uts, lams, errs, ns = [], [], [], []
@@ -156,18 +176,28 @@ def _seq_speculative(Td, shape, R, o, tol_mlsvd, tc):
         lams.append(lam.double())
         ns.append(int(lam.shape[0]))
         S, cur = kernels.ttm(S, cur, l, Ut)
-    host = torch.cat(lams).cpu().numpy()          # the one wait of the whole MLSVD
-    for err in errs:
+    return Pending(S.contiguous().view(*cur), Uts, cur, lams, errs, ns, state, tol_mlsvd)
+
+
+def mlsvd_confirm(p):
+    """Reads the eigenvalues of a pending MLSVD in one transfer and applies the
+    energy truncation (``clean_compression``).  Returns the singular values per
+    mode, or None when some mode keeps fewer vectors than assumed -- NumPy's
+    RNG is then put back to where it was before the MLSVD, and the caller
+    redoes the work mode by mode (the reference's order of draws)."""
+    host = torch.cat(p.lams).cpu().numpy()
+    for err in p.errs:
         kernels.check_gram_flag(err)
+    L = len(p.ns)
     sigmas, off = [], 0
     for l in range(L):
-        sigma = np.sqrt(np.maximum(host[off:off + ns[l]], 0.0))
-        off += ns[l]
-        if clean_compression(sigma, tol_mlsvd, L) != ns[l]:
-            np.random.set_state(state)
+        sigma = np.sqrt(np.maximum(host[off:off + p.ns[l]], 0.0))
+        off += p.ns[l]
+        if clean_compression(sigma, p.tol_mlsvd, L) != p.ns[l]:
+            np.random.set_state(p.state)
             return None
         sigmas.append(sigma)
-    return S, Uts, sigmas, cur
+    return sigmas
 
 
 def _finish(S, Uts, sigmas, cur, o, L):
