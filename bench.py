@@ -592,7 +592,20 @@ def run_case(case):
     import torch
     import tensorfox_gb300 as tfx
     from tensorfox_gb300 import kernels, compression, api, gauss_newton, _dev
-    if case == "tc_gram_small":
+    if case == "direct":
+        # two dGN iterations with the 'direct' inner method on a 50^3 FP64 core,
+        # rank 50: the 7500 x 7500 damped system factored by LU twice
+        rng = np.random.default_rng(102)
+        dims, R = (50, 50, 50), 50
+        W = [rng.standard_normal((d, R)) for d in dims]
+        T = np.einsum('ir,jr,kr->ijk', *W) + 1e-2 * rng.standard_normal(dims)
+        o = tfx.make_options(None)
+        o.inner_method = 'direct'
+        o.maxiter = 2
+        _, _, er, _, _, _ = tfx.dGN(T, [w + 0.3 * rng.standard_normal(w.shape) for w in W], R, o)
+        torch.cuda.synchronize()
+        print(json.dumps({"case": case, "errors": [float(e) for e in er]}))
+    elif case == "tc_gram_small":
         # tcgen05 Gram of a 512 x 128 x 512 FP32 tensor (128 MB), mode 0, four launches
         T = torch.randn(512, 128, 512, device="cuda", generator=torch.Generator("cuda").manual_seed(0))
         for _ in range(4):
@@ -644,7 +657,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-sparse", action="store_true")
-    ap.add_argument("--case", default=None, help="tc_gram_small | engine_core | residual_tc | c3_autograd | sparse_c5 (profiling workloads)")
+    ap.add_argument("--case", default=None, help="tc_gram_small | engine_core | residual_tc | c3_autograd | sparse_c5 | direct (profiling workloads)")
     args = ap.parse_args()
     if args.case:
         run_case(args.case)
