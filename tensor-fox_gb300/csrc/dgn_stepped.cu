@@ -214,17 +214,23 @@ __global__ void k_direct_hessian(const T* __restrict__ W, Shape sh, const double
 // first row of largest |value| is the pivot (LAPACK's choice), the pivot row
 // is swapped inside the panel, the column below is divided by the pivot and
 // the panel's later columns get the rank-one update.  A zero pivot marks the
-// matrix singular (flag) and leaves the column as it is.
+// matrix singular (flag) and leaves the column as it is.  Each thread owns
+// rows; a row's panel segment is read in two chunks of 16 independent loads
+// (the pivot row comes from shared memory), so a row costs two memory round
+// trips per column rather than one per updated entry.
+constexpr int PCH = 16;  // panel entries per register chunk
 __global__ void __launch_bounds__(PANEL_THREADS) k_lu_panel(double* __restrict__ H, long long n, int k0, int kb,
                                                             int* __restrict__ piv, int* __restrict__ flag) {
   __shared__ double sv[PANEL_THREADS / 32];
   __shared__ long long si[PANEL_THREADS / 32];
   __shared__ long long s_p;
+  __shared__ double sp[NB];  // the pivot row's panel segment
   const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
   for (int j = 0; j < kb; ++j) {
     const long long c = k0 + j;
     double best = -1.0;
     long long bi = c;
+#pragma unroll 4
     for (long long i = c + tid; i < n; i += PANEL_THREADS) {
       const double v = fabs(H[i * n + c]);
       if (v > best) {
@@ -266,16 +272,32 @@ __global__ void __launch_bounds__(PANEL_THREADS) k_lu_panel(double* __restrict__
         H[pr * n + k0 + t] = a;
       }
     __syncthreads();
-    const double pv = H[c * n + c];
+    if (tid < kb) sp[tid] = H[c * n + k0 + tid];
+    __syncthreads();
+    const double pv = sp[j];
     if (pv == 0.0) {
       if (tid == 0) *flag = 1;
       __syncthreads();
       continue;
     }
     for (long long i = c + 1 + tid; i < n; i += PANEL_THREADS) {
-      const double lic = H[i * n + c] / pv;
-      H[i * n + c] = lic;
-      for (int t = j + 1; t < kb; ++t) H[i * n + k0 + t] -= lic * H[c * n + k0 + t];
+      double* row = H + i * n + k0;
+      const double lic = row[j] / pv;
+      for (int t0 = 0; t0 < kb; t0 += PCH) {
+        if (t0 + PCH <= j + 1) continue;  // chunk entirely at or left of column j
+        double v[PCH];
+#pragma unroll
+        for (int u = 0; u < PCH; ++u) {
+          const int t = t0 + u;
+          v[u] = (t > j && t < kb) ? row[t] : 0.0;
+        }
+#pragma unroll
+        for (int u = 0; u < PCH; ++u) {
+          const int t = t0 + u;
+          if (t > j && t < kb) row[t] = v[u] - lic * sp[t];
+        }
+      }
+      row[j] = lic;
     }
     __syncthreads();
   }

@@ -254,3 +254,28 @@ def test_cp_residual_tensor_core_path(dims, R):
     x = np.concatenate([w.flatten('F') for w in W]).astype(np.float32)
     got = float(kernels.cp_residual_sq(dev(T, torch.float32), list(dims), dev(x, torch.float32), R).cpu().numpy()[0])
     assert abs(got - ref) <= 2e-5 * ref
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_cpd_truncating_mlsvd_falls_back_in_step_with_reference(precision):
+    """An exact rank-2 tensor asked for rank 4: the MLSVD's energy truncation
+    keeps 2 singular vectors per mode instead of the assumed 4, so the queued
+    (speculative) path is discarded and the CPD reruns mode by mode.  Result
+    and NumPy's RNG afterwards match the oracle's."""
+    rng = np.random.default_rng(77)
+    dims, R = (10, 9, 8), 4
+    W = [rng.standard_normal((d, 2)) for d in dims]
+    T = orc.cpd2tens(W)
+    np.random.seed(78)
+    _, out0 = orc.cpd(T, R, orc.make_options(None))
+    want = np.random.rand()
+    o = tfx.make_options(None)
+    o.precision = precision
+    np.random.seed(78)
+    _, out1 = tfx.cpd(T if precision == "fp64" else T.astype(np.float32), R, o)
+    assert np.random.rand() == want
+    assert out1.stop[0] == out0.stop[0] or precision == "mixed"
+    if precision == "fp64":
+        np.testing.assert_allclose(out1.rel_error, out0.rel_error, rtol=1e-6, atol=1e-12)
+    else:
+        assert out1.rel_error < 1e-3
