@@ -264,7 +264,10 @@ def test_cpd_truncating_mlsvd_falls_back_in_step_with_reference(precision):
     RNG afterwards is where the oracle leaves it.  'cg_static' keeps the dGN
     itself free of draws: a rank-4 fit of a rank-2 tensor is degenerate and its
     iteration count (hence the number of 'cg' cap draws) changes with the last
-    bit of the input, in the reference as well."""
+    bit of the input, in the reference as well.  tol_mlsvd is 1e-6: at the
+    default 1e-16 the truncation of exactly-zero directions is decided below
+    the Gram route's resolution (eigenvalues of T T^T carry ~1e-16 of the
+    largest), where the reference's SVD still sees them as zero."""
     rng = np.random.default_rng(77)
     dims, R = (10, 9, 8), 4
     W = [rng.standard_normal((d, 2)) for d in dims]
@@ -274,6 +277,7 @@ def test_cpd_truncating_mlsvd_falls_back_in_step_with_reference(precision):
         inner_method = 'cg_static'
         cg_maxiter = 8
         maxiter = 30
+        tol_mlsvd = 1e-6
     np.random.seed(78)
     _, out0 = orc.cpd(T, R, orc.make_options(O))
     want = np.random.rand()
