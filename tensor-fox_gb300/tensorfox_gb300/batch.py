@@ -144,6 +144,8 @@ def cpd_batch(tensors, ranks, options=None, timings=None, tune=True):
     ``tune``: pick the engine's tile and problem order with the autotuner
     (``tuner.py``; the first batch of a new size class pays for the timing);
     ``options.tile`` (1, 2 or 4) forces a tile with the largest-first order.
+    Methods the batched engine does not run (``method='als'``, the 'als' and
+    'direct' inner methods) are solved problem by problem with ``cpd``.
     """
     _dev.require_cuda()
     import time as _time
@@ -161,6 +163,10 @@ def cpd_batch(tensors, ranks, options=None, timings=None, tune=True):
         return []
     if isinstance(ranks, int):
         ranks = [ranks] * n
+    from .stepped import uses_stepped
+    if o.method != 'dGN' or uses_stepped(o):
+        from .api import cpd
+        return [cpd(T, int(r), o) for T, r in zip(tensors, ranks)]
     lib = _lib.load()
     prec = o.precision if o.precision in ('fp64', 'fp32') else (
         'fp64' if (tensors[0].dtype == np.float64 or tensors[0].dtype == torch.float64) else 'fp32')
