@@ -263,7 +263,7 @@ def run_ours(args):
         from tensorfox_gb300.distributed import max_over_ranks
         t_dev, t_e2e = max_over_ranks([t_dev, t_e2e], device=dev)
 
-    # the plain FP32 path on the same input (the north_star's "plain" comparison)
+    # the plain FP32 path on the same input (no tensor cores in the compression)
     plain = tfx.make_options(None)
     plain.precision = "fp32"
     np.random.seed(0)
