@@ -25,7 +25,7 @@ Differences from the reference, both deliberate:
 * Nothing is printed or plotted (``plot`` is accepted and ignored).
 
 The 'als' method solves each problem with its own graph launch; sparse
-``[data, idxs, dims]`` input runs ``cpd`` per trial.
+``[data, idxs, dims]`` input and ``method='ttcpd'`` run ``cpd`` per trial.
 """
 import time
 
@@ -164,7 +164,8 @@ def stats(T, R, options=False, num_samples=100):
     t0 = time.perf_counter()
     o = make_options(options)
     n = int(num_samples)
-    if isinstance(T, list):
+    if isinstance(T, list) or o.method not in ('dGN', 'als'):
+        # COO input and the tensor-train method: one cpd per sample
         times, steps, errors = np.empty(n), np.empty(n), np.empty(n)
         for k in range(n):
             t = time.perf_counter()
@@ -174,8 +175,6 @@ def stats(T, R, options=False, num_samples=100):
             errors[k] = out.rel_error
         return times, steps, errors
     consistency(R, T.shape, o)
-    if o.method not in ('dGN', 'als'):
-        raise NotImplementedError("method %r" % (o.method,))
     X = _Dense(T, o)
     S, Uts, core = X.compress(R, o)
     probs = [(S, Uts, core, R, X.start(R, o, Uts, core, S)) for _ in range(n)]
@@ -233,8 +232,9 @@ def rank(T, options=False, plot=True, trials=3):
     ``(final_rank, error_per_rank)``."""
     _dev.require_cuda()
     o = make_options(options)
-    if isinstance(T, list):
-        dims = [int(d) for d in T[2]]
+    if isinstance(T, list) or o.method not in ('dGN', 'als'):
+        # COO input and the tensor-train method: trials run one cpd at a time
+        dims = [int(d) for d in (T[2] if isinstance(T, list) else T.shape)]
 
         def best_errors_of(ranks):
             out = []
