@@ -459,6 +459,11 @@ CASES = {
     "cpd_symm": lambda: cpd_case("cpd_symm", [10, 10, 10], 3, 35, 1e-4, symmetric=True, symm=True, maxiter=60),
     "cpd_symm_direct": lambda: cpd_case("cpd_symm_direct", [8, 8, 8], 2, 36, 1e-4, symmetric=True, symm=True,
                                         inner_method='direct', maxiter=30),
+    "dgn_damp_sched_L3": lambda: dgn_case("dgn_damp_sched_L3", [9, 8, 7], 3, 39, inner_method='cg_static',
+                                          cg_maxiter=8, maxiter=25,
+                                          init_damp=[float(0.5 * 0.8 ** k) for k in range(26)]),
+    "dgn_norm_L3": lambda: dgn_case("dgn_norm_L3", [9, 8, 7], 3, 40, inner_method='cg_static', cg_maxiter=8,
+                                    maxiter=25, factors_norm=2.0),
     "dgn_mixed_L3": lambda: dgn_case("dgn_mixed_L3", [9, 8, 7], 3, 27, inner_method=['direct'] * 4 + ['als'] * 26,
                                      maxiter=30),
     "mlsvd_seq": lambda: mlsvd_case("mlsvd_seq", [20, 15, 12], 4, 21),

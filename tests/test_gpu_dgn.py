@@ -140,3 +140,16 @@ def test_dgn_symm_matches_reference(name, cluster):
     # step sizes late in the run are differences of nearly equal points: the
     # rounding of the engine's reductions shows there first (1.7e-5 seen)
     np.testing.assert_allclose(ss, g["step_sizes"], rtol=1e-4, atol=1e-12)
+
+
+@pytest.mark.parametrize("name", ["dgn_damp_sched_L3", "dgn_norm_L3"])
+def test_dgn_options_match_reference(name):
+    """A damping schedule (init_damp as a list, GaussNewton.py:110-111, 490-495)
+    and factors_norm (Conversion.py:439-442) on the engine."""
+    g = load_golden(name)
+    dims, R = [int(d) for d in g["dims"]], int(g["R"])
+    bf, ss, er, im, gr, st = tfx.dGN(g["T"], _start(g), R, _opts(g, tfx))
+    assert st == int(g["stop"])
+    assert len(er) == len(g["errors"])
+    np.testing.assert_allclose(er, g["errors"], rtol=1e-6, atol=1e-12)
+    np.testing.assert_allclose(ss, g["step_sizes"], rtol=1e-4, atol=1e-12)

@@ -76,6 +76,7 @@ INNER_CASES = ["dgn_als_L3", "dgn_als_L4", "dgn_als_fix_L3", "dgn_direct_L3", "d
                "dgn_direct_symm_L3", "dgn_direct_big_L3", "dgn_mixed_L3", "dgn_symm_direct_alias_L3",
                "dgn_fix_cg_L3", "dgn_fix_cgr_L3"]
 SYMM_CASES = ["dgn_symm_L3", "dgn_symm_alias_L3", "dgn_symm_norm_L3"]
+OPTION_CASES = ["dgn_damp_sched_L3", "dgn_norm_L3"]
 
 
 def start_of(g):
@@ -104,6 +105,21 @@ def test_dgn_inner_als_direct_match_reference(name):
     np.testing.assert_allclose(er, g["errors"], rtol=1e-7, atol=1e-13)
     np.testing.assert_allclose(ss, g["step_sizes"], rtol=1e-6, atol=1e-13)
     np.testing.assert_allclose(gr, g["gradients"], rtol=1e-6, atol=1e-12)   # NaN for 'als' steps
+    np.testing.assert_allclose(orc.cpd2flat(bf), g["best_x"], rtol=1e-6, atol=1e-9)
+
+
+@pytest.mark.parametrize("name", OPTION_CASES)
+def test_dgn_options_match_reference(name):
+    """A damping schedule (``init_damp`` as a list, GaussNewton.py:110-111,
+    490-495) and ``factors_norm`` (Conversion.py:439-442) on the CG path."""
+    g = load_golden(name)
+    R = int(g["R"])
+    np.random.seed(int(g["seed"]))
+    bf, ss, er, im, gr, st = orc.dGN(g["T"], start_of(g), R, _opts(g))
+    assert st == int(g["stop"])
+    assert len(er) == len(g["errors"])
+    np.testing.assert_allclose(er, g["errors"], rtol=1e-7, atol=1e-13)
+    np.testing.assert_allclose(ss, g["step_sizes"], rtol=1e-6, atol=1e-13)
     np.testing.assert_allclose(orc.cpd2flat(bf), g["best_x"], rtol=1e-6, atol=1e-9)
 
 
