@@ -1,0 +1,100 @@
+"""Conversions of Tensor Fox's public namespace that users of the CPD path call
+on its results (Conversion.py:52-141, 207-315): ``cpd2tens``, ``cpd2unfold1``,
+``unfold``, ``foldback``.
+
+``cpd2tens`` forms the tensor on the device (``tfx_cp_full``).  ``unfold`` and
+``foldback`` are index permutations, done on whichever device holds the
+tensor (a NumPy input is permuted on the GPU and returned as NumPy, like the
+reference's arrays).  The mode-m unfolding uses Kolda's column order
+(Critical.py:124+): the column of entry (i_1, ..., i_L) is
+sum_{k != m} i_k prod_{j < k, j != m} d_j, so the remaining axes are flattened
+with the first one varying fastest.
+"""
+import numpy as np
+import torch
+
+from . import _dev
+
+
+def _as_tensor(T):
+    """(tensor, was_numpy): NumPy input goes to the GPU as float64."""
+    if isinstance(T, torch.Tensor):
+        return T, False
+    return _dev.to_device(np.asarray(T), torch.float64), True
+
+
+def unfold_tensor(t, mode):
+    """Mode-``mode`` (1-based) unfolding of a torch tensor, same device, as a
+    (d_mode, N / d_mode) tensor in Kolda's column order."""
+    L = t.dim()
+    m = int(mode) - 1
+    if not 0 <= m < L:
+        raise ValueError("mode must be between 1 and the order of the tensor")
+    rest = [k for k in range(L) if k != m]
+    # the remaining axes reversed and flattened row-major = flattened with the
+    # first remaining axis fastest
+    return t.permute(m, *reversed(rest)).reshape(t.shape[m], -1)
+
+
+def foldback_tensor(Tl, mode, dims):
+    """Inverse of ``unfold_tensor``: the tensor of shape ``dims``."""
+    L = len(dims)
+    m = int(mode) - 1
+    if not 0 <= m < L:
+        raise ValueError("mode must be between 1 and the order of the tensor")
+    rest = [k for k in range(L) if k != m]
+    order = [m] + list(reversed(rest))
+    t = Tl.reshape([int(dims[k]) for k in order])
+    inv = [0] * L
+    for pos, k in enumerate(order):
+        inv[k] = pos
+    return t.permute(*inv).contiguous()
+
+
+def unfold(T, mode):
+    """Drop-in for Conversion.unfold (Conversion.py:207-228): the mode-``mode``
+    unfolding (1 <= mode <= L), a Fortran-ordered NumPy array for NumPy input,
+    a device tensor for a torch tensor."""
+    t, was_np = _as_tensor(T)
+    out = unfold_tensor(t, mode)
+    if was_np:
+        return np.asfortranarray(out.cpu().numpy())
+    return out
+
+
+def foldback(T, Tl, mode):
+    """Drop-in for Conversion.foldback (Conversion.py:305-315): fills ``T``
+    (whose shape gives the dimensions) from its mode-``mode`` unfolding ``Tl``
+    and returns it."""
+    dims = tuple(int(d) for d in T.shape)
+    tl, was_np = _as_tensor(Tl)
+    out = foldback_tensor(tl, mode, dims)
+    if isinstance(T, torch.Tensor):
+        T.copy_(out.to(device=T.device, dtype=T.dtype))
+        return T
+    T[...] = out.cpu().numpy()
+    return T
+
+
+def cpd2tens(factors):
+    """Drop-in for Conversion.cpd2tens (Conversion.py:52-79): the tensor of the
+    CPD ``factors`` ((d_l, R) arrays), formed on the device in FP64 and returned
+    as NumPy (torch factors give a device tensor of their dtype)."""
+    from .autograd import cp_full
+    if all(isinstance(W, torch.Tensor) for W in factors):
+        return cp_full([W.to(device=_dev.device()) for W in factors])
+    Wd = [_dev.to_device(np.asarray(W, dtype=np.float64), torch.float64) for W in factors]
+    return cp_full(Wd).cpu().numpy()
+
+
+def cpd2unfold1(T1_approx, factors):
+    """Drop-in for Conversion.cpd2unfold1 (Conversion.py:117-141): the first
+    unfolding of the CPD's tensor, written into ``T1_approx`` and returned."""
+    from .autograd import cp_full
+    Wd = [_dev.to_device(np.asarray(W, dtype=np.float64), torch.float64) for W in factors]
+    out = unfold_tensor(cp_full(Wd), 1)
+    if isinstance(T1_approx, torch.Tensor):
+        T1_approx.copy_(out.to(device=T1_approx.device, dtype=T1_approx.dtype))
+        return T1_approx
+    T1_approx[...] = out.cpu().numpy()
+    return T1_approx

@@ -1,0 +1,24 @@
+"""The conversions users of the CPD path call on its results (cpd2tens,
+cpd2unfold1, unfold, foldback) on the device vs the oracle."""
+import numpy as np
+import pytest
+
+import tfx_oracle as orc
+
+pytestmark = pytest.mark.gpu
+
+tfx = pytest.importorskip("tensorfox_gb300")
+
+
+def test_cpd2tens_and_unfoldings_vs_oracle():
+    rng = np.random.default_rng(11)
+    dims, R = (6, 5, 4, 3), 3
+    W = [rng.standard_normal((d, R)) for d in dims]
+    T = tfx.cpd2tens(W)
+    np.testing.assert_allclose(T, orc.cpd2tens(W), rtol=1e-12, atol=1e-12)
+    for m in range(1, 5):
+        np.testing.assert_array_equal(tfx.unfold(T, m), orc.unfold(T, m))
+        back = tfx.foldback(np.empty(dims), tfx.unfold(T, m), m)
+        np.testing.assert_array_equal(back, T)
+    T1 = np.empty((dims[0], int(np.prod(dims[1:]))))
+    np.testing.assert_allclose(tfx.cpd2unfold1(T1, W), orc.cpd2unfold1(W), rtol=1e-12, atol=1e-12)
