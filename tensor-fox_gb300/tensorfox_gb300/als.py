@@ -9,7 +9,6 @@ until the reference's stop tests fire on the device.
 """
 import ctypes
 
-import numpy as np
 import torch
 
 from . import _dev, _lib

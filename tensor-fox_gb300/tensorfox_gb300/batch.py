@@ -24,7 +24,7 @@ import numpy as np
 import torch
 
 from . import _dev, _lib, tuner
-from .api import Output, consistency, sort_dims
+from .api import Output, consistency
 from .gauss_newton import _inner_of
 from .options import make_options
 

@@ -18,8 +18,6 @@ import torch
 
 from . import _dev, _lib, kernels
 from .compression import clean_compression, top_eig, _draw_omega
-from .gauss_newton import _Batch, advance_rng, auto_cluster
-from .options import make_options
 
 
 def _vp(t):
