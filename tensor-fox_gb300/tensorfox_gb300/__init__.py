@@ -16,4 +16,4 @@ from .sweeps import rank, stats  # noqa: F401,E402
 from .distributed import cpd_batch_distributed  # noqa: F401,E402
 from .sparse import DeviceCOO, coo_mttkrp, sparse_residual_sq  # noqa: F401,E402
 from .autograd import cp_reconstruct, cp_fit_loss, mttkrp  # noqa: F401,E402
-from .conversion import cpd2tens, cpd2unfold1, unfold, foldback  # noqa: F401,E402
+from .conversion import cpd2tens, cpd2unfold1, unfold, foldback, dense2sparse, sparse2dense  # noqa: F401,E402

@@ -1,6 +1,7 @@
 """Conversions of Tensor Fox's public namespace that users of the CPD path call
-on its results (Conversion.py:52-141, 207-315): ``cpd2tens``, ``cpd2unfold1``,
-``unfold``, ``foldback``.
+on its inputs and results (Conversion.py:52-315): ``cpd2tens``, ``cpd2unfold1``,
+``unfold``, ``foldback``, and the COO converters ``dense2sparse`` /
+``sparse2dense`` of the sparse input format ``[data, idxs, dims]``.
 
 ``cpd2tens`` forms the tensor on the device (``tfx_cp_full``).  ``unfold`` and
 ``foldback`` are index permutations, done on whichever device holds the
@@ -98,3 +99,39 @@ def cpd2unfold1(T1_approx, factors):
         return T1_approx
     T1_approx[...] = out.cpu().numpy()
     return T1_approx
+
+
+def dense2sparse_tensor(t):
+    """(values, indices (nnz, L) int64) of the nonzero entries of a torch tensor,
+    in row-major (C) order, on its device."""
+    idx = torch.nonzero(t)
+    return t[tuple(idx.t())], idx
+
+
+def sparse2dense_tensor(vals, idx, dims, dtype=torch.float64):
+    """Dense tensor of shape ``dims`` from values and (nnz, L) indices on the
+    same device (a repeated coordinate keeps the sum of its values)."""
+    out = torch.zeros([int(d) for d in dims], dtype=dtype, device=vals.device)
+    if idx.numel():
+        out.index_put_(tuple(idx.t().long()), vals.to(dtype), accumulate=True)
+    return out
+
+
+def dense2sparse(T):
+    """Drop-in for Conversion.dense2sparse (Conversion.py:174-204):
+    ``[data, idxs, dims]`` of the nonzero entries of ``T``, in row-major order."""
+    if isinstance(T, torch.Tensor):
+        t = T
+    else:
+        arr = np.asarray(T)
+        t = _dev.to_device(arr, torch.float32 if arr.dtype == np.float32 else torch.float64)
+    vals, idx = dense2sparse_tensor(t)
+    return [vals.cpu().numpy(), idx.cpu().numpy(), list(int(d) for d in t.shape)]
+
+
+def sparse2dense(data, idxs, dims):
+    """Drop-in for Conversion.sparse2dense (Conversion.py:144-171): the dense
+    FP64 tensor of ``[data, idxs, dims]``."""
+    vals = _dev.to_device(np.asarray(data, dtype=np.float64), torch.float64)
+    idx = torch.as_tensor(np.asarray(idxs, dtype=np.int64).reshape(-1, len(dims)), device=vals.device)
+    return sparse2dense_tensor(vals, idx, dims).cpu().numpy()

@@ -36,3 +36,22 @@ def test_foldback_fills_the_given_array():
 def test_mode_out_of_range():
     with pytest.raises(ValueError):
         conv.unfold_tensor(torch.zeros(2, 3), 3)
+
+
+def test_dense2sparse_row_major_and_back():
+    rng = np.random.default_rng(12)
+    T = rng.standard_normal((4, 3, 5))
+    T[rng.random(T.shape) < 0.6] = 0.0
+    vals, idx = conv.dense2sparse_tensor(torch.from_numpy(T))
+    nz = np.nonzero(T)                      # the reference's order (Conversion.py:174-204)
+    np.testing.assert_array_equal(idx.numpy(), np.stack(nz, axis=1))
+    np.testing.assert_array_equal(vals.numpy(), T[nz])
+    back = conv.sparse2dense_tensor(vals, idx, T.shape)
+    np.testing.assert_array_equal(back.numpy(), T)
+
+
+def test_sparse2dense_sums_repeated_coordinates():
+    vals = torch.tensor([1.0, 2.0, 5.0], dtype=torch.float64)
+    idx = torch.tensor([[0, 1], [0, 1], [1, 0]])
+    out = conv.sparse2dense_tensor(vals, idx, (2, 2))
+    np.testing.assert_array_equal(out.numpy(), [[0.0, 3.0], [5.0, 0.0]])

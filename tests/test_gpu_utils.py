@@ -22,3 +22,15 @@ def test_cpd2tens_and_unfoldings_vs_oracle():
         np.testing.assert_array_equal(back, T)
     T1 = np.empty((dims[0], int(np.prod(dims[1:]))))
     np.testing.assert_allclose(tfx.cpd2unfold1(T1, W), orc.cpd2unfold1(W), rtol=1e-12, atol=1e-12)
+
+
+def test_dense2sparse_sparse2dense_vs_reference_rules():
+    rng = np.random.default_rng(13)
+    T = rng.standard_normal((5, 4, 3))
+    T[rng.random(T.shape) < 0.5] = 0.0
+    data, idxs, dims = tfx.dense2sparse(T)
+    nz = np.nonzero(T)
+    np.testing.assert_array_equal(idxs, np.stack(nz, axis=1))
+    np.testing.assert_array_equal(data, T[nz])
+    assert dims == [5, 4, 3]
+    np.testing.assert_array_equal(tfx.sparse2dense(data, idxs, dims), T)
