@@ -2,7 +2,8 @@
 
 Drop-in functions (same names, arguments and return values as Tensor Fox 1.2.1):
 ``cpd``, ``mlsvd``, ``dGN``, ``als``, ``rank``, ``stats``, ``make_options``, ``cpd2tens``, ``cpd2unfold1``,
-``unfold``, ``foldback``.  All computation runs in ``libtfx_gb300.so`` on the GPU.
+``unfold``, ``foldback``, ``dense2sparse``, ``sparse2dense``, ``multilin_mult``, ``multilin_mult_cpd``,
+``sparse_multilin_mult``.  All computation runs in ``libtfx_gb300.so`` on the GPU.
 """
 __version__ = "1.2.1+gb300"
 
@@ -16,4 +17,5 @@ from .sweeps import rank, stats  # noqa: F401,E402
 from .distributed import cpd_batch_distributed  # noqa: F401,E402
 from .sparse import DeviceCOO, coo_mttkrp, sparse_residual_sq  # noqa: F401,E402
 from .autograd import cp_reconstruct, cp_fit_loss, mttkrp  # noqa: F401,E402
-from .conversion import cpd2tens, cpd2unfold1, unfold, foldback, dense2sparse, sparse2dense  # noqa: F401,E402
+from .conversion import (cpd2tens, cpd2unfold1, unfold, foldback, dense2sparse, sparse2dense,  # noqa: F401,E402
+                         multilin_mult, multilin_mult_cpd, sparse_multilin_mult)

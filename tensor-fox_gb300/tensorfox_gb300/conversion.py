@@ -135,3 +135,43 @@ def sparse2dense(data, idxs, dims):
     vals = _dev.to_device(np.asarray(data, dtype=np.float64), torch.float64)
     idx = torch.as_tensor(np.asarray(idxs, dtype=np.int64).reshape(-1, len(dims)), device=vals.device)
     return sparse2dense_tensor(vals, idx, dims).cpu().numpy()
+
+
+def multilin_mult(UT, T1, dims):
+    """Drop-in for MultilinearAlgebra.multilin_mult (MultilinearAlgebra.py:72-105):
+    (U[0]^T, ..., U[L-1]^T) * T from the first unfolding ``T1`` of T (shape
+    ``dims``); UT[l] is (n_l, d_l).  The mode products run on the device
+    (``tfx_ttm``) in FP64; returns NumPy."""
+    from . import kernels
+    dims = [int(d) for d in dims]
+    t1, _ = _as_tensor(T1)
+    S = foldback_tensor(t1.to(torch.float64), 1, dims)
+    cur = list(dims)
+    for l in range(len(dims)):
+        Ut = _dev.to_device(np.asarray(UT[l], dtype=np.float64), torch.float64)
+        S, cur = kernels.ttm(S.contiguous(), cur, l, Ut)
+    return S.reshape(cur).cpu().numpy()
+
+
+def multilin_mult_cpd(U, W, dims):
+    """Drop-in for MultilinearAlgebra.multilin_mult_cpd (MultilinearAlgebra.py:42-69):
+    the tensor of the CPD (U[0] W[0], ..., U[L-1] W[L-1])."""
+    from . import kernels
+    from .autograd import cp_full
+    UW = []
+    for Ul, Wl in zip(U, W):
+        Ud = _dev.to_device(np.asarray(Ul, dtype=np.float64), torch.float64)
+        Wd = _dev.to_device(np.asarray(Wl, dtype=np.float64), torch.float64)
+        UW.append(kernels.matmul(Ud, Wd))
+    return cp_full(UW).cpu().numpy()
+
+
+def sparse_multilin_mult(UT, data, idxs, dims):
+    """Drop-in for MultilinearAlgebra.sparse_multilin_mult (MultilinearAlgebra.py:
+    145-190): the dense core (U[0]^T, ..., U[L-1]^T) * T of the COO tensor
+    ``[data, idxs, dims]``, UT[l] (n_l, d_l), computed on the device in FP64
+    (``tfx_sparse_ttmc``); returns NumPy."""
+    from .sparse import DeviceCOO, sparse_ttmc
+    X = DeviceCOO(data, idxs, dims, torch.float64)
+    Uts = [_dev.to_device(np.asarray(u, dtype=np.float64), torch.float64) for u in UT]
+    return sparse_ttmc(X, Uts).cpu().numpy()

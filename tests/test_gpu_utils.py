@@ -34,3 +34,23 @@ def test_dense2sparse_sparse2dense_vs_reference_rules():
     np.testing.assert_array_equal(data, T[nz])
     assert dims == [5, 4, 3]
     np.testing.assert_array_equal(tfx.sparse2dense(data, idxs, dims), T)
+
+
+def test_multilinear_products_vs_oracle():
+    """multilin_mult / multilin_mult_cpd / sparse_multilin_mult
+    (MultilinearAlgebra.py:42-190) on the device vs the oracle."""
+    rng = np.random.default_rng(14)
+    dims = (6, 5, 4)
+    T = rng.standard_normal(dims)
+    UT = [rng.standard_normal((n, d)) for n, d in zip((3, 2, 4), dims)]
+    np.testing.assert_allclose(tfx.multilin_mult(UT, orc.unfold(T, 1), dims), orc.multilin_mult(UT, T),
+                               rtol=1e-12, atol=1e-12)
+    U = [u.T for u in UT]
+    W = [rng.standard_normal((n, 2)) for n in (3, 2, 4)]
+    np.testing.assert_allclose(tfx.multilin_mult_cpd(U, W, (3, 2, 4)),
+                               orc.cpd2tens([u @ w for u, w in zip(U, W)]), rtol=1e-12, atol=1e-12)
+    lin = rng.choice(int(np.prod(dims)), size=40, replace=False)
+    idxs = np.stack(np.unravel_index(lin, dims), axis=1)
+    data = rng.standard_normal(40)
+    np.testing.assert_allclose(tfx.sparse_multilin_mult(UT, data, idxs, dims),
+                               orc.sparse_multilin_mult(UT, data, idxs, dims), rtol=1e-10, atol=1e-12)
