@@ -12,7 +12,8 @@ already in device memory; ``e2e`` is the same call from pinned host memory with
 the host->device copy of the tensor and the device->host copy of the factors
 inside the timed region.  The tensor (537 MB) is larger than the 129 MB L2, so
 no explicit flush is needed between steps.  ``--impl reference`` times the CPU
-oracle (the reference's algorithm restated in NumPy) on the host cores.
+oracle (the reference's algorithm restated in NumPy, FP64) running the same
+512^3 workload on the host cores, one full ``cpd`` per step.
 """
 import argparse
 import json
@@ -62,9 +63,19 @@ class Clocks:
         self.proc = None
         self.lines = []
 
+    def _smi_id(self):
+        """nvidia-smi numbers GPUs in PCI order and ignores CUDA_VISIBLE_DEVICES,
+        so the GPU is named by its UUID."""
+        try:
+            import torch
+            u = str(torch.cuda.get_device_properties(self.index).uuid)
+            return u if u.startswith("GPU-") else "GPU-" + u
+        except Exception:
+            return str(self.index)
+
     def __enter__(self):
         try:
-            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", self._smi_id(), "--query-gpu=" + self.Q,
                                           "--format=csv,noheader,nounits", "-lms", "200"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
@@ -135,34 +146,22 @@ def peaks():
         return 6800.0, 1900.0, "fallback"
 
 
-SAMPLE_DIMS = (256, 256, 256)
-
-
 def cpu_reference_step(T, R):
-    """One full CPU-oracle cpd of ``T``; returns (seconds, output, phase timings)."""
+    """One full CPU-oracle cpd of the FP32 tensor ``T`` (the FP64 cast included,
+    as the reference casts inside ``unfold``); returns (seconds, factors, output,
+    phase timings)."""
     import tfx_oracle as orc
     np.random.seed(0)
     tm = {}
     t0 = time.perf_counter()
-    _, out = orc.cpd(T.astype(np.float64), R, timings=tm)
-    return time.perf_counter() - t0, out, tm
+    f, out = orc.cpd(T.astype(np.float64), R, timings=tm)
+    return time.perf_counter() - t0, f, out, tm
 
 
-def cpu_sample(R=RANK):
-    """Bounded CPU sample: the same workload at 256^3 (1/8 of the entries).
-
-    The size-dependent phases (conversion, MLSVD, final residual) are scaled by
-    the entry ratio; the dGN phase runs on the rank-sized core, whose size does
-    not depend on the tensor's, and is kept as measured.  Returns
-    (estimated seconds at 512^3, measured seconds, output, description)."""
-    Ts, _ = make_problem(dims=SAMPLE_DIMS)
-    dt, out, tm = cpu_reference_step(Ts, R)
-    ratio = float(np.prod(DIMS)) / float(np.prod(SAMPLE_DIMS))
-    est = ratio * (tm.get('prepare', 0) + tm.get('mlsvd', 0) + tm.get('final', 0)) + tm.get('dgn', 0)
-    desc = ("one full cpd of the same workload at 256^3 (NumPy oracle, FP64): %.2f s measured "
-            "(mlsvd %.2f, dgn %.2f, final %.2f); size-dependent phases scaled x%d to 512^3"
-            % (dt, tm.get('mlsvd', 0), tm.get('dgn', 0), tm.get('final', 0), int(ratio)))
-    return est, dt, out, desc
+def cpu_desc(dt, tm):
+    return ("one full cpd of the same 512^3 rank-50 tensor by the FP64 NumPy oracle (the reference's "
+            "algorithm): %.2f s (mlsvd %.2f, dgn %.2f, final error %.2f)"
+            % (dt, tm.get('mlsvd', 0), tm.get('dgn', 0), tm.get('final', 0)))
 
 
 def run_reference(args):
@@ -171,22 +170,36 @@ def run_reference(args):
     if rank != 0:
         return
     cores = os.cpu_count()
+    T, _ = make_problem()
     times = []
     out = None
     desc = ""
     for i in range(args.warmup + args.steps):
-        est, dt, out, desc = cpu_sample()
+        dt, _, out, tm = cpu_reference_step(T, RANK)
         if i >= args.warmup:
-            times.append(est)
+            times.append(dt)
+            desc = cpu_desc(dt, tm)
     v = float(np.mean(times))
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "s", "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": v * 1e3, "higher_is_better": False, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": {"workload": WORKLOAD, "global_batch": 1, "parallelism": "replicas"},
             "rel_error": float(out.rel_error), "num_steps": int(out.num_steps),
-            "cpu_baseline": {"value": v, "unit": "s", "cores": cores, "kind": "port", "sample": desc},
+            "cpu_baseline": {"value": v, "unit": "s", "cores": cores, "kind": "port",
+                             "sample": "each step " + desc + "; mean of %d steps" % args.steps},
             "e2e": {"value": v, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+def congruence(A, B):
+    """Smallest over matched columns of the product over modes of |cos|."""
+    from scipy.optimize import linear_sum_assignment
+    R = A[0].shape[1]
+    C = np.ones((R, R))
+    for a, b in zip(A, B):
+        C *= np.abs((a / np.linalg.norm(a, axis=0)).T @ (b / np.linalg.norm(b, axis=0)))
+    r, c = linear_sum_assignment(-C)
+    return float(C[r, c].min())
 
 
 def run_ours(args):
@@ -273,24 +286,12 @@ def run_ours(args):
     p0.record(stream)
     for _ in range(max(1, args.steps // 2)):
         np.random.seed(0)
-        _, out_plain = tfx.cpd(Td, R, plain)
+        f_plain, out_plain = tfx.cpd(Td, R, plain)
     p1.record(stream)
     barrier()
     t_plain = p0.elapsed_time(p1) / 1e3 / max(1, args.steps // 2)
 
-    # dominant dense kernel: the tcgen05 mode-1 Gram of the 512 x 262144 unfolding,
-    # timed alone with CUDA events on the launching stream
-    nrep = 20
-    for _ in range(3):
-        kernels.mode_gram_tc(Td, list(DIMS), 0)
-    torch.cuda.synchronize()
-    g0, g1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    g0.record(stream)
-    for _ in range(nrep):
-        kernels.mode_gram_tc(Td, list(DIMS), 0)
-    g1.record(stream)
-    torch.cuda.synchronize()
-    t_gram = g0.elapsed_time(g1) / 1e3 / nrep
+    kern = kernel_rooflines(Td, R, opts, t_dev)
 
     batched = run_batched(args) if not args.no_batched else None
     sparse_leg = run_sparse(args) if not args.no_sparse else None
@@ -300,22 +301,32 @@ def run_ours(args):
     inner_leg = run_inner(args) if not args.no_batched else None
     clk.__exit__(None, None, None)
     clk_summary = clk.summary()
-    flops = 2.0 * DIMS[0] * DIMS[0] * DIMS[1] * DIMS[2]
-    hbm, bf16, src = peaks()
-    achieved_tf = flops / t_gram / 1e12
-    # DRAM traffic of one launch, from the ncu capture of the small case
-    # (profiles/k_gram_tc2_mode0_512x128x512.md: 134.60 MB read + 3.43 MB written
-    # for a 134 MB input) scaled by the input size, which the traffic follows
-    # (the tensor crosses HBM once; the partials grow with the split count only)
-    traffic = (134.60e6 + 3.43e6) * (float(np.prod(DIMS)) * 4 / (512 * 128 * 512 * 4))
 
-    # congruence with the planted factors and the FP64 oracle error of the result
+    # the FP64 oracle on the same tensor (the CPU baseline run): its error, the
+    # GPU result's error re-measured in FP64 and the congruences
     fl = outs[-1]
     cpu = None
+    check = None
     if rank == 0 and not args.no_cpu_baseline:
         sys.path.insert(0, os.path.join(ROOT, "oracle"))
-        est, dt_cpu, out_cpu, desc = cpu_sample(R)
-        cpu = {"value": est, "unit": "s", "cores": os.cpu_count(), "kind": "port", "sample": desc}
+        import tfx_oracle as orc
+        dt_cpu, f_cpu, out_cpu, tm = cpu_reference_step(T, R)
+        cpu = {"value": dt_cpu, "unit": "s", "cores": os.cpu_count(), "kind": "port", "sample": cpu_desc(dt_cpu, tm)}
+        T64 = T.astype(np.float64)
+        U1 = orc.unfold(T64, 1)
+        nT = np.linalg.norm(T64)
+        e_mixed = orc.fastnorm(U1, orc.cpd2unfold1(f)) / nT
+        e_plain = orc.fastnorm(U1, orc.cpd2unfold1(f_plain)) / nT
+        check = {"fp64_oracle_rel_error": float(out_cpu.rel_error), "fp64_oracle_num_steps": int(out_cpu.num_steps),
+                 "mixed_rel_error_reported": float(fl.rel_error), "mixed_rel_error_fp64": float(e_mixed),
+                 "plain_fp32_rel_error_fp64": float(e_plain),
+                 "mixed_vs_oracle_rel_diff": float(abs(e_mixed - out_cpu.rel_error) / out_cpu.rel_error),
+                 "congruence_mixed_vs_oracle": congruence(f, f_cpu),
+                 "congruence_mixed_vs_planted": congruence(f, [w.astype(np.float64) for w in Wp]),
+                 "congruence_plain_vs_oracle": congruence(f_plain, f_cpu),
+                 "time_to_1e-6": "not attainable on this tensor: its 40 dB noise puts the best relative "
+                                 "error near 1e-2 (the oracle's own is %.4e); see c1_fp64 for time to 1e-6"
+                                 % out_cpu.rel_error}
 
     line = {"metric": METRIC, "value": t_dev, "unit": "s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t_dev * 1e3, "higher_is_better": False, "scaling": "weak",
@@ -323,15 +334,17 @@ def run_ours(args):
             "config": {"workload": WORKLOAD, "global_batch": world, "parallelism": "replicas",
                        "l2_flush": "none: 537 MB tensor exceeds the 129 MB L2"},
             "rel_error": float(fl.rel_error), "num_steps": int(fl.num_steps), "stop": [int(s) for s in fl.stop],
-            "plain_fp32": {"value": t_plain, "unit": "s", "rel_error": float(out_plain.rel_error)},
+            "plain_fp32": {"value": t_plain, "unit": "s", "rel_error": float(out_plain.rel_error),
+                           "num_steps": int(out_plain.num_steps), "mixed_speedup": t_plain / t_dev},
             "e2e": {"value": t_e2e, "unit": "s", "h2d_bytes_per_step": int(T.nbytes),
                     "d2h_bytes_per_step": int(sum(d * R * 8 for d in DIMS)),
                     "h2d_copy_s": t_h2d, "h2d_GBps": float(T.nbytes) / t_h2d / 1e9},
-            "roofline": {"bound": "tensor", "kernel": "k_gram_tc2 (tcgen05 TF32 mode-1 Gram, 512 x 262144, 2x2 super-blocks, incl. split-K reduce)",
-                         "achieved": achieved_tf, "peak": bf16, "unit": "TFLOP/s", "frac": achieved_tf / bf16,
-                         "traffic": traffic, "peak_source": src + " bf16 dense (TF32 tensor rate is half of it)"},
+            "roofline": kern[0],
+            "roofline_kernels": kern,
             "gpu_launches": int(launches / max(1, args.steps)) * args.steps,
             "clocks": clk_summary}
+    if check is not None:
+        line["oracle_check"] = check
     if cpu is not None:
         line["cpu_baseline"] = cpu
     if batched is not None:
@@ -353,16 +366,101 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
-def run_sparse(args, dims=(20000, 20000, 20000), nnz=10_000_000, R=16, seed=11):
-    """c5: COO MTTKRP and sparse residual at 20000^3 with 1e7 nonzeros, rank 16.
-
-    Algorithmic bytes per MTTKRP mode and per residual pass: nnz * (L*4 + 4) --
-    int32 coordinates (re-encoded once at the boundary) plus an FP32 value; the
-    16-wide factor rows (1.28 MB per mode) are gathered from L2 and not counted.
-    Setup (coordinate encoding, the per-mode counting sorts) is done once before
-    the timed region."""
+def _time_events(fn, reps):
+    """Mean seconds of ``fn()`` over ``reps`` runs, CUDA events on the current stream."""
     import torch
-    from tensorfox_gb300 import sparse as tsp
+    stream = torch.cuda.current_stream()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    a.record(stream)
+    for _ in range(reps):
+        fn()
+    b.record(stream)
+    torch.cuda.synchronize()
+    return a.elapsed_time(b) / 1e3 / reps
+
+
+def kernel_rooflines(Td, R, opts, t_step):
+    """The kernels of one headline CPD, each timed alone on the CPD's own
+    inputs with CUDA events, largest share of the step first.
+
+    Algorithmic bytes / flops per launch (s = 4 bytes, N = 512^3, core 50^3):
+      * dGN engine: per CG iteration s*7*n_x + 8*(L^2+L)*R^2, per outer iteration
+        two passes over the core (gradient, residual) and four factor vectors
+        (2*N_core*s + 4*s*n_x); n_x = R*sum(core dims) = 7500;
+      * tcgen05 mode-1 Gram: 2*512^2*512^2 flop (upper blocks only are computed);
+      * mode-1 truncation product: reads N*s, writes 50*512*512*s;
+      * tcgen05 residual: reads N*s;
+      * eigen-step (orthonormalisations + Jacobi of the 60 x 60 Rayleigh-Ritz
+        matrix, single CTAs): latency bound, no roofline."""
+    import torch
+    from tensorfox_gb300 import kernels, compression, api, gauss_newton, _dev
+    hbm, bf16, src = peaks()
+    out = []
+    N = float(np.prod(DIMS))
+    np.random.seed(0)
+    S, Uts, sig, core = compression.mlsvd_device(Td, R, opts)
+    init = api.starting_point_random(core, R, opts)
+    x0 = torch.from_numpy(_dev.flat_factors(init)).cuda().float()
+    cl = gauss_newton.auto_cluster(tuple(S.shape), R)
+    holder = {}
+
+    def engine():
+        holder["b"] = b = gauss_newton._Batch([S], [x0], [R], opts, "fp32")
+        b.launch(cl)
+    engine()
+    t_eng = _time_events(engine, 5)
+    b = holder["b"]
+    res = b.result[0].cpu().numpy()
+    info = b.info[0].cpu().numpy()
+    iters, mv = int(res[1]), float(info[4])
+    L, Nc = 3, float(np.prod(core))
+    nx = R * sum(core)
+    by_eng = mv * (4 * 7 * nx + 8 * (L * L + L) * R * R) + iters * (2 * Nc * 4 + 4 * 4 * nx)
+    out.append({"kernel": "dgn_kernel<float,4> (cluster-persistent dGN engine, %d CTAs, 50^3 core, rank 50: "
+                          "%d iterations, %d J^T J v products)" % (cl, iters, int(mv)),
+                "bound": "hbm", "achieved": by_eng / t_eng / 1e9, "peak": hbm, "unit": "GB/s",
+                "frac": by_eng / t_eng / 1e9 / hbm, "traffic": None, "ms": t_eng * 1e3, "share": t_eng / t_step,
+                "sms_used": cl, "note": "latency bound: its operands live in shared memory; the HBM roofline "
+                                        "does not bound it"})
+    # tcgen05 mode-1 Gram
+    t_g = _time_events(lambda: kernels.mode_gram_tc(Td, list(DIMS), 0, check=False), 20)
+    fl_g = 2.0 * DIMS[0] * DIMS[0] * DIMS[1] * DIMS[2]
+    # DRAM traffic of one launch from the ncu capture of the 512 x 128 x 512
+    # case (134.60 MB read + 3.43 MB written for a 134 MB input), scaled by the
+    # input size, which the traffic follows
+    traffic = (134.60e6 + 3.43e6) * (N * 4 / (512 * 128 * 512 * 4))
+    out.append({"kernel": "k_gram_tc2 (tcgen05 TF32 mode-1 Gram, 512 x 262144, incl. split-K reduce)",
+                "bound": "tensor", "achieved": fl_g / t_g / 1e12, "peak": bf16, "unit": "TFLOP/s",
+                "frac": fl_g / t_g / 1e12 / bf16, "traffic": traffic, "ms": t_g * 1e3, "share": t_g / t_step,
+                "peak_source": src + " bf16 dense (TF32 tensor rate is half of it)"})
+    # mode-1 truncation product
+    Ut0 = Uts[0]
+    t_t = _time_events(lambda: kernels.ttm(Td, list(DIMS), 0, Ut0), 20)
+    by_t = N * 4 + Ut0.shape[0] * DIMS[1] * DIMS[2] * 4
+    out.append({"kernel": "tfx_ttm mode-1 truncation product (50 x 512 x 262144)", "bound": "hbm",
+                "achieved": by_t / t_t / 1e9, "peak": hbm, "unit": "GB/s", "frac": by_t / t_t / 1e9 / hbm,
+                "traffic": None, "ms": t_t * 1e3, "share": t_t / t_step})
+    # residual on the tensor cores (the final error)
+    Wf = api._decompress(Uts, b.best[0], core, R)
+    t_r = _time_events(lambda: kernels.cp_residual_sq(Td, list(DIMS), Wf, R), 20)
+    out.append({"kernel": "k_residual_tc (tcgen05 3xTF32 ||T - [[W]]||^2, 512^3, rank 50)", "bound": "hbm",
+                "achieved": N * 4 / t_r / 1e9, "peak": hbm, "unit": "GB/s", "frac": N * 4 / t_r / 1e9 / hbm,
+                "traffic": None, "ms": t_r * 1e3, "share": t_r / t_step})
+    # eigen-step of one 512-row mode (Krylov block, Rayleigh-Ritz, Jacobi)
+    G = kernels.mode_gram_tc(Td, list(DIMS), 0)
+    om = np.random.default_rng(0).standard_normal((512, 60))
+    t_e = _time_events(lambda: compression.top_eig(G, 50, om, host=False), 10)
+    out.append({"kernel": "eigen-step of a 512 x 512 Gram (k_orth_bcgs x3, Rayleigh-Ritz, k_jacobi 60 x 60)",
+                "bound": "latency", "achieved": None, "peak": None, "unit": None, "frac": None, "traffic": None,
+                "ms": t_e * 1e3, "share": 3 * t_e / t_step, "note": "three per CPD (one per mode)"})
+    out.sort(key=lambda k: -k["share"])
+    return out
+
+
+def make_coo(dims, nnz, R, seed):
+    """``nnz`` distinct uniform coordinates (int64) of ``dims``; FP32 values of a
+    planted rank-R N(0,1) model at them plus 1% Gaussian noise."""
     rng = np.random.default_rng(seed)
     L = len(dims)
     space = int(np.prod(np.array(dims, dtype=np.int64)))
@@ -378,6 +476,21 @@ def run_sparse(args, dims=(20000, 20000, 20000), nnz=10_000_000, R=16, seed=11):
         vals *= W[l][idx[:, l]]
     vals = vals.sum(axis=1)
     vals += 0.01 * np.linalg.norm(vals) / np.sqrt(vals.size) * rng.standard_normal(vals.size).astype(np.float32)
+    return vals, idx, W
+
+
+def run_sparse(args, dims=(20000, 20000, 20000), nnz=10_000_000, R=16, seed=11):
+    """c5: COO MTTKRP and sparse residual at 20000^3 with 1e7 nonzeros, rank 16.
+
+    Algorithmic bytes per MTTKRP mode and per residual pass: nnz * (L*4 + 4) --
+    int32 coordinates (re-encoded once at the boundary) plus an FP32 value; the
+    16-wide factor rows (1.28 MB per mode) are gathered from L2 and not counted.
+    Setup (coordinate encoding, the per-mode counting sorts) is done once before
+    the timed region."""
+    import torch
+    from tensorfox_gb300 import sparse as tsp
+    vals, idx, W = make_coo(dims, nnz, R, seed)
+    L = len(dims)
     X = tsp.DeviceCOO(vals, idx, dims, torch.float32)
     Wd = [torch.from_numpy(w).cuda() for w in W]
     for l in range(L):
@@ -504,7 +617,13 @@ def run_inner(args, seed=102):
 def run_c1(args, seed=101):
     """c1: plain dGN CPD of a dense FP64 100^3 tensor at rank 10 (planted N(0,1)
     factors, noise 1e-6 relative, default options): the FP64 GPU path against the
-    FP64 NumPy oracle on the host cores, both timed on the same input."""
+    FP64 NumPy oracle on the host cores, both timed on the same input.
+
+    Time to relative error 1e-6: the full run's per-iteration errors (of the
+    compressed core) give, with the energy the compression leaves out, the full
+    tensor's error after every iteration; the first iteration k at which it is
+    below 1e-6 is found, and a run with maxiter = k + 1 (so it stops there) is
+    timed on the GPU and on the host, its final error checked to be below 1e-6."""
     import torch
     import tensorfox_gb300 as tfx
     rng = np.random.default_rng(seed)
@@ -514,19 +633,42 @@ def run_c1(args, seed=101):
     E = rng.standard_normal(dims)
     T += 1e-6 * np.linalg.norm(T) / np.linalg.norm(E) * E
     Td = torch.from_numpy(T).cuda()
-    for _ in range(2):
-        np.random.seed(0)
-        tfx.cpd(Td, R, None)
-    torch.cuda.synchronize()
-    reps = 3
-    t0 = time.perf_counter()
-    for _ in range(reps):
-        np.random.seed(0)
-        _, out = tfx.cpd(Td, R, None)
-    torch.cuda.synchronize()
-    t_gpu = (time.perf_counter() - t0) / reps
+
+    def gpu_time(o, reps=3):
+        for _ in range(2):
+            np.random.seed(0)
+            tfx.cpd(Td, R, o)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            np.random.seed(0)
+            _, out = tfx.cpd(Td, R, o)
+        torch.cuda.synchronize()
+        return (time.perf_counter() - t0) / reps, out
+    t_gpu, out = gpu_time(None)
     res = {"workload": "dense FP64 100x100x100, rank 10, noise 1e-6, default options",
            "gpu_s": t_gpu, "gpu_rel_error": float(out.rel_error), "gpu_steps": int(out.num_steps)}
+    # the full tensor's error after every iteration: ||T||^2 = ||S||^2 + the energy
+    # outside the core, so e_full^2 = (e_core^2 ||S||^2 + ||T||^2 - ||S||^2) / ||T||^2
+    from tensorfox_gb300 import compression
+    o = tfx.make_options(None)
+    np.random.seed(0)
+    S, _, _, _ = compression.mlsvd_device(Td, R, o)
+    nS2 = float((S.double() ** 2).sum().item())
+    nT2 = float(np.sum(T * T))
+    er = np.asarray(out.errors[0])
+    full = np.sqrt(np.maximum(er ** 2 * nS2 + nT2 - nS2, 0.0) / nT2)
+    hit = np.nonzero(full < 1e-6)[0]
+    ttt = {"threshold": 1e-6}
+    if hit.size:
+        k = int(hit[0])
+        o1 = tfx.make_options(None)
+        o1.maxiter = k + 1
+        t1, out1 = gpu_time(o1)
+        ttt.update({"iterations": k + 1, "gpu_s": t1, "gpu_rel_error": float(out1.rel_error),
+                    "reached": bool(out1.rel_error < 1e-6)})
+    else:
+        ttt["reached"] = False
     if not args.no_cpu_baseline:
         sys.path.insert(0, os.path.join(ROOT, "oracle"))
         import tfx_oracle as orc
@@ -535,15 +677,26 @@ def run_c1(args, seed=101):
         _, oc = orc.cpd(T, R, None)
         res.update({"cpu_oracle_s": time.perf_counter() - t0, "cpu_rel_error": float(oc.rel_error),
                     "cpu_cores": os.cpu_count()})
+        if hit.size:
+            oo = orc.make_options(None)
+            oo.maxiter = int(hit[0]) + 1
+            np.random.seed(0)
+            t0 = time.perf_counter()
+            _, oc1 = orc.cpd(T, R, oo)
+            ttt.update({"cpu_oracle_s": time.perf_counter() - t0, "cpu_rel_error": float(oc1.rel_error)})
+    res["time_to_1e-6"] = ttt
     return res
 
 
-def run_batched(args, n=4096, seed=7):
+def run_batched(args, n=4096, seed=7, n_serial=256):
     """c4-style batch: n small FP32 CPDs (dims U[8,64], rank U[2,12], noise 1e-4).
 
-    Reports the batch wall time and the engine's J^T J v throughput in the
-    algorithmic-bytes sense: bytes_mv = s*3*n_x + 8*L^2*R^2 per product, summed
-    over every product the engine ran, divided by the engine's share of the time."""
+    Reports the batch wall time, the J^T J v throughput of the engine in the
+    algorithmic-bytes sense (bytes_mv = s*3*n_x + 8*L^2*R^2 per product, summed
+    over every product the engine ran, divided by the whole batch's wall time),
+    and the batched form against the plain form on the same inputs: the first
+    ``n_serial`` problems solved one ``cpd`` call at a time on the GPU (the
+    serial loop of the reference's rank/stats drivers) and as one batch."""
     import torch
     import tensorfox_gb300 as tfx
     rng = np.random.default_rng(seed)
@@ -574,17 +727,40 @@ def run_batched(args, n=4096, seed=7):
         from tensorfox_gb300.distributed import max_over_ranks
         t = max_over_ranks([t], device=torch.device("cuda", torch.cuda.current_device()))[0]
     errs = np.array([op.rel_error for _, op in outs])
-    # J^T J v products the engine ran (counted on the device), with the
-    # algorithmic bytes of each: read W and v, write z (s*3*n_x) and the FP64
-    # R x R Gram Hadamards (8*L^2*R^2)
     nmv, nbytes = 0, 0.0
     for (f, op), R in zip(outs, Rs):
         nx = R * sum(op.core_dims)
         nmv += op.matvecs
         nbytes += op.matvecs * (4 * 3 * nx + 8 * 9 * R * R)
-    return {"problems": n, "seconds": t, "median_rel_error": float(np.median(errs)),
-            "frac_below_1e-3": float(np.mean(errs < 1e-3)), "matvecs": int(nmv),
-            "matvec_GBps_vs_batch_time": nbytes / t / 1e9}
+    res = {"problems": n, "seconds": t, "median_rel_error": float(np.median(errs)),
+           "frac_below_1e-3": float(np.mean(errs < 1e-3)), "matvecs": int(nmv),
+           "matvec_GBps_vs_batch_time": nbytes / t / 1e9}
+    # batched vs plain on the same first n_serial problems
+    sub_T, sub_R = Ts[:n_serial], Rs[:n_serial]
+    np.random.seed(1)
+    tfx.cpd_batch(sub_T, sub_R, o)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    np.random.seed(1)
+    ob = tfx.cpd_batch(sub_T, sub_R, o)
+    torch.cuda.synchronize()
+    t_b = time.perf_counter() - t0
+    for T_, R_ in zip(sub_T[:4], sub_R[:4]):    # warm-up of the single-problem path
+        tfx.cpd(T_, R_, o)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    np.random.seed(1)
+    os_ = [tfx.cpd(T_, R_, o)[1] for T_, R_ in zip(sub_T, sub_R)]
+    torch.cuda.synchronize()
+    t_s = time.perf_counter() - t0
+    eb = np.array([op.rel_error for _, op in ob])
+    es = np.array([op.rel_error for op in os_])
+    res["batched_vs_plain"] = {"problems": n_serial, "batched_s": t_b, "plain_serial_s": t_s,
+                               "speedup": t_s / t_b, "batched_median_rel_error": float(np.median(eb)),
+                               "plain_median_rel_error": float(np.median(es)),
+                               "plain": "one cpd call per problem on the GPU (FP32 path), as the reference's "
+                                        "rank/stats loop calls cpd"}
+    return res
 
 
 def run_case(case):
@@ -640,6 +816,24 @@ def run_case(case):
         # the c3 CP fit loss, forward + backward, three times
         res = run_autograd(None)
         print(json.dumps({"case": case, "ms": res["ms"]}))
+    elif case.startswith("sparse_cpd"):
+        # the sparse CPD (compress-first path, the reference's semantics) at
+        # c5 scale or a smaller one: "sparse_cpd" = 20000^3 / 1e7 nonzeros,
+        # "sparse_cpd_mid" = 2000^3 / 1e6
+        dims, nnz = ((20000,) * 3, 10_000_000) if case == "sparse_cpd" else ((2000,) * 3, 1_000_000)
+        vals, idx, W = make_coo(dims, nnz, 16, 11)
+        o = tfx.make_options(None)
+        o.precision = "fp32"
+        res = {"case": case}
+        for rep in range(2):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            np.random.seed(0)
+            f, out = tfx.cpd([vals, idx, np.array(dims)], 16, o)
+            torch.cuda.synchronize()
+            res["s_%d" % rep] = time.perf_counter() - t0
+        res.update({"rel_error": float(out.rel_error), "num_steps": int(out.num_steps), "stop": list(out.stop)})
+        print(json.dumps(res), flush=True)
     elif case == "sparse_c5":
         # the c5 COO MTTKRP and residual (20000^3, 1e7 nonzeros, rank 16)
         res = run_sparse(None)

@@ -33,6 +33,11 @@ int tfx_host_gather(const void* const* src, const long long* bytes, const long l
 const char* tfx_last_error(void);
 long long tfx_launch_count(void); /* kernels enqueued by this library so far */
 int tfx_version(void);
+/* The bounded-wait error path of the tensor-core kernels, exercised on its own
+ * (no reference counterpart): one warp waits with `limit` polls (1..2^26) on an
+ * mbarrier that nothing arrives on, so the wait runs out and *status (device
+ * int) receives TFX_STATUS_ERR_TIMEOUT; nothing is left in flight. */
+int tfx_wait_probe(unsigned int limit, int* status, void* stream);
 
 /* ---- damped Gauss-Newton ------------------------------------------------
  * GaussNewton.py:29 dGN(T, factors, R, options) -> (best_factors, step_sizes,
@@ -43,6 +48,27 @@ int tfx_version(void);
 size_t tfx_dgn_workspace_bytes(int dtype, int L, const int* dims, int R);
 int tfx_dgn_solve(int dtype, const tfx_dgn_problem* h_probs, tfx_dgn_problem* d_probs, int nprob,
                   const tfx_dgn_options* options, int cluster, void* stream);
+/* The solver's per-iteration products at one point, without iterating, by the
+ * same device code as tfx_dgn_solve on a cluster of `cluster` CTAs:
+ * grad = GaussNewton.py:401-427 compute_grad (g_l = W_l P1_l - T_(l) KR_l,
+ * flat layout) and jtjv = J^T J v (GaussNewton.py:551-581 matvec, the product
+ * inside every CG iteration), after the Gramians and preconditioner set-up of
+ * GaussNewton.py:520-548, 584-627 with damping `damp`.  h_prob->x holds the
+ * point (flat factors); tensor, work (tfx_dgn_workspace_bytes) and result are
+ * used, result[2] receives the status of the bounded waits.  Either product
+ * may be skipped by passing NULL (v and jtjv together). */
+int tfx_jtj_matvec(int dtype, const tfx_dgn_problem* h_prob, tfx_dgn_problem* d_prob, const tfx_dgn_options* options,
+                   int cluster, double damp, const void* v, void* jtjv, void* grad, void* stream);
+/* The dogleg trials that follow a rejected step (GaussNewton.py:713-795
+ * compute_dogleg_steps / dogleg / update_delta), by the solver's own device
+ * code: from the point x (h_prob->x), the rejected step y, the gradient grad
+ * and J^T J grad as the CG hands them over, and the rejected step's relative
+ * error; options->symm / factors_norm apply as in the solve.  Outputs: the
+ * best point, step and (unbalanced, transformed) factors in the flat layout,
+ * and the best error (device double). */
+int tfx_dgn_dogleg(int dtype, const tfx_dgn_problem* h_prob, tfx_dgn_problem* d_prob, const tfx_dgn_options* options,
+                   int cluster, double damp, double error, const void* y, const void* grad, const void* jtj,
+                   void* best_x, void* best_y, void* best_W, double* best_error, void* stream);
 
 /* ---- alternating least squares ---------------------------------------------
  * Alternating_Least_Squares.py:18 als(T, factors, R, options) -> (factors,
@@ -145,7 +171,9 @@ int tfx_mode_gram_tc(const float* S, long long P, int D, long long Q, float* G, 
  * D*D*element size must not exceed 32 MiB (D <= 2896 in float32, 2048 in
  * float64); larger D is refused with TFX_STATUS_ERR_ARG.  The first call on a
  * device looks the array's address up and should come before any stream
- * capture.  Calls share the array: calls that overlap on the GPU race. */
+ * capture; the address is cached with the device's context, and a call after
+ * that context changed (cudaDeviceReset) looks it up again.  Calls share the
+ * array: calls that overlap on the GPU race. */
 size_t tfx_mode_gram_noalloc_capacity_bytes(void);
 int tfx_mode_gram_noalloc(int dtype, const void* S, long long P, int D, long long Q, void* G, void* stream);
 /* Orthonormal basis of the k columns of Y (D x k column-major), in place
@@ -206,7 +234,9 @@ size_t tfx_sparse_residual_scratch_bytes(void);
 int tfx_sparse_residual(int dtype, const int* idx32, const void* vals, long long nnz, int L, const int* dims, int R,
                         const void* const* Wrow_dev, double* out, void* scratch, void* stream);
 /* Compression.py:211-215 with 240-258 (dot_product_mkl(Tl, Tl.T)): dense
- * T_(l) T_(l)^T from COO; *err = 2 if the fibre hash table overflows. */
+ * T_(l) T_(l)^T from COO; entries of one fibre are matched by comparing their
+ * coordinates, so any dimensions are exact; nnz < 2^31 (TFX_STATUS_ERR_ARG
+ * otherwise); *err = 2 if the fibre hash table overflows. */
 size_t tfx_coo_gram_scratch_bytes(long long nnz, int d);
 int tfx_coo_gram(int dtype, const int* idx32, const void* vals, long long nnz, const void* svals_sorted,
                  const long long* rowptr, int L, const int* dims, int mode, void* G, void* scratch, size_t scratch_bytes,

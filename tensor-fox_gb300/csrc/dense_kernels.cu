@@ -1304,7 +1304,10 @@ extern "C" int tfx_tensor_norms(int dtype, const void* T, long long N, double* o
 // * The first call on each device looks up the array's device address with
 //   cudaGetSymbolAddress while that device is current (the symbol's host-side
 //   name is not a device address).  That first call on a device should come
-//   before any stream capture.
+//   before any stream capture.  The address is cached per device together with
+//   the device's current context; when that context changes (after
+//   cudaDeviceReset, or a new primary context on the ordinal) the next call
+//   looks the address up again instead of reusing the destroyed context's.
 // * Every call shares the one array: calls that overlap on the GPU (other
 //   streams, other host threads) race on it.  The kernels overwrite every
 //   scratch entry they later read, so nothing needs clearing between calls.
@@ -1318,6 +1321,23 @@ static __device__ __align__(256) unsigned char g_noalloc_gram_scratch[TFX_NOALLO
 
 static std::mutex g_noalloc_mu;
 static void* g_noalloc_addr[TFX_NOALLOC_MAX_DEVICES] = {nullptr};
+static void* g_noalloc_ctx[TFX_NOALLOC_MAX_DEVICES] = {nullptr};
+
+// the driver's current context (cuCtxGetCurrent), resolved through the runtime
+// so that only the CUDA runtime is linked
+typedef int (*CtxGetCurrentFn)(void**);
+static CtxGetCurrentFn ctx_get_current_fn() {
+  static CtxGetCurrentFn fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = (CtxGetCurrentFn)p;
+  });
+  return fn;
+}
 
 static int noalloc_scratch_address(void** out) {
   int dev = -1;
@@ -1325,13 +1345,19 @@ static int noalloc_scratch_address(void** out) {
   if (e != cudaSuccess) return tfx_set_cuda_error(e, "mode_gram_noalloc: current device");
   if (dev < 0 || dev >= TFX_NOALLOC_MAX_DEVICES)
     return tfx_set_error(TFX_STATUS_ERR_UNSUPPORTED, "mode_gram_noalloc: device ordinal above 63");
+  CtxGetCurrentFn get = ctx_get_current_fn();
+  if (!get) return tfx_set_error(TFX_STATUS_ERR_CUDA, "mode_gram_noalloc: cuCtxGetCurrent unavailable");
+  void* ctx = nullptr;
+  if (get(&ctx) != 0) ctx = nullptr;  // null before the runtime has bound this device's context
   std::lock_guard<std::mutex> lock(g_noalloc_mu);
-  if (g_noalloc_addr[dev] == nullptr) {
+  if (g_noalloc_addr[dev] == nullptr || ctx == nullptr || g_noalloc_ctx[dev] != ctx) {
     void* p = nullptr;
-    e = cudaGetSymbolAddress(&p, g_noalloc_gram_scratch);
+    e = cudaGetSymbolAddress(&p, g_noalloc_gram_scratch);  // binds the primary context if needed
     if (e != cudaSuccess || p == nullptr)
       return tfx_set_cuda_error(e == cudaSuccess ? cudaErrorInvalidSymbol : e, "mode_gram_noalloc: scratch address");
+    if (get(&ctx) != 0) ctx = nullptr;  // a null context is never matched, so the lookup repeats
     g_noalloc_addr[dev] = p;
+    g_noalloc_ctx[dev] = ctx;
   }
   *out = g_noalloc_addr[dev];
   return TFX_STATUS_OK;

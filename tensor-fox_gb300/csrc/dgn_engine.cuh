@@ -1496,10 +1496,12 @@ struct Engine {
   }
 };
 
+// Binds an engine to one problem: shape tables, workspace and shared-memory
+// pointers, the third-order slab barriers.  Used by the solve and by the
+// standalone gradient / J^T J v entry point.
 template <class T, int TS>
-__device__ void solve_problem(const tfx_dgn_problem& pb, const tfx_dgn_options& op, Team tm, char* smem,
-                              const SmemPlan& sp) {
-  Engine<T, TS> E;
+__device__ __forceinline__ void engine_setup(Engine<T, TS>& E, const tfx_dgn_problem& pb, const tfx_dgn_options& op,
+                                             Team tm, char* smem, const SmemPlan& sp) {
   E.d = (int*)(smem + sp.misc + 64);
   E.off = E.d + TFX_MAX_ORDER;
   E.st = (long long*)(smem + sp.misc + 64 + 4 * TFX_MAX_ORDER * 8);
@@ -1610,6 +1612,13 @@ __device__ void solve_problem(const tfx_dgn_problem& pb, const tfx_dgn_options& 
   E.flip4 = 0;
   E.flip12 = 0;
   E.flipw = 0;
+}
+
+template <class T, int TS>
+__device__ void solve_problem(const tfx_dgn_problem& pb, const tfx_dgn_options& op, Team tm, char* smem,
+                              const SmemPlan& sp) {
+  Engine<T, TS> E;
+  engine_setup<T, TS>(E, pb, op, tm, smem, sp);
 
   // error / improvement history: every CTA keeps its own copy in shared
   // memory so that the stop tests never depend on another SM's writes
@@ -1821,6 +1830,99 @@ __global__ void __launch_bounds__(TFX_THREADS, TFX_DENSE_CTAS)
   solve_problem<T, TS>(pb, op, tm, smem, sp);
 }
 
+// Arguments of the standalone evaluations (tfx_jtj_matvec, tfx_dgn_dogleg).
+struct UnitsArgs {
+  int mode;            // 0: gradient and/or J^T J v; 1: dogleg trials
+  double damp;
+  double error;        // dogleg: the rejected step's relative error
+  const void* v;       // J^T J v input (flat), or null
+  void* jtjv;          // J^T J v output, or null
+  void* grad;          // gradient output (mode 0, or null) / dogleg gradient input (mode 1)
+  const void* y;       // dogleg: the rejected step
+  const void* jtj;     // dogleg: J^T J grad
+  void* best_x;        // dogleg outputs: best point, step, factors and error
+  void* best_y;
+  void* best_W;
+  double* best_error;
+};
+
+// One evaluation of the solver's own device code at a given point, without
+// iterating.  Mode 0: the MTTKRP gradient g (GaussNewton.py:401-427
+// compute_grad, the reference's sign) and J^T J v for a caller's vector v
+// through the CG's product (GaussNewton.py:551-581), after the same Gramians
+// and preconditioner set-up (GaussNewton.py:520-548, 584-627) as every dGN
+// iteration; either output may be skipped (null).  Mode 1: the dogleg trials
+// that follow a rejected step (GaussNewton.py:713-795) from the point x, the
+// step y, the gradient and J^T J grad.
+template <class T, int TS>
+__global__ void __launch_bounds__(TFX_THREADS, 1)
+    dgn_units_kernel(const tfx_dgn_problem* __restrict__ probs, tfx_dgn_options op, int cluster, SmemPlan sp,
+                     UnitsArgs ua) {
+  extern __shared__ __align__(16) char smem[];
+  Team tm = make_team(cluster);
+  tfx_dgn_problem pb = probs[0];
+  Engine<T, TS> E;
+  engine_setup<T, TS>(E, pb, op, tm, smem, sp);
+  E.cprof = nullptr;
+  E.gprof = nullptr;
+  const T* x0 = (const T*)pb.x;
+  E.damp = ua.damp;
+  if (ua.mode == 0) {
+    E.for_own([&](int e, int l, int c) { E.W[e] = x0[e]; });
+    E.tm.sync();
+    E.stage_W();
+    E.gramians_and_precond();
+    if (ua.grad) {
+      T* gout = (T*)ua.grad;
+      if (E.sG3 && E.stage)
+        E.template gradient_l3<true>();
+      else if (E.sG3)
+        E.template gradient_l3<false>();
+      else
+        E.gradient();
+      // the engine keeps M_l - W_l P1_l; the reference's g is its negative
+      E.for_own([&](int e, int l, int c) { gout[e] = -E.grad[e]; });
+    }
+    E.tm.sync();
+    if (ua.v && ua.jtjv) {
+      if (E.stage)
+        cg_matvec<T, true>(E.L, E.R, E.nx, E.ncol, E.c0, E.cgo, (const T*)ua.v, (T*)ua.jtjv, E.W, E.P1, E.P2);
+      else
+        cg_matvec<T, false>(E.L, E.R, E.nx, E.ncol, E.c0, E.cgo, (const T*)ua.v, (T*)ua.jtjv, E.W, E.P1, E.P2);
+    }
+  } else {
+    double meanabs;
+    E.tensor_norms(E.Tsize, meanabs);
+    const T* yin = (const T*)ua.y;
+    const T* gin = (const T*)ua.grad;
+    const T* jin = (const T*)ua.jtj;
+    // the state after a rejected step: xn = x + y, W = the rejected factors
+    // (zero here: only read back when no trial improves)
+    E.for_own([&](int e, int l, int c) {
+      E.xn[e] = x0[e] + yin[e];
+      E.y[e] = yin[e];
+      E.grad[e] = gin[e];
+      E.jtj[e] = jin[e];
+      E.W[e] = T(0);
+    });
+    E.tm.sync();
+    E.stage_W();
+    const double err = E.dogleg(ua.error);
+    T* bx = (T*)ua.best_x;
+    T* by = (T*)ua.best_y;
+    T* bw = (T*)ua.best_W;
+    E.for_own([&](int e, int l, int c) {
+      bx[e] = E.xn[e];
+      by[e] = E.y[e];
+      bw[e] = E.W[e];
+    });
+    if (E.tm.rank == 0 && threadIdx.x == 0) *ua.best_error = err;
+  }
+  if (E.tm.rank == 0 && threadIdx.x == 0) pb.result[2] = TFX_OK;
+  E.tm.sync();
+  if (threadIdx.x == 0 && E.g3err) atomicMax(&pb.result[2], 3);
+}
+
 }  // namespace tfx
 
 
@@ -1877,8 +1979,46 @@ static int launch_dgn(const tfx_dgn_problem* d_probs, int nprob, const tfx_dgn_o
   return TFX_STATUS_OK;
 }
 
+template <class T, int TS>
+static int launch_units(const tfx_dgn_problem* d_prob, const tfx_dgn_options* op, int cluster, const SmemPlan& sp,
+                        const UnitsArgs& ua, cudaStream_t st) {
+  auto kfn = dgn_units_kernel<T, TS>;
+  cudaError_t e = cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sp.total);
+  if (e != cudaSuccess) return tfx_set_cuda_error(e, "dgn units smem attribute");
+  if (cluster > 8) {
+    e = cudaFuncSetAttribute(kfn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    if (e != cudaSuccess) return tfx_set_cuda_error(e, "dgn units cluster attribute");
+  }
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)cluster);
+  cfg.blockDim = dim3(TFX_THREADS);
+  cfg.dynamicSmemBytes = sp.total;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = (unsigned)cluster;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  if (cluster > 1) {
+    int ncl = 0;
+    e = cudaOccupancyMaxActiveClusters(&ncl, kfn, &cfg);
+    if (e != cudaSuccess) return tfx_set_cuda_error(e, "dgn units cluster occupancy");
+    if (ncl < 1) return tfx_set_error(TFX_STATUS_ERR_UNSUPPORTED, "cluster size cannot be scheduled");
+  }
+  e = cudaLaunchKernelEx(&cfg, kfn, d_prob, *op, cluster, sp, ua);
+  if (e != cudaSuccess) return tfx_set_cuda_error(e, "dgn units launch");
+  tfx_count_launch(1);
+  return TFX_STATUS_OK;
+}
+
 int launch_dgn_f32(int TS, const tfx_dgn_problem* d_probs, int nprob, const tfx_dgn_options* op, int cluster,
                    const SmemPlan& sp, cudaStream_t st);
+int launch_units_f32(int TS, const tfx_dgn_problem* d_prob, const tfx_dgn_options* op, int cluster, const SmemPlan& sp,
+                     const UnitsArgs& ua, cudaStream_t st);
+int launch_units_f64(int TS, const tfx_dgn_problem* d_prob, const tfx_dgn_options* op, int cluster, const SmemPlan& sp,
+                     const UnitsArgs& ua, cudaStream_t st);
 int launch_dgn_f64(int TS, const tfx_dgn_problem* d_probs, int nprob, const tfx_dgn_options* op, int cluster,
                    const SmemPlan& sp, cudaStream_t st);
 

@@ -8,4 +8,10 @@ int launch_dgn_f64(int TS, const tfx_dgn_problem* d_probs, int nprob, const tfx_
   if (TS == 2) return launch_dgn<double, 2>(d_probs, nprob, op, cluster, sp, st);
   return launch_dgn<double, 4>(d_probs, nprob, op, cluster, sp, st);
 }
+int launch_units_f64(int TS, const tfx_dgn_problem* d_prob, const tfx_dgn_options* op, int cluster, const SmemPlan& sp,
+                     const UnitsArgs& ua, cudaStream_t st) {
+  if (TS == 1) return launch_units<double, 1>(d_prob, op, cluster, sp, ua, st);
+  if (TS == 2) return launch_units<double, 2>(d_prob, op, cluster, sp, ua, st);
+  return launch_units<double, 4>(d_prob, op, cluster, sp, ua, st);
+}
 }  // namespace tfx

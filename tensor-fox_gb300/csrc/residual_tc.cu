@@ -61,18 +61,7 @@ __device__ __forceinline__ void mma(uint32_t tmem, uint64_t a, uint64_t b, uint3
 }
 
 __device__ __forceinline__ bool wait_bar(uint64_t* bar, uint32_t parity) {
-  const uint32_t a = su32(bar);
-  for (uint32_t it = 0; it < SPIN; ++it) {
-    uint32_t done;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-        "selp.u32 %0, 1, 0, p;\n\t}"
-        : "=r"(done)
-        : "r"(a), "r"(parity)
-        : "memory");
-    if (done) return true;
-  }
-  return false;
+  return mbar_wait_bounded(su32(bar), parity, SPIN);
 }
 
 __device__ __forceinline__ float tf32_hi(float x) {

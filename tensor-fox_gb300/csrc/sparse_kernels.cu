@@ -283,20 +283,13 @@ __global__ void __launch_bounds__(256) k_sparse_residual(const int* __restrict__
 
 // ---------------------------------------------------------------------------
 // COO Gram.  Diagonal: sum of v^2 per row of the row-sorted copy.  Entries of
-// one fibre (same indices in every mode but l) are grouped by hashing the
-// fibre key with bounded linear probing; each pair of distinct rows in a fibre
-// adds v*v' to G[i,i'] and G[i',i].
+// one fibre (same indices in every mode but l) are grouped in a hash table with
+// bounded linear probing.  A slot holds the id of the first entry that claimed
+// it (the fibre's representative); an entry joins a slot only when its
+// coordinates equal the representative's in every mode but l, so two fibres
+// never merge, whatever the dimensions (no mixed-radix key that could wrap).
+// Each pair of distinct rows in a fibre adds v*v' to G[i,i'] and G[i',i].
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ unsigned long long fibre_key(const int* __restrict__ idx32, long long nnz, long long k,
-                                                        const CooShape& sh, int mode) {
-  unsigned long long key = 0;
-  for (int m = 0; m < sh.L; ++m) {
-    if (m == mode) continue;
-    key = key * (unsigned long long)sh.dims[m] + (unsigned long long)idx32[(size_t)m * nnz + k];
-  }
-  return key;
-}
-
 __device__ __forceinline__ unsigned long long mix64(unsigned long long x) {
   x ^= x >> 33;
   x *= 0xff51afd7ed558ccdULL;
@@ -306,20 +299,40 @@ __device__ __forceinline__ unsigned long long mix64(unsigned long long x) {
   return x;
 }
 
-#define TFX_EMPTY_KEY 0xffffffffffffffffULL
+// hash of the coordinates of entry k in every mode but `mode` (a hash only:
+// equal hashes are resolved by comparing coordinates)
+__device__ __forceinline__ unsigned long long fibre_hash(const int* __restrict__ idx32, long long nnz, long long k,
+                                                         int L, int mode) {
+  unsigned long long h = 0x9e3779b97f4a7c15ULL;
+  for (int m = 0; m < L; ++m) {
+    if (m == mode) continue;
+    h = mix64(h ^ (unsigned long long)(unsigned int)idx32[(size_t)m * nnz + k]);
+  }
+  return h;
+}
+
+__device__ __forceinline__ bool same_fibre(const int* __restrict__ idx32, long long nnz, long long a, long long b,
+                                           int L, int mode) {
+  for (int m = 0; m < L; ++m) {
+    if (m == mode) continue;
+    if (idx32[(size_t)m * nnz + a] != idx32[(size_t)m * nnz + b]) return false;
+  }
+  return true;
+}
+
+#define TFX_EMPTY_SLOT 0xffffffffffffffffULL
 #define TFX_MAX_PROBES 4096
 
-// insert every entry's fibre key; slot_of[k] = slot, heads form per-slot lists
-__global__ void k_fibre_insert(const int* __restrict__ idx32, long long nnz, CooShape sh, int mode,
-                               unsigned long long* __restrict__ keys, long long nslots, int* __restrict__ head,
+// insert every entry into its fibre's slot; heads form per-slot lists
+__global__ void k_fibre_insert(const int* __restrict__ idx32, long long nnz, int L, int mode,
+                               unsigned long long* __restrict__ rep, long long nslots, int* __restrict__ head,
                                int* __restrict__ next, int* __restrict__ err) {
   for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < nnz; k += (long long)gridDim.x * blockDim.x) {
-    const unsigned long long key = fibre_key(idx32, nnz, k, sh, mode);
-    long long s = (long long)(mix64(key) % (unsigned long long)nslots);
+    long long s = (long long)(fibre_hash(idx32, nnz, k, L, mode) % (unsigned long long)nslots);
     int probes = 0;
     while (true) {
-      const unsigned long long prev = atomicCAS(keys + s, TFX_EMPTY_KEY, key);
-      if (prev == TFX_EMPTY_KEY || prev == key) break;
+      const unsigned long long prev = atomicCAS(rep + s, TFX_EMPTY_SLOT, (unsigned long long)k);
+      if (prev == TFX_EMPTY_SLOT || same_fibre(idx32, nnz, (long long)prev, k, L, mode)) break;
       if (++probes >= TFX_MAX_PROBES) {
         atomicExch(err, 2);
         s = -1;
@@ -600,11 +613,14 @@ extern "C" int tfx_coo_gram(int dtype, const int* idx32, const void* vals, long 
   if (fill_shape(sh, L, dims, 1) || mode < 0 || mode >= L || !idx32 || !vals || !svals_sorted || !rowptr || !G ||
       !scratch || !err)
     return tfx_set_error(TFX_STATUS_ERR_ARG, "coo_gram args");
+  // the per-entry fibre lists hold 32-bit entry ids
+  if (nnz < 0 || nnz >= (1LL << 31))
+    return tfx_set_error(TFX_STATUS_ERR_ARG, "coo_gram: the number of stored entries must be below 2^31");
   const int d = dims[mode];
   const long long nslots = 2 * std::max<long long>(nnz, 1) + 1;
   if (scratch_bytes < tfx_coo_gram_scratch_bytes(nnz, d)) return tfx_set_error(TFX_STATUS_ERR_ARG, "coo_gram scratch");
   char* p = (char*)scratch;
-  unsigned long long* keys = (unsigned long long*)p;
+  unsigned long long* rep = (unsigned long long*)p;
   p += (size_t)nslots * 8;
   int* head = (int*)p;
   p += (size_t)nslots * 4;
@@ -613,12 +629,12 @@ extern "C" int tfx_coo_gram(int dtype, const int* idx32, const void* vals, long 
   p = (char*)(((uintptr_t)p + 15) & ~(uintptr_t)15);
   double* Gd = (double*)p;
   cudaStream_t st = (cudaStream_t)stream;
-  cudaError_t e = cudaMemsetAsync(keys, 0xff, (size_t)nslots * 8, st);
+  cudaError_t e = cudaMemsetAsync(rep, 0xff, (size_t)nslots * 8, st);
   if (e == cudaSuccess) e = cudaMemsetAsync(head, 0xff, (size_t)nslots * 4, st);
   if (e == cudaSuccess) e = cudaMemsetAsync(Gd, 0, (size_t)d * d * 8, st);
   if (e != cudaSuccess) return tfx_set_cuda_error(e, "coo_gram memset");
   if (nnz > 0) {
-    k_fibre_insert<<<grid_for(nnz), 256, 0, st>>>(idx32, nnz, sh, mode, keys, nslots, head, next, err);
+    k_fibre_insert<<<grid_for(nnz), 256, 0, st>>>(idx32, nnz, L, mode, rep, nslots, head, next, err);
     if (int s = launched("fibre_insert")) return s;
     if (dtype == TFX_F32)
       k_fibre_pairs<float><<<grid_for(nslots), 256, 0, st>>>(idx32, (const float*)vals, nnz, mode, nslots, head, next,

@@ -43,19 +43,7 @@ __device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
 
 // bounded wait for phase `parity`; returns false on timeout
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
-  const uint32_t a = smem_u32(bar);
-  for (uint32_t it = 0; it < TCG_SPIN_LIMIT; ++it) {
-    uint32_t done;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-        "selp.u32 %0, 1, 0, p;\n\t}"
-        : "=r"(done)
-        : "r"(a), "r"(parity)
-        : "memory");
-    if (done) return true;
-  }
-  return false;
+  return mbar_wait_bounded(smem_u32(bar), parity, TCG_SPIN_LIMIT);
 }
 
 __device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, uint64_t* bar, int x, int y, int z) {
@@ -444,6 +432,21 @@ __global__ void k_gram_tc_reduce(const float* __restrict__ part, int D, int ks_d
   }
 }
 
+// The bounded-wait error path on its own: one warp waits, with `limit` polls,
+// on phase 0 of a freshly initialised mbarrier that nothing arrives on (no
+// copy or MMA is in flight), so the wait always runs out; the kernel then
+// records TFX_STATUS_ERR_TIMEOUT and returns like the tensor-core kernels do.
+__global__ void k_wait_probe(uint32_t limit, int* status) {
+  __shared__ __align__(8) uint64_t bar;
+  if (threadIdx.x == 0) {
+    mbar_init(&bar, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  const bool landed = mbar_wait_bounded(smem_u32(&bar), 0, limit);
+  if (threadIdx.x == 0) *status = landed ? TFX_STATUS_OK : TFX_STATUS_ERR_TIMEOUT;
+}
+
 }  // namespace tfx
 
 using namespace tfx;
@@ -562,6 +565,15 @@ extern "C" int tfx_mode_gram_tc(const float* S, long long P, int D, long long Q,
   k_gram_tc_reduce<<<rb, 256, 0, st>>>((const float*)scratch, D, kk.ks_d, kk.ks_o, tc_use2(D) ? 1 : 0, G);
   e = cudaGetLastError();
   if (e != cudaSuccess) return tfx_set_cuda_error(e, "mode_gram_tc reduce");
+  tfx_count_launch(1);
+  return TFX_STATUS_OK;
+}
+
+extern "C" int tfx_wait_probe(unsigned int limit, int* status, void* stream) {
+  if (!status || limit == 0 || limit > (1u << 26)) return tfx_set_error(TFX_STATUS_ERR_ARG, "wait_probe args");
+  k_wait_probe<<<1, 32, 0, (cudaStream_t)stream>>>(limit, status);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return tfx_set_cuda_error(e, "wait_probe launch");
   tfx_count_launch(1);
   return TFX_STATUS_OK;
 }

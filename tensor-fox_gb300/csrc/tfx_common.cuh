@@ -448,6 +448,25 @@ __device__ __forceinline__ void tile_zero(T (&acc)[TM][TN]) {
 }
 
 // Status codes shared with the C ABI.
+// Bounded wait on phase `parity` of a shared-memory mbarrier (its 32-bit
+// shared address): at most `limit` polls with mbarrier.try_wait.parity.
+// Returns false when the wait ran out; the caller then records an error status
+// instead of spinning on (the tensor-core kernels' copy and MMA waits use it).
+__device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar_addr, uint32_t parity, uint32_t limit) {
+  for (uint32_t it = 0; it < limit; ++it) {
+    uint32_t done;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(done)
+        : "r"(bar_addr), "r"(parity)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+
 #define TFX_OK 0
 #define TFX_ERR_ARG 1
 #define TFX_ERR_NUMERIC 2

@@ -73,6 +73,13 @@ def _declare(lib):
     lib.tfx_dgn_solve.restype = c_int
     lib.tfx_dgn_solve.argtypes = [c_int, POINTER(DgnProblem), c_void_p, c_int, POINTER(DgnOptions), c_int,
                                   c_void_p]
+    lib.tfx_jtj_matvec.restype = c_int
+    lib.tfx_jtj_matvec.argtypes = [c_int, POINTER(DgnProblem), c_void_p, POINTER(DgnOptions), c_int, c_double,
+                                   c_void_p, c_void_p, c_void_p, c_void_p]
+    lib.tfx_dgn_dogleg.restype = c_int
+    lib.tfx_dgn_dogleg.argtypes = [c_int, POINTER(DgnProblem), c_void_p, POINTER(DgnOptions), c_int, c_double,
+                                   c_double, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
+                                   c_void_p]
     for name, args in _EXTRA_SIGNATURES.items():
         fn = getattr(lib, name)
         fn.restype = c_int
@@ -96,6 +103,7 @@ _D = c_double
 _SZ = c_size_t
 _EXTRA_SIGNATURES = {
     "tfx_mode_gram": [_I, _P, _LL, _I, _LL, _P, _P, _SZ, _P],
+    "tfx_wait_probe": [ctypes.c_uint, _P, _P],
     "tfx_gemm": [_I, _P, _P, _P, _LL, _LL, _LL, _LL, POINTER(c_longlong), _D, _D, _P],
     "tfx_orthonormalize": [_I, _P, _I, _I, _P],
     "tfx_ttm": [_I, _P, _LL, _I, _LL, _P, _I, _P, _P],

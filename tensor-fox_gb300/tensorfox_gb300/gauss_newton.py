@@ -175,6 +175,90 @@ def dGN_device(Td, x0d, R, options, precision, cluster=None, aliased=False, fix_
     return b
 
 
+class _Single:
+    """One problem's descriptor and workspace for the standalone evaluations."""
+
+    def __init__(self, T, x_flat, R, precision):
+        self.precision = precision
+        self.dt = _dev.torch_dtype(precision)
+        self.Td = _dev.to_device(T, self.dt)
+        self.dims = tuple(int(d) for d in self.Td.shape)
+        dev = self.Td.device
+        self.x = (x_flat if isinstance(x_flat, torch.Tensor) else torch.from_numpy(np.asarray(x_flat)))
+        self.x = self.x.to(dev, self.dt).contiguous()
+        lib = _lib.load()
+        L = len(self.dims)
+        dims_c = (ctypes.c_int * L)(*self.dims)
+        self.ws = torch.empty(int(lib.tfx_dgn_workspace_bytes(_dev.lib_dtype(precision), L, dims_c, int(R))),
+                              dtype=torch.uint8, device=dev)
+        self.result = torch.zeros(4, dtype=torch.int32, device=dev)
+        d = _lib.DgnProblem()
+        d.L, d.R = L, int(R)
+        for l, v in enumerate(self.dims):
+            d.dims[l] = v
+        d.tensor, d.x, d.work, d.result = _dev.ptr(self.Td), _dev.ptr(self.x), _dev.ptr(self.ws), _dev.ptr(self.result)
+        self.desc = d
+        self.d_desc = torch.empty(ctypes.sizeof(_lib.DgnProblem), dtype=torch.uint8, device=dev)
+        o = _lib.DgnOptions()
+        o.maxiter = 1
+        self.opts = o
+
+    def vec(self, v):
+        t = v if isinstance(v, torch.Tensor) else torch.from_numpy(np.ascontiguousarray(v))
+        return t.to(self.Td.device, self.dt).contiguous()
+
+    def check(self):
+        _lib.check_solve_status(self.result.cpu().numpy())
+
+
+def _vp(t):
+    return ctypes.c_void_p(_dev.ptr(t) if t is not None else None)
+
+
+def jtj_matvec(T, factors, R, v=None, damp=1.0, cluster=None, precision=None, gradient=True):
+    """The solver's per-iteration products at one point, computed by the same
+    device code as the solve (``tfx_jtj_matvec``): the gradient ``g`` of
+    GaussNewton.py:401-427 (``compute_grad``) and ``J^T J v`` of
+    GaussNewton.py:551-581 (``matvec``), both in the flat layout.
+
+    ``T`` and ``v`` may be NumPy arrays or torch tensors; the results are
+    device tensors of the working precision (``None`` for a skipped product)."""
+    _dev.require_cuda()
+    if precision is None:
+        precision = 'fp64' if (getattr(T, 'dtype', None) in (np.float64, torch.float64)) else 'fp32'
+    s = _Single(T, _dev.flat_factors(list(factors)), R, precision)
+    vd = s.vec(v) if v is not None else None
+    jv = torch.empty_like(s.x) if v is not None else None
+    g = torch.empty_like(s.x) if gradient else None
+    c = cluster if cluster is not None else auto_cluster(s.dims, R)
+    _lib.call("tfx_jtj_matvec", _dev.lib_dtype(precision), ctypes.byref(s.desc), _vp(s.d_desc),
+              ctypes.byref(s.opts), int(c), float(damp), _vp(vd), _vp(jv), _vp(g), ctypes.c_void_p(_dev.stream()))
+    s.check()
+    return g, jv
+
+
+def dogleg_steps(T, x, y, grad, jtj, error, damp, R, cluster=None, precision=None, symm=False, factors_norm=0):
+    """The dogleg trials after a rejected step (GaussNewton.py:713-795
+    ``compute_dogleg_steps``) on the device, by the solver's own code.  Returns
+    ``(best_factors_flat, best_x, best_y, best_error)`` as device tensors and a
+    float."""
+    _dev.require_cuda()
+    if precision is None:
+        precision = 'fp64' if (getattr(T, 'dtype', None) in (np.float64, torch.float64)) else 'fp32'
+    s = _Single(T, x, R, precision)
+    s.opts.symm = 1 if symm else 0
+    s.opts.factors_norm = float(factors_norm)
+    yd, gd, jd = s.vec(y), s.vec(grad), s.vec(jtj)
+    bx, by, bw = torch.empty_like(s.x), torch.empty_like(s.x), torch.empty_like(s.x)
+    be = torch.empty(1, dtype=torch.float64, device=s.x.device)
+    c = cluster if cluster is not None else auto_cluster(s.dims, R)
+    _lib.call("tfx_dgn_dogleg", _dev.lib_dtype(precision), ctypes.byref(s.desc), _vp(s.d_desc), ctypes.byref(s.opts),
+              int(c), float(damp), float(error), _vp(yd), _vp(gd), _vp(jd), _vp(bx), _vp(by), _vp(bw), _vp(be),
+              ctypes.c_void_p(_dev.stream()))
+    s.check()
+    return bw, bx, by, float(be.item())
+
+
 def dGN(T, factors, R, options=None, precision=None):
     """Damped Gauss-Newton (GaussNewton.py:29-251) on the device.
 

@@ -73,6 +73,8 @@ class DeviceCOO:
 
     def gram(self, mode):
         """Dense T_(l) T_(l)^T (d_l x d_l) on the device."""
+        if self.nnz >= 2 ** 31:
+            raise ValueError("the sparse Gram takes fewer than 2^31 stored entries")
         rowptr, sidx, svals = self.sort_mode(mode)
         d = self.dims[mode]
         lib = _lib.load()
@@ -164,10 +166,17 @@ def tricpd_sparse(T, R, options):
     if o.method not in ('dGN', 'als'):
         raise NotImplementedError("method %r is outside the damped Gauss-Newton and ALS paths" % (o.method,))
     data, idxs, dims = T
+    in_f32 = np.asarray(data).dtype == np.float32
     data = np.asarray(data, dtype=np.float64)
     idxs = np.asarray(idxs, dtype=np.int64).reshape(len(data), -1)
     dims = np.asarray(dims)
-    prec = o.precision if o.precision in ('fp64', 'fp32') else 'fp64'
+    # the input's own precision unless the options name one ('mixed' computes in FP32)
+    if o.precision in ('fp64', 'fp32'):
+        prec = o.precision
+    elif o.precision == 'mixed' or in_f32:
+        prec = 'fp32'
+    else:
+        prec = 'fp64'
     dt = _dev.torch_dtype(prec)
     ordering = np.argsort(-dims)
     sdims = dims[ordering]

@@ -1,9 +1,10 @@
 """Generates the golden fixtures in this folder by running the reference itself.
 
 Run from the repository root, in a container where the reference source tree is
-mounted (see ``ref_harness.py``):
+mounted, with TFX_REFERENCE_MODULES naming its ``modules`` directory (see
+``ref_harness.py``):
 
-    python tests/golden/make_golden.py [case ...]
+    TFX_REFERENCE_MODULES=<reference>/modules python tests/golden/make_golden.py [case ...]
 
 With case names, only those fixtures are regenerated (see ``CASES``).
 Each ``.npz`` holds seeded inputs and the reference's outputs for one case.  The

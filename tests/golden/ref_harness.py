@@ -22,7 +22,13 @@ import os
 import sys
 import types
 
-REF_MODULES = os.environ.get("TFX_REFERENCE_MODULES", "/root/reference/modules")
+def _ref_modules():
+    """The reference's ``modules`` directory, named by TFX_REFERENCE_MODULES."""
+    path = os.environ.get("TFX_REFERENCE_MODULES")
+    if not path or not os.path.isdir(os.path.join(path, "TensorFox")):
+        raise RuntimeError("set TFX_REFERENCE_MODULES to the reference source tree's 'modules' directory "
+                           "(the one holding the TensorFox package) to regenerate the fixtures")
+    return path
 
 
 def _stub_modules():
@@ -59,11 +65,10 @@ def load_reference():
     global _TFX
     if _TFX is not None:
         return _TFX
-    if not os.path.isdir(REF_MODULES):
-        raise RuntimeError("reference source tree not found at " + REF_MODULES)
+    ref_modules = _ref_modules()
     _stub_modules()
-    if REF_MODULES not in sys.path:
-        sys.path.insert(0, REF_MODULES)
+    if ref_modules not in sys.path:
+        sys.path.insert(0, ref_modules)
     import io
     import contextlib
     with contextlib.redirect_stderr(io.StringIO()):

@@ -84,3 +84,37 @@ def test_engine_tile_and_order_do_not_change_results():
             for a, b in zip(errs, ref):
                 assert len(a) == len(b)
                 np.testing.assert_allclose(a, b, rtol=1e-10, atol=1e-15)
+
+
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+def test_every_batch_problem_equals_its_solve_alone(dtype):
+    """Each problem of one batched launch gives exactly what the same problem
+    gives when solved alone from the same start: the batch draws the starts
+    of all problems from NumPy's RNG in problem order, so replaying the draws
+    of the problems before it reproduces problem p's start; 'cg_static' fixes
+    the CG caps.  No problem's result depends on its neighbours."""
+    Ts, _, Rs = problems(24, 6, dtype=dtype)
+
+    class O:
+        inner_method = 'cg_static'
+        cg_maxiter = 10
+        maxiter = 80
+    o = tfx.make_options(O)
+    np.random.seed(21)
+    s0 = np.random.get_state()
+    outb = tfx.cpd_batch(Ts, Rs, o)
+    off = 0
+    for p in range(len(Ts)):
+        np.random.set_state(s0)
+        if off:
+            np.random.randn(off)         # the draws of the problems before p
+        f1, o1 = tfx.cpd_batch([Ts[p]], [Rs[p]], o)[0]
+        fb, ob = outb[p]
+        assert o1.core_dims == ob.core_dims
+        assert o1.num_steps == ob.num_steps
+        tol = 1e-10 if dtype == np.float64 else 1e-6
+        np.testing.assert_allclose(o1.errors[0], ob.errors[0], rtol=tol, atol=1e-15)
+        assert abs(o1.rel_error - ob.rel_error) <= tol * ob.rel_error + 1e-15
+        for a, b in zip(f1, fb):
+            np.testing.assert_allclose(a, b, rtol=100 * tol, atol=100 * tol * np.abs(b).max())
+        off += Rs[p] * sum(ob.core_dims)

@@ -86,6 +86,37 @@ def test_coo_gram_with_shared_fibres():
         np.testing.assert_allclose(X.gram(l).cpu().numpy(), U @ U.T, rtol=1e-12, atol=1e-12)
 
 
+def fibre_gram(data, idxs, d, mode):
+    """T_(mode) T_(mode)^T from the entries, grouped by their exact fibre tuple."""
+    others = np.delete(np.asarray(idxs), mode, axis=1)
+    _, fib = np.unique(others, axis=0, return_inverse=True)
+    V = np.zeros((fib.max() + 1, d))
+    np.add.at(V, (fib.ravel(), np.asarray(idxs)[:, mode]), data)
+    return V.T @ V
+
+
+def test_coo_gram_wide_dims_no_key_wrap():
+    """Order 4 with three modes of 1e7: the product of the other modes' dims
+    (1e21) exceeds 2^64.  Fibre B below sits exactly 2^64 past fibre A in the
+    mixed-radix order (i1 * 1e14 + i2 * 1e7 + i3), so a key formed that way in
+    64 bits would merge them and add false off-diagonal terms."""
+    dims = (6, 10 ** 7, 10 ** 7, 10 ** 7)
+    A = (1, 2, 3)
+    B = (1 + 184467, 2 + 4407370, 3 + 9551616)
+    assert (B[0] - A[0]) * 10 ** 14 + (B[1] - A[1]) * 10 ** 7 + (B[2] - A[2]) == 2 ** 64
+    rng = np.random.default_rng(8)
+    rows = [[0] + list(A), [1] + list(A), [2] + list(B), [3] + list(B), [4] + list(A)]
+    for _ in range(300):   # more fibres, some shared by several rows
+        f = rng.integers(0, 10 ** 7, size=3) if rng.random() < 0.5 else np.array([7, 7, rng.integers(0, 4)])
+        rows.append([int(rng.integers(0, 6))] + [int(v) for v in f])
+    idxs = np.array(rows, dtype=np.int64)
+    data = rng.standard_normal(len(idxs))
+    want = fibre_gram(data, idxs, 6, 0)
+    assert want[0, 2] == 0.0 and want[1, 3] == 0.0      # A and B never meet
+    X = sparse.DeviceCOO(data, idxs, dims, torch.float64)
+    np.testing.assert_allclose(X.gram(0).cpu().numpy(), want, rtol=1e-12, atol=1e-12)
+
+
 def test_coo_encode_rejects_out_of_range():
     with pytest.raises(ValueError):
         sparse.DeviceCOO(np.ones(2), np.array([[0, 0, 0], [0, 5, 0]]), (3, 3, 3), torch.float64)

@@ -1,4 +1,5 @@
-"""The allocation-free mode Gram (tfx_mode_gram_noalloc) agrees with tfx_mode_gram.
+"""The allocation-free mode Gram (tfx_mode_gram_noalloc) agrees with tfx_mode_gram
+and with the FP64 NumPy product of the unfolding with its transpose.
 
 It exists for callers that cannot allocate device memory at call time (a host
 whose memory pool owns the device, a latency-critical path, a no-allocation
@@ -37,6 +38,9 @@ def test_noalloc_matches_allocating_entry_point(dtype, shape, l):
     D = int(shape[l])
     Q = int(np.prod(shape[l + 1:]))
     ref = kernels.mode_gram(T, list(shape), l).double().cpu().numpy()
+    # the same Gram in FP64 NumPy: the (P, D, Q) view's mode unfolding times its transpose
+    U = np.moveaxis(T.double().cpu().numpy().reshape(P, D, Q), 1, 0).reshape(D, P * Q)
+    exact = U @ U.T
     code = L.F64 if dtype == torch.float64 else L.F32
     stream = ctypes.c_void_p(int(torch.cuda.current_stream().cuda_stream))
     tol = 1e-12 if dtype == torch.float64 else 2e-5
@@ -46,7 +50,9 @@ def test_noalloc_matches_allocating_entry_point(dtype, shape, l):
                                            ctypes.c_void_p(G.data_ptr()), stream)
         assert status == 0, lib.tfx_last_error()
         torch.cuda.synchronize()
-        np.testing.assert_allclose(G.double().cpu().numpy(), ref, rtol=tol, atol=tol * np.abs(ref).max())
+        got = G.double().cpu().numpy()
+        np.testing.assert_allclose(got, ref, rtol=tol, atol=tol * np.abs(ref).max())
+        np.testing.assert_allclose(got, exact, rtol=tol, atol=tol * np.abs(exact).max())
 
 
 def test_noalloc_rejects_a_gram_larger_than_its_scratch():
