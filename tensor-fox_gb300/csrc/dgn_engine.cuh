@@ -75,7 +75,11 @@ __host__ __device__ inline size_t g3_stage(int d1, int d2) { return ((size_t)d1 
 __host__ __device__ inline size_t g3_floats(int d0, int d1, int d2) {
   const size_t d2p = ((size_t)d2 + 3) & ~(size_t)3;
   return 3 * g3_stage(d1, d2) + 2 * (d0 + d1 + d2p) * 4 + 2 * (TFX_THREADS / 32) * 4 +
-         (TFX_THREADS / 32) * d2p * 4;
+         (TFX_THREADS / 32) * d2p * 4 + 2 * (TFX_THREADS / 32) * 64;
+}
+// offset (elements) of the slab-split gradient's M0 warp partials inside it
+__host__ __device__ inline size_t g3_p0x(int d0, int d1, int d2) {
+  return g3_floats(d0, d1, d2) - 2 * (TFX_THREADS / 32) * 64;
 }
 
 struct SmemPlan {
@@ -984,6 +988,242 @@ struct Engine {
   }
 
   // -------------------------------------------------------------------------
+  // Third-order gradient with the SLABS split across the team (every mode <=
+  // 64, R <= 64, and the partials below fit in the three slab stages).  CTA q
+  // streams its own slabs T[i, :, :], i in [d0 q / n, d0 (q + 1) / n), and forms
+  // for every column at once (64 x 64 register tiles, 4 x 4 outputs a thread):
+  //   Y = T[i] W2                      M0[i, :] = sum_j Y[j, :] o W1[j, :]
+  //   M1 += Y o (1 W0[i, :])           M2 += (T[i]^T W1) o (1 W0[i, :])
+  // (the MTTKRP dimension tree, two small products per slab).  M0's rows go to
+  // a global scratch vector, the M1 and M2 partials to the CTA's (then idle)
+  // slab stages; after a team barrier the CTA owning column c sums the peers'
+  // partials of that column through distributed shared memory in rank order
+  // and writes grad_l = M_l - W_l P1_l (the negative of GaussNewton.py:401-427).
+  // Deterministic: every sum has a fixed order.
+  // -------------------------------------------------------------------------
+  __device__ bool l3_slab_split_ok() const {
+    const int SL = (int)g3_stage(d[1], d[2]);
+    return R <= 64 && (d[1] + d[2]) * 64 <= 3 * SL;
+  }
+
+  template <bool STAGED>
+  __device__ void gradient_l3s() {
+    long long gt = gprof ? clock64() : 0;
+    auto gtick = [&](int ph) {
+      if (gprof) {
+        const long long now = clock64();
+        gprof[ph] += now - gt;
+        gt = now;
+      }
+    };
+    constexpr int NW = TFX_THREADS / 32;
+    const int d0 = d[0], d1 = d[1], d2 = d[2];
+    char* smb = dyn_smem();
+    const T* Wl = STAGED ? (const T*)(smb + cgo.sWf) : W;
+    const T* P1l = STAGED ? (const T*)(smb + cgo.sP1o) : P1;
+    const int p1s = STAGED ? ncol : R;  // P1 column stride
+    const int p1c = STAGED ? 0 : c0;    // P1 column offset
+    const int SL = (int)g3_stage(d1, d2);
+    T* sT = (T*)(smb + g3off);  // 3 stages, then the M1 | M2 partials (64 columns a row)
+    T* sM1p = sT;
+    T* sM2p = sT + d1 * 64;
+    T* sP0x = sT + g3_p0x(d0, d1, d2);  // [2][NW][64] M0 warp partials
+    unsigned long long* mbar = (unsigned long long*)(smb + g3off + g3_floats(d0, d1, d2) * sizeof(T));
+    const T* W0 = Wl + off[0];
+    const T* W1 = Wl + off[1];
+    const T* W2 = Wl + off[2];
+    T* M0g = z + off[0];  // M0 rows, column-major like the factors (z is free outside the CG)
+    const int lane = tid & 31, wid = tid >> 5;
+    const int tx = tid & 15, ty = tid >> 4;
+    const int i0 = (int)((long long)d0 * tm.rank / tm.size);
+    const int ns = (int)((long long)d0 * (tm.rank + 1) / tm.size) - i0;
+    const unsigned bytes = (unsigned)((size_t)d1 * d2 * sizeof(T));
+    auto issue = [&](int t) {
+      if (tid == 0) {
+        const int b = (int)((g3base + t) % 3);
+        const unsigned mb = (unsigned)__cvta_generic_to_shared(mbar + b);
+        const unsigned dst = (unsigned)__cvta_generic_to_shared(sT + b * SL);
+        // the stage's previous contents were read (or written) by the generic proxy
+        asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(mb), "r"(bytes) : "memory");
+        asm volatile(
+            "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(dst),
+            "l"(Tt + (long long)(i0 + t) * d1 * d2), "r"(bytes), "r"(mb)
+            : "memory");
+      }
+    };
+    auto wait_slab = [&](int t) {
+      const unsigned n = g3base + t;
+      const unsigned mb = (unsigned)__cvta_generic_to_shared(mbar + n % 3);
+      const unsigned par = (n / 3) & 1;
+      if (!mbar_wait_bounded(mb, par, 1u << 24)) g3err = 1;
+    };
+    // M0 row of slab t from the warp partials of buffer (t & 1), by 64 threads
+    auto m0_row = [&](int t) {
+      if (tid < 64 && tid < R) {
+        const T* pp = sP0x + (t & 1) * NW * 64 + tid;
+        T sacc = pp[0];
+#pragma unroll
+        for (int w = 1; w < NW; ++w) sacc += pp[w * 64];
+        M0g[tid * d0 + i0 + t] = sacc;
+      }
+    };
+    __syncthreads();  // every stage is free (the previous phase ended with barriers)
+    if (ns > 0) issue(0);
+    if (ns > 1) issue(1);
+    T m1a[4][4], m2a[4][4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+#pragma unroll
+      for (int v = 0; v < 4; ++v) {
+        m1a[u][v] = T(0);
+        m2a[u][v] = T(0);
+      }
+    gtick(0);
+    for (int t = 0; t < ns; ++t) {
+      wait_slab(t);
+      __syncthreads();  // every warp is past slab t-1: its stage may be refilled
+      gtick(1);
+      if (t + 2 < ns) issue(t + 2);
+      if (t > 0) m0_row(t - 1);
+      gtick(2);
+      const T* tr = sT + ((g3base + t) % 3) * SL;
+      const int i = i0 + t;
+      T w0[4];
+#pragma unroll
+      for (int v = 0; v < 4; ++v) {
+        const int r = tx + 16 * v;
+        w0[v] = r < R ? W0[r * d0 + i] : T(0);
+      }
+      // Y = T[i] W2 (rows j = ty + 16u, columns r = tx + 16v)
+      T y[4][4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+#pragma unroll
+        for (int v = 0; v < 4; ++v) y[u][v] = T(0);
+#pragma unroll 2
+      for (int k = 0; k < d2; ++k) {
+        T a[4], b[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) a[u] = (ty + 16 * u < d1) ? tr[(ty + 16 * u) * d2 + k] : T(0);
+#pragma unroll
+        for (int v = 0; v < 4; ++v) b[v] = (tx + 16 * v < R) ? W2[(tx + 16 * v) * d2 + k] : T(0);
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+#pragma unroll
+          for (int v = 0; v < 4; ++v) y[u][v] = fma(a[u], b[v], y[u][v]);
+      }
+      // M1 partial and this slab's M0 partial (over the thread's rows)
+      T p[4] = {T(0), T(0), T(0), T(0)};
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int j = ty + 16 * u;
+#pragma unroll
+        for (int v = 0; v < 4; ++v) {
+          const int r = tx + 16 * v;
+          m1a[u][v] = fma(y[u][v], w0[v], m1a[u][v]);
+          if (j < d1 && r < R) p[v] = fma(y[u][v], W1[r * d1 + j], p[v]);
+        }
+      }
+#pragma unroll
+      for (int v = 0; v < 4; ++v) p[v] += __shfl_xor_sync(0xffffffffu, p[v], 16);
+      if (lane < 16)
+#pragma unroll
+        for (int v = 0; v < 4; ++v) sP0x[(t & 1) * NW * 64 + wid * 64 + tx + 16 * v] = p[v];
+      // M2 partial: (T[i]^T W1)[k, r] W0[i, r] (rows k = ty + 16u)
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+#pragma unroll
+        for (int v = 0; v < 4; ++v) y[u][v] = T(0);
+#pragma unroll 2
+      for (int j = 0; j < d1; ++j) {
+        T a[4], b[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) a[u] = (ty + 16 * u < d2) ? tr[j * d2 + ty + 16 * u] : T(0);
+#pragma unroll
+        for (int v = 0; v < 4; ++v) b[v] = (tx + 16 * v < R) ? W1[(tx + 16 * v) * d1 + j] : T(0);
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+#pragma unroll
+          for (int v = 0; v < 4; ++v) y[u][v] = fma(a[u], b[v], y[u][v]);
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+#pragma unroll
+        for (int v = 0; v < 4; ++v) m2a[u][v] = fma(y[u][v], w0[v], m2a[u][v]);
+      gtick(3);
+    }
+    __syncthreads();  // every slab consumed; the stages are idle (every copy was waited for)
+    if (ns > 0) m0_row(ns - 1);
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+#pragma unroll
+      for (int v = 0; v < 4; ++v) {
+        const int r = tx + 16 * v, row = ty + 16 * u;
+        if (r < R) {
+          if (row < d1) sM1p[row * 64 + r] = m1a[u][v];
+          if (row < d2) sM2p[row * 64 + r] = m2a[u][v];
+        }
+      }
+    g3base += ns;
+    tm.sync();  // partials and M0 rows visible to the team
+    gtick(4);
+    const int sd = d0 + d1 + d2;
+    for (int e = tid; e < sd * ncol; e += TFX_THREADS) {
+      const int c = e / sd;
+      int l = 0, i = e - c * sd;
+      if (i >= d0) {
+        i -= d0;
+        l = 1;
+        if (i >= d1) {
+          i -= d1;
+          l = 2;
+        }
+      }
+      const int col = c0 + c;
+      T m;
+      if (l == 0) {
+        m = __ldcg(M0g + col * d0 + i);
+      } else {
+        const T* part = (l == 1 ? sM1p : sM2p) + i * 64 + col;
+        T pv[TFX_MAX_TEAM];
+#pragma unroll
+        for (int q = 0; q < TFX_MAX_TEAM; ++q) pv[q] = q < tm.size ? *tm.peer(part, q) : T(0);
+        m = pv[0];
+#pragma unroll
+        for (int q = 1; q < TFX_MAX_TEAM; ++q)
+          if (q < tm.size) m += pv[q];
+      }
+      const int dl = d[l];
+      T wp = T(0);
+      const T* p1 = P1l + (size_t)l * R * p1s + p1c + c;
+      for (int s2 = 0; s2 < R; ++s2) wp = fma(Wl[off[l] + s2 * dl + i], p1[s2 * p1s], wp);
+      grad[off[l] + col * dl + i] = m - wp;
+    }
+    gtick(5);
+    // the peers are done reading this CTA's partials; the CG reads every column
+    tm.sync();
+    gtick(7);
+  }
+
+  // the gradient by the fastest form that applies
+  __device__ void gradient_any() {
+    if (sG3 && l3_slab_split_ok()) {
+      if (stage)
+        gradient_l3s<true>();
+      else
+        gradient_l3s<false>();
+    } else if (sG3) {
+      if (stage)
+        gradient_l3<true>();
+      else
+        gradient_l3<false>();
+    } else {
+      gradient();
+    }
+  }
+
+  // -------------------------------------------------------------------------
   // Gradient (GaussNewton.py:401-427): grad_l = T_(l) KR_l - W_l P1_l, the
   // negative of the reference's g.  Split-K over the team, partial d_l x R
   // tiles summed through distributed shared memory by the CTA owning the column.
@@ -1671,12 +1911,7 @@ __device__ void solve_problem(const tfx_dgn_problem& pb, const tfx_dgn_options& 
     tick(6);
     E.gramians_and_precond();
     tick(0);
-    if (E.sG3 && E.stage)
-      E.template gradient_l3<true>();
-    else if (E.sG3)
-      E.template gradient_l3<false>();
-    else
-      E.gradient();
+    E.gradient_any();
     tick(1);
     double rn;
     const int itn = E.cg(pb.budgets[it], rn);
@@ -1874,12 +2109,7 @@ __global__ void __launch_bounds__(TFX_THREADS, 1)
     E.gramians_and_precond();
     if (ua.grad) {
       T* gout = (T*)ua.grad;
-      if (E.sG3 && E.stage)
-        E.template gradient_l3<true>();
-      else if (E.sG3)
-        E.template gradient_l3<false>();
-      else
-        E.gradient();
+      E.gradient_any();
       // the engine keeps M_l - W_l P1_l; the reference's g is its negative
       E.for_own([&](int e, int l, int c) { gout[e] = -E.grad[e]; });
     }

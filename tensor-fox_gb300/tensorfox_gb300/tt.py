@@ -165,57 +165,64 @@ def _tricpd(G1, R, options):
         options.method = saved
 
 
-def cpd_cores(G, max_trials, epochs, R, options, prec):
-    """Auxiliar.py:413-527: CPDs of the inner cores, left to right (and back when
-    ``epochs`` > 1), each the best of ``max_trials`` (stopping early below 1e-4)."""
-    L = len(G)
-    if epochs % 2 == 0:
-        epochs += 1
-    cpd_list = list(range(L - 2))
-    outputs = list(range(L - 2))
-    best = np.inf
-    for _ in range(max_trials):
-        f, out = _tricpd(G[1], R, options)
-        if out.rel_error < best:
-            best_out, best = out, out.rel_error
-            bX, bY, bZ = f
-            if best < 1e-4:
-                break
-    outputs[0] = best_out
-    cpd_list[0] = [bX, bY, bZ]
-    low, upp = 2, L - 2
-    for epoch in range(epochs):
-        if epoch % 2 == 0:
-            for l in range(low, L - 1):
-                best = np.inf
-                fX = np.linalg.pinv(bZ.T)
-                for _ in range(max_trials):
-                    X, Y, Z, out = bicpd(G[l], R, [fX, 0], options, prec)
-                    if out.rel_error < best:
-                        best_out, best = out, out.rel_error
-                        bX, bY, bZ = fX, Y, Z
-                        if best < 1e-4:
-                            break
-                if epoch == epochs - 1:
-                    outputs[l - 1] = best_out
-                    cpd_list[l - 1] = [fX, bY, bZ]
+def sweep_schedule(L, epochs):
+    """The order in which the inner cores G[1..L-2] are decomposed after the
+    first one, as ``(core, fixed_mode, record)`` steps (Auxiliar.py:413-527).
+
+    The epoch count is made odd.  Even epochs walk forward and fix each core's
+    first factor (mode 0) from the previous core's last one; odd epochs walk
+    backward and fix the last factor (mode 2) from the previous core's first
+    one.  Forward walks start at core 2; for order 3 the first backward walk
+    moves the start to core 1, and backward walks cover cores 1 .. L-3 (core 1
+    for order 3).  ``record``: the step's result is the one kept for its core --
+    forward steps of the last epoch, backward steps of the one before it."""
+    epochs = epochs + 1 - epochs % 2
+    steps = []
+    fwd_start = 2
+    for e in range(epochs):
+        if e % 2 == 0:
+            steps += [(l, 0, e == epochs - 1) for l in range(fwd_start, L - 1)]
         else:
             if L == 3:
-                low, upp = 1, L - 1
-            for l in reversed(range(1, upp)):
-                best = np.inf
-                fZ = np.linalg.pinv(bX.T)
-                for _ in range(max_trials):
-                    X, Y, Z, out = bicpd(G[l], R, [fZ, 2], options, prec)
-                    if out.rel_error < best:
-                        best_out, best = out, out.rel_error
-                        bX, bY, bZ = X, Y, fZ
-                        if best < 1e-4:
-                            break
-                if epoch == epochs - 2:
-                    outputs[l - 1] = best_out
-                    cpd_list[l - 1] = [bX, bY, fZ]
-    return cpd_list, outputs, bZ
+                fwd_start = 1
+            top = L - 1 if L == 3 else L - 2
+            steps += [(l, 2, e == epochs - 2) for l in range(top - 1, 0, -1)]
+    return steps
+
+
+def _best_of(max_trials, trial):
+    """The trial with the smallest relative error, stopping below 1e-4."""
+    best = None
+    for _ in range(max_trials):
+        f, out = trial()
+        if best is None or out.rel_error < best[1].rel_error:
+            best = (f, out)
+            if out.rel_error < 1e-4:
+                break
+    return best
+
+
+def cpd_cores(G, max_trials, epochs, R, options, prec):
+    """CPDs of the inner TT cores (Auxiliar.py:413-527): core 1 by ``tricpd``,
+    then every step of ``sweep_schedule`` by ``bicpd`` with one factor fixed to
+    the pseudo-inverse link of its neighbour's result.  Returns the kept
+    factors and outputs per inner core and the last step's third factor."""
+    L = len(G)
+    kept = [None] * (L - 2)
+    outs = [None] * (L - 2)
+    link, outs[0] = _best_of(max_trials, lambda: _tricpd(G[1], R, options))
+    link = list(link)
+    kept[0] = link
+    for core, fmode, record in sweep_schedule(L, epochs):
+        fixed = np.linalg.pinv((link[2] if fmode == 0 else link[0]).T)
+
+        def trial():
+            X, Y, Z, out = bicpd(G[core], R, [fixed, fmode], options, prec)
+            return ([fixed, Y, Z] if fmode == 0 else [X, Y, fixed]), out
+        link, out = _best_of(max_trials, trial)
+        if record:
+            kept[core - 1], outs[core - 1] = link, out
+    return kept, outs, link[2]
 
 
 def highcpd(S, R, options, prec):

@@ -112,7 +112,11 @@ def test_coo_gram_wide_dims_no_key_wrap():
     idxs = np.array(rows, dtype=np.int64)
     data = rng.standard_normal(len(idxs))
     want = fibre_gram(data, idxs, 6, 0)
-    assert want[0, 2] == 0.0 and want[1, 3] == 0.0      # A and B never meet
+    # what a wrapped 64-bit key would give: fibres A and B merged
+    merged = idxs.copy()
+    merged[2:4, 1:] = A
+    wrapped = fibre_gram(data, merged, 6, 0)
+    assert not np.allclose(want, wrapped)
     X = sparse.DeviceCOO(data, idxs, dims, torch.float64)
     np.testing.assert_allclose(X.gram(0).cpu().numpy(), want, rtol=1e-12, atol=1e-12)
 
