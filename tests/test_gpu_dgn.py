@@ -153,3 +153,34 @@ def test_dgn_options_match_reference(name):
     assert len(er) == len(g["errors"])
     np.testing.assert_allclose(er, g["errors"], rtol=1e-6, atol=1e-12)
     np.testing.assert_allclose(ss, g["step_sizes"], rtol=1e-4, atol=1e-12)
+
+
+@pytest.mark.parametrize("dims,R", [((50, 48, 44), 12), ((50, 50, 50), 50), ((64, 60, 56), 24)])
+def test_dgn_large_core_slab_split_gradient_vs_oracle(dims, R):
+    """Cores large enough for the slab-split gradient (every CTA streams its own
+    slabs for all columns, partials summed through distributed shared memory):
+    FP64 trajectories equal the oracle's for several cluster sizes; FP32 stays
+    within 1e-3 of them over the first iterations (the FP32 and FP64 paths
+    drift apart by rounding as the damping and CG caps compound it)."""
+    rng = np.random.default_rng(31)
+    W = [rng.standard_normal((d, R)) for d in dims]
+    T = orc.cpd2tens(W) + 1e-3 * rng.standard_normal(dims)
+    init = [w + 0.2 * rng.standard_normal(w.shape) for w in W]
+
+    class O:
+        inner_method = 'cg_static'
+        cg_maxiter = 10
+        maxiter = 12
+    _, ss0, er0, _, gr0, st0 = orc.dGN(T, [w.copy() for w in init], R, orc.make_options(O))
+    for c in (None, 4, 12):
+        if c is not None and c > R:
+            continue
+        o = tfx.make_options(O)
+        o.cluster = c
+        _, ss1, er1, _, gr1, st1 = tfx.dGN(T, [w.copy() for w in init], R, o)
+        assert st1 == st0 and len(er1) == len(er0)
+        np.testing.assert_allclose(er1, er0, rtol=1e-8)
+        np.testing.assert_allclose(gr1, gr0, rtol=1e-6)
+        o.precision = 'fp32'
+        _, _, er2, _, _, _ = tfx.dGN(T.astype(np.float32), [w.copy() for w in init], R, o)
+        np.testing.assert_allclose(er2[:6], er0[:6], rtol=1e-3)
