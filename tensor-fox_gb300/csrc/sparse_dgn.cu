@@ -565,6 +565,53 @@ __global__ void __launch_bounds__(TFX_THREADS) k_dogleg_trial(long long n, const
   }
 }
 
+// the scalars of an accepted step (GaussNewton.py:472-487, 199-211):
+// partials of (x - x_old).(grad + damp (x - x_old)), |x - x_old|^2, |x_old|^2, max|grad|
+template <class T>
+__global__ void __launch_bounds__(TFX_THREADS) k_step_sums(long long n, const T* __restrict__ x,
+                                                            const T* __restrict__ x_old,
+                                                            const double* __restrict__ grad, double damp,
+                                                            double* __restrict__ part) {
+  __shared__ double sw[4][TFX_THREADS / 32];
+  double s[4] = {0.0, 0.0, 0.0, 0.0};
+  for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x) {
+    const double dx = (double)x[k] - (double)x_old[k];
+    s[0] += dx * (grad[k] + damp * dx);
+    s[1] += dx * dx;
+    s[2] += (double)x_old[k] * (double)x_old[k];
+    s[3] = fmax(s[3], fabs(grad[k]));
+  }
+  for (int j = 0; j < 4; ++j) {
+    const double v = j == 3 ? warp_max(s[j]) : warp_sum(s[j]);
+    if ((threadIdx.x & 31) == 0) sw[j][threadIdx.x >> 5] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < 4) {
+    double t = 0.0;
+    for (int w = 0; w < TFX_THREADS / 32; ++w)
+      t = threadIdx.x == 3 ? fmax(t, sw[3][w]) : t + sw[threadIdx.x][w];
+    part[(size_t)blockIdx.x * 4 + threadIdx.x] = t;
+  }
+}
+
+__global__ void k_sum_parts4(const double* part, int nb, double* out) {
+  if (threadIdx.x < 4) {
+    double s = 0.0;
+    for (int c = 0; c < nb; ++c) {
+      const double v = part[(size_t)c * 4 + threadIdx.x];
+      s = threadIdx.x == 3 ? fmax(s, v) : s + v;
+    }
+    out[threadIdx.x] = s;
+  }
+}
+
+// x_out = x - y (the reference's revert of a rejected step, in floating point)
+template <class T>
+__global__ void k_revert(long long n, const T* __restrict__ x, const double* __restrict__ y, T* __restrict__ x_out) {
+  for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x)
+    x_out[k] = x[k] - (T)y[k];
+}
+
 static int launched(const char* where) {
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return tfx_set_cuda_error(e, where);
@@ -722,4 +769,31 @@ extern "C" int tfx_dogleg_trial(int dtype, long long n, const void* x_old, doubl
   if (int s = launched("dogleg_trial")) return s;
   k_sum_parts<<<1, 32, 0, st>>>((const double*)scratch, blocks, 2, out2);
   return launched("sum_parts");
+}
+
+extern "C" int tfx_step_sums(int dtype, long long n, const void* x, const void* x_old, const double* grad, double damp,
+                             double* out4, void* scratch, void* stream) {
+  if (n < 0 || !x || !x_old || !grad || !out4 || !scratch) return tfx_set_error(TFX_STATUS_ERR_ARG, "step_sums args");
+  cudaStream_t st = (cudaStream_t)stream;
+  const int blocks = (int)std::max<long long>(1, std::min<long long>((n + 255) / 256, 1024));
+  if (dtype == TFX_F64)
+    k_step_sums<double><<<blocks, TFX_THREADS, 0, st>>>(n, (const double*)x, (const double*)x_old, grad, damp,
+                                                        (double*)scratch);
+  else
+    k_step_sums<float><<<blocks, TFX_THREADS, 0, st>>>(n, (const float*)x, (const float*)x_old, grad, damp,
+                                                       (double*)scratch);
+  if (int s = launched("step_sums")) return s;
+  k_sum_parts4<<<1, 32, 0, st>>>((const double*)scratch, blocks, out4);
+  return launched("sum_parts4");
+}
+
+extern "C" int tfx_step_revert(int dtype, long long n, const void* x, const double* y, void* x_out, void* stream) {
+  if (n < 0 || !x || !y || !x_out) return tfx_set_error(TFX_STATUS_ERR_ARG, "step_revert args");
+  cudaStream_t st = (cudaStream_t)stream;
+  const int blocks = (int)std::max<long long>(1, std::min<long long>((n + 255) / 256, 1024));
+  if (dtype == TFX_F64)
+    k_revert<double><<<blocks, 256, 0, st>>>(n, (const double*)x, y, (double*)x_out);
+  else
+    k_revert<float><<<blocks, 256, 0, st>>>(n, (const float*)x, y, (float*)x_out);
+  return launched("step_revert");
 }

@@ -104,6 +104,13 @@ _SZ = c_size_t
 _EXTRA_SIGNATURES = {
     "tfx_mode_gram": [_I, _P, _LL, _I, _LL, _P, _P, _SZ, _P],
     "tfx_wait_probe": [ctypes.c_uint, _P, _P],
+    "tfx_coo_dgn_cg": [_I, _I, POINTER(c_int), _I, _P, _P, _D, _I, _D, _P, _P, _P, _P, _P, _SZ, _P],
+    "tfx_coo_model_error": [_I, _I, POINTER(c_int), _I, _P, _P, _D, _P, _P, _SZ, _P],
+    "tfx_factors_to_rows": [_I, _I, POINTER(c_int), _I, _P, _P, _P],
+    "tfx_dogleg_dots": [_LL, _P, _P, _P, _P, _P, _P, _P, _P, _P],
+    "tfx_dogleg_trial": [_I, _LL, _P, _P, _P, _D, _D, _D, _P, _P, _P, _P, _P],
+    "tfx_step_sums": [_I, _LL, _P, _P, _P, _D, _P, _P, _P],
+    "tfx_step_revert": [_I, _LL, _P, _P, _P, _P],
     "tfx_gemm": [_I, _P, _P, _P, _LL, _LL, _LL, _LL, POINTER(c_longlong), _D, _D, _P],
     "tfx_orthonormalize": [_I, _P, _I, _I, _P],
     "tfx_ttm": [_I, _P, _LL, _I, _LL, _P, _I, _P, _P],
@@ -133,6 +140,9 @@ _SIZE_FUNCS = {
     "tfx_sparse_ttmc_scratch_bytes": [_I, _LL, _I, POINTER(c_int)],
     "tfx_als_workspace_bytes": [_I, _I, POINTER(c_int), _I],
     "tfx_dgn_direct_workspace_bytes": [_I, _I, POINTER(c_int), _I],
+    "tfx_coo_dgn_cg_workspace_bytes": [_I, _I, POINTER(c_int), _I],
+    "tfx_coo_model_error_scratch_bytes": [_I, _I],
+    "tfx_dogleg_scratch_bytes": [],
 }
 
 

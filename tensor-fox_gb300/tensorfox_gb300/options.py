@@ -5,15 +5,18 @@ defaults, exactly like the reference.  Three fields are added by this package an
 ignored by the reference: ``precision`` ('fp64', 'fp32' or None for the input's
 own type, 'mixed' = FP32 data with TF32 tensor-core contractions for the
 compression), ``cluster`` (CTAs per problem in the device engine, None = auto)
-and ``tile`` (the engine's register tile, 1, 2 or 4; None = chosen by size, or by
-the autotuner in ``cpd_batch``).
+``tile`` (the engine's register tile, 1, 2 or 4; None = chosen by size, or by
+the autotuner in ``cpd_batch``) and ``sparse_solver`` (None = the reference's
+path for a COO tensor: compression, then dGN on the dense core; 'direct' = dGN
+on the COO tensor itself, gradient and error from COO MTTKRPs).
 """
 
 _DEFAULTS = dict(maxiter=200, tol=1e-16, tol_step=1e-6, tol_improv=1e-6, tol_grad=1e-6, tol_jump=10,
                  method='dGN', inner_method='cg', cg_maxiter=100, cg_factor=1, cg_tol=1e-16,
                  initialization='random', trunc_dims=0, mlsvd_method='seq', tol_mlsvd=1e-16, init_damp=1,
                  refine=False, symm=False, factors_norm=0, trials=3, display=0, epochs=1, gpu=False,
-                 mkl_dot=True, svd_n_components=None, precision=None, cluster=None, tile=None)
+                 mkl_dot=True, svd_n_components=None, precision=None, cluster=None, tile=None,
+                 sparse_solver=None)
 
 
 class Options:

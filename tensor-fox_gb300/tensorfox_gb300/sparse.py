@@ -159,6 +159,49 @@ def mlsvd_sparse_device(X, R, options):
     return S, Uts, sigmas
 
 
+def coo_provider(X, R):
+    """MTTKRP provider of a DeviceCOO for ``mttkrp_dgn.dgn_mttkrp``: writes
+    T_(l) KR_l (row-major) into the mode-l block of ``Mrm``."""
+    dims = X.dims
+    es = X.vals.element_size()
+    offs = np.concatenate([[0], np.cumsum([R * d for d in dims])])
+    cache = {}
+
+    def provide(Wrm, Mrm, modes):
+        key = Wrm.data_ptr()
+        if cache.get('key') != key:
+            cache['key'] = key
+            cache['ptrs'] = torch.tensor([key + int(offs[l]) * es for l in range(X.L)], dtype=torch.int64,
+                                         device=Wrm.device)
+        for l in modes:
+            rowptr, sidx, svals = X.sort_mode(l)
+            _lib.call("tfx_coo_mttkrp", X.dt(), _vp(sidx), _vp(svals), X.nnz, _vp(rowptr), X.L, _cint(dims), int(R),
+                      int(l), _vp(cache['ptrs']), ctypes.c_void_p(Mrm.data_ptr() + int(offs[l]) * es), _st())
+    return provide
+
+
+def tricpd_sparse_direct(X, data, R, o, prec, ordering, sdims, Tsize):
+    """dGN on the COO tensor itself (``options.sparse_solver = 'direct'``): no
+    compression; the start is drawn in the full space like the reference's
+    random start, the gradient and error come from COO MTTKRPs
+    (``mttkrp_dgn.dgn_mttkrp``).  The objective is the reference's (absent
+    entries are zeros of the data)."""
+    from .api import starting_point_random
+    from .mttkrp_dgn import dgn_mttkrp
+    dt = X.vals.dtype
+    dims = [int(d) for d in sdims]
+    if isinstance(o.initialization, list):
+        init = [np.asarray(o.initialization[ordering[l]], dtype=np.float64) for l in range(len(dims))]
+    elif o.initialization == 'random':
+        init = starting_point_random(dims, R, o)
+    else:
+        raise NotImplementedError("sparse_solver='direct' takes a 'random' or given start")
+    x0 = torch.from_numpy(_dev.flat_factors(init)).to(device=X.vals.device, dtype=dt)
+    nrm = kernels.tensor_norms(X.vals).cpu().numpy()
+    meanabs = float(nrm[1]) / float(np.prod(np.array(dims, dtype=np.float64)))
+    return dgn_mttkrp(coo_provider(X, R), dims, R, x0, o, prec, float(nrm[0]), meanabs)
+
+
 def tricpd_sparse(T, R, options):
     """``tricpd`` for ``[data, idxs, dims]`` (TensorFox.py:424-655, sparse branches)."""
     from .api import Output, starting_point_core, _decompress, _run_dgn, _run_als, unsort_dims
@@ -182,6 +225,12 @@ def tricpd_sparse(T, R, options):
     sdims = dims[ordering]
     X = DeviceCOO(data, idxs[:, ordering], sdims, dt)
     Tsize = float(np.linalg.norm(data))
+    if getattr(o, 'sparse_solver', None) == 'direct':
+        if o.method != 'dGN':
+            raise NotImplementedError("sparse_solver='direct' runs method 'dGN'")
+        best, ss, er, im, gr, st, _ = tricpd_sparse_direct(X, data, R, o, prec, ordering, sdims, Tsize)
+        factors = _dev.unflat(best.double().cpu().numpy(), [int(d) for d in sdims], R)
+        return _sparse_output(X, factors, ordering, Tsize, ss, er, im, gr, st, o)
     S, Uts, sigmas = mlsvd_sparse_device(X, R, o)
     core = [int(u.shape[0]) for u in Uts]
     if isinstance(o.initialization, list):
@@ -199,8 +248,15 @@ def tricpd_sparse(T, R, options):
         best, ss, er, im, gr, st = _run_dgn(S, x0, R, o, prec, aliased=alias)
     Wf = _decompress(Uts, best, core, R)
     factors = _dev.unflat(Wf.double().cpu().numpy(), [int(d) for d in sdims], R)
-    # final error on the stored entries (Auxiliar.py:155-159), sorted order
-    frm = [torch.from_numpy(np.ascontiguousarray(f)).to(S.device, dt) for f in factors]
+    return _sparse_output(X, factors, ordering, Tsize, ss, er, im, gr, st, o)
+
+
+def _sparse_output(X, factors, ordering, Tsize, ss, er, im, gr, st, o):
+    """Final error on the stored entries (Auxiliar.py:155-159) and the output
+    object; ``factors`` in the sorted mode order."""
+    from .api import Output, unsort_dims
+    dt = X.vals.dtype
+    frm = [torch.from_numpy(np.ascontiguousarray(f)).to(X.vals.device, dt) for f in factors]
     res = float(sparse_residual_sq(X, frm).cpu().numpy()[0])
     factors = unsort_dims(factors, ordering)
     out = Output()

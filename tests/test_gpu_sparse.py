@@ -189,3 +189,66 @@ def test_coo_vectorized_paths_with_unaligned_factors(R):
     for fac in (al, un):
         got = float(sparse.sparse_residual_sq(X, fac).item())
         assert abs(got - want) <= 1e-4 * want
+
+
+class _Static:
+    inner_method = 'cg_static'
+    cg_maxiter = 10
+    maxiter = 25
+
+
+@pytest.mark.parametrize("dims,R,nnz", [((12, 10, 9), 3, 400), ((9, 8, 7, 6), 2, 600), ((30, 25, 20), 6, 6000)])
+@pytest.mark.parametrize("dt", [torch.float64, torch.float32])
+def test_direct_coo_dgn_matches_dense_oracle(dims, R, nnz, dt):
+    """dGN on the COO tensor itself (gradient and error from COO MTTKRPs, CG on
+    the Gramians) against the oracle's dense dGN on sparse2dense of it, from the
+    same start: the reference's objective, absent entries being zeros."""
+    from tensorfox_gb300 import mttkrp_dgn
+    data, idxs, _ = coo(dims, R, nnz, 4)
+    T = dense_of(data, idxs, dims)
+    rng = np.random.default_rng(5)
+    init = [rng.standard_normal((d, R)) for d in dims]
+    _, ss0, er0, _, gr0, st0 = orc.dGN(T, [w.copy() for w in init], R, orc.make_options(_Static))
+    X = sparse.DeviceCOO(data, idxs, dims, dt)
+    prec = 'fp64' if dt == torch.float64 else 'fp32'
+    x0 = torch.from_numpy(orc.cpd2flat(init)).to("cuda", dt)
+    best, ss1, er1, _, gr1, st1, mv = mttkrp_dgn.dgn_mttkrp(sparse.coo_provider(X, R), list(dims), R, x0,
+                                                         tfx.make_options(_Static), prec, float(np.sum(T * T)),
+                                                         float(np.mean(np.abs(T))))
+    if dt == torch.float64:
+        assert st1 == st0 and len(er1) == len(er0)
+        np.testing.assert_allclose(er1, er0, rtol=1e-8)
+        np.testing.assert_allclose(ss1, ss0, rtol=1e-6, atol=1e-12)
+        np.testing.assert_allclose(gr1, gr0, rtol=1e-6)
+    else:
+        np.testing.assert_allclose(er1[:6], er0[:6], rtol=1e-4)
+    assert mv > len(er1)
+
+
+def test_direct_coo_cpd_equals_dense_uncompressed_oracle():
+    """cpd(..., sparse_solver='direct') draws the reference's random start in the
+    full space and runs dGN on the COO tensor: the same trajectory as the
+    oracle's cpd of the dense tensor without compression (tol_mlsvd = -1)."""
+    dims, R = (14, 12, 10), 3
+    data, idxs, _ = coo(dims, R, 700, 6)
+    T = dense_of(data, idxs, dims)
+
+    class O(_Static):
+        pass
+    o = tfx.make_options(O)
+    o.sparse_solver = 'direct'
+    np.random.seed(3)
+    f, out = tfx.cpd([data, idxs, np.array(dims)], R, o)
+    after = np.random.rand()
+    oo = orc.make_options(O)
+    oo.tol_mlsvd = -1
+    np.random.seed(3)
+    f0, out0 = orc.cpd(T, R, oo)
+    assert np.random.rand() == after                 # the RNG left where the reference leaves it
+    np.testing.assert_allclose(out.errors[0], out0.errors[0], rtol=1e-8)
+    # rel_error: the stored entries only, as the reference reports a sparse CPD
+    model = np.ones((len(data), R))
+    for l in range(3):
+        model *= f[l][idxs[:, l]]
+    want = np.linalg.norm(data - model.sum(1)) / np.linalg.norm(data)
+    assert abs(out.rel_error - want) <= 1e-10 * want
