@@ -205,6 +205,21 @@ size_t tfx_mttkrp_scratch_bytes(int dtype, int L, const int* dims, int R, int mo
 int tfx_mttkrp(int dtype, const void* T, int L, const int* dims, int R, const void* W, int mode, void* out, void* scratch,
                size_t scratch_bytes, void* stream);
 int tfx_cp_full(int dtype, int L, const int* dims, int R, const void* W, void* out, void* stream);
+/* The same product T_(l) KR_l of an FP32 tensor on the 5th-generation tensor
+ * cores (GaussNewton.py:401-427 compute_grad's contraction, 411-423): the
+ * tensor viewed as (P, d_l, Q) is the A operand, TMA-loaded straight from the
+ * C-order array; the B operand (the factor products) is formed in shared
+ * memory; tcgen05.mma kind::tf32 with every operand split hi + lo (3xTF32:
+ * FP32 accuracy), FP32 accumulation in TMEM, split-K partials summed in
+ * compensated FP32.  W: HOST array of L device pointers to the factors
+ * (column r of W_m at W[m] + r dims[m]).  Needs R <= 64, mode < L - 1 (for the
+ * last mode pass a copy of the tensor with that mode moved first), the product
+ * of the later dims a multiple of 4, T 16-byte aligned.  out: d_mode x R,
+ * row-major (col_major = 0) or column-major.  *err (device int) is set if a
+ * bounded wait ran out.  scratch: tfx_mttkrp_tc_scratch_bytes(). */
+size_t tfx_mttkrp_tc_scratch_bytes(int L, const int* dims, int R, int mode);
+int tfx_mttkrp_tc(const float* T, int L, const int* dims, int R, const float* const* W, int mode, float* out,
+                  int col_major, void* scratch, size_t scratch_bytes, int* err, void* stream);
 size_t tfx_cp_wp1_scratch_bytes(int L, int R);
 int tfx_cp_wp1(int dtype, int L, const int* dims, int R, const void* W, void* out, void* scratch, void* stream);
 /* Backward of the fit loss ||T - [[W]]||^2 in one call: grad (flat layout) =
@@ -244,6 +259,46 @@ int tfx_coo_gram(int dtype, const int* idx32, const void* vals, long long nnz, c
 /* MultilinearAlgebra.py:145-190 sparse_multilin_mult (Critical.py:2703-2720):
  * dense core S (n_0 x ... x n_{L-1}) = T x_1 U_1^T ... ; U_dev: device array of
  * L pointers to row-major (d_l x n_l) matrices. */
+/* ---- dGN driven by MTTKRPs (the direct COO solver; no reference
+ * counterpart: the reference compresses a COO tensor before dGN).  The
+ * reference's objective with absent entries as zeros:
+ * ||T - [[W]]||^2 = ||T||^2 - 2 <W_0, T_(0) KR_0> + sum prod_l G_l.
+ * tfx_coo_dgn_cg: one dGN iteration's inner solve (GaussNewton.py:315-398):
+ * Gramians, P1/P2 (:520-548), regularisation and preconditioner (:584-627),
+ * y = M (CG solution), grad = T_(l) KR_l - W_l P1_l (the CG's grad, -g of
+ * :401-427) and J^T J grad, all FP64 flat vectors, from the factors W (flat)
+ * and the L MTTKRPs Mrm (row-major d_l x R blocks at the flat offsets); ONE
+ * cooperative launch (one CTA per SM) whose CTAs meet at bounded grid
+ * barriers; out[0] = J^T J products, out[1] = the last residual norm^2,
+ * out[2] = 3 if a barrier ran out.  work: 256-byte aligned,
+ * tfx_coo_dgn_cg_workspace_bytes().  Order and rank within the kernel's shared
+ * memory (3 L R^2 + L^2 R^2 elements <= 200 KB).
+ * tfx_coo_model_error: out[0] = ||T - [[W]]||^2 from ||T||^2, W and the mode-0
+ * MTTKRP (row-major), out[1] = <W_0, M_0>, out[2] = ||[[W]]||^2.
+ * tfx_factors_to_rows: the flat factors as row-major d_l x R blocks.
+ * tfx_dogleg_dots: out3 = {a.b, c.d, e.f}; tfx_dogleg_trial: one trial of
+ * GaussNewton.py:713-795: y <- ca y + cb grad (rounded to the working type),
+ * x = x_old + y, W = x, out2 = {(x - x_old).(grad + damp (x - x_old)),
+ * |x - x_old|^2}; tfx_step_sums: out4 = {(x - x_old).(grad + damp (x -
+ * x_old)), |x - x_old|^2, |x_old|^2, max|grad|}; tfx_step_revert: x_out =
+ * x - y.  scratch: tfx_dogleg_scratch_bytes(). */
+size_t tfx_coo_dgn_cg_workspace_bytes(int dtype, int L, const int* dims, int R);
+int tfx_coo_dgn_cg(int dtype, int L, const int* dims, int R, const void* W, const void* Mrm, double damp, int budget,
+                   double cg_tol, double* y, double* grad, double* jtj, double* out, void* work, size_t work_bytes,
+                   void* stream);
+size_t tfx_coo_model_error_scratch_bytes(int L, int R);
+int tfx_coo_model_error(int dtype, int L, const int* dims, int R, const void* W, const void* M0rm, double tnorm2,
+                        double* out, void* scratch, size_t scratch_bytes, void* stream);
+int tfx_factors_to_rows(int dtype, int L, const int* dims, int R, const void* W, void* Wrm, void* stream);
+size_t tfx_dogleg_scratch_bytes(void);
+int tfx_dogleg_dots(long long n, const double* a, const double* b, const double* c, const double* d, const double* e,
+                    const double* f, double* out3, void* scratch, void* stream);
+int tfx_dogleg_trial(int dtype, long long n, const void* x_old, double* y, const double* grad, double ca, double cb,
+                     double damp, void* x, void* W, double* out2, void* scratch, void* stream);
+int tfx_step_sums(int dtype, long long n, const void* x, const void* x_old, const double* grad, double damp,
+                  double* out4, void* scratch, void* stream);
+int tfx_step_revert(int dtype, long long n, const void* x, const double* y, void* x_out, void* stream);
+
 size_t tfx_sparse_ttmc_scratch_bytes(int dtype, long long nnz, int L, const int* n);
 int tfx_sparse_ttmc(int dtype, const int* idx32, const void* vals, long long nnz, int L, const int* dims, const int* n,
                     const void* const* U_dev, void* S, void* scratch, size_t scratch_bytes, void* stream);

@@ -111,6 +111,7 @@ _EXTRA_SIGNATURES = {
     "tfx_dogleg_trial": [_I, _LL, _P, _P, _P, _D, _D, _D, _P, _P, _P, _P, _P],
     "tfx_step_sums": [_I, _LL, _P, _P, _P, _D, _P, _P, _P],
     "tfx_step_revert": [_I, _LL, _P, _P, _P, _P],
+    "tfx_mttkrp_tc": [_P, _I, POINTER(c_int), _I, _P, _I, _P, _I, _P, _SZ, _P, _P],
     "tfx_gemm": [_I, _P, _P, _P, _LL, _LL, _LL, _LL, POINTER(c_longlong), _D, _D, _P],
     "tfx_orthonormalize": [_I, _P, _I, _I, _P],
     "tfx_ttm": [_I, _P, _LL, _I, _LL, _P, _I, _P, _P],
@@ -143,6 +144,7 @@ _SIZE_FUNCS = {
     "tfx_coo_dgn_cg_workspace_bytes": [_I, _I, POINTER(c_int), _I],
     "tfx_coo_model_error_scratch_bytes": [_I, _I],
     "tfx_dogleg_scratch_bytes": [],
+    "tfx_mttkrp_tc_scratch_bytes": [_I, POINTER(c_int), _I, _I],
 }
 
 

@@ -147,7 +147,18 @@ def _run_dgn(Td, x0, R, options, prec, aliased=False, fix_mode=-1):
     from .stepped import uses_stepped, dgn_stepped
     if uses_stepped(options):
         return dgn_stepped(Td, x0, R, options, prec, fix_mode=fix_mode, aliased=aliased)
+    if Td.numel() >= DENSE_MTTKRP_MIN and fix_mode < 0 and not aliased:
+        # a large FP32 tensor (the refinement on the full tensor, or no
+        # compression): tensor-core MTTKRPs and a grid-wide CG instead of one
+        # thread-block cluster streaming the whole tensor
+        from .mttkrp_dgn import dense_supported, dgn_dense
+        if dense_supported(Td, R, options, prec):
+            return dgn_dense(Td, x0, R, options)[:6]
     return _engine_collect(_engine_launch(Td, x0, R, options, prec, aliased, fix_mode), options)
+
+
+# tensors of at least this many entries take the MTTKRP-driven dGN when it applies
+DENSE_MTTKRP_MIN = 1 << 22
 
 
 def _engine_launch(Td, x0, R, options, prec, aliased=False, fix_mode=-1):

@@ -163,3 +163,52 @@ def tensor_norms(T):
     out = torch.empty(2, dtype=torch.float64, device=T.device)
     _lib.call("tfx_tensor_norms", _dt(T), _vp(T), int(T.numel()), _vp(out), _vp(scratch), _st())
     return out
+
+
+def mttkrp_tc_supported(T, dims, R, mode):
+    """The tensor-core MTTKRP applies: FP32, order >= 3, R <= 64, the later dims'
+    product (of the tensor the kernel reads) a multiple of 4, 16-byte aligned."""
+    L = len(dims)
+    if T.dtype != torch.float32 or L < 3 or R > 64 or T.data_ptr() % 16 != 0:
+        return False
+    if mode < L - 1:
+        return int(np.prod(dims[mode + 1:], dtype=np.int64)) % 4 == 0
+    return int(np.prod(dims[:L - 1], dtype=np.int64)) % 4 == 0
+
+
+def last_mode_first(T, dims):
+    """A copy of the tensor with its last mode moved first (the tensor-core
+    MTTKRP's operand for the last mode)."""
+    L = len(dims)
+    return T.reshape(dims).permute(L - 1, *range(L - 1)).contiguous()
+
+
+def mttkrp_tc(T, dims, W_flat, R, mode, col_major=False, T_last=None, out=None):
+    """``T_(mode) KR`` on the tensor cores (tcgen05, 3xTF32, FP32 accumulation).
+
+    ``W_flat``: the factors in the flat layout (column-major blocks).  The last
+    mode reads ``T_last`` (``last_mode_first(T, dims)``, made here if absent).
+    Returns (d_mode x R) row-major, or column-major with ``col_major``."""
+    L = len(dims)
+    dims = [int(d) for d in dims]
+    offs = np.concatenate([[0], np.cumsum([R * d for d in dims])])
+    base = W_flat.data_ptr()
+    if mode < L - 1:
+        Tk, dk, mk = T, dims, mode
+        ptrs = [base + int(offs[m]) * 4 for m in range(L)]
+    else:
+        Tk = T_last if T_last is not None else last_mode_first(T, dims)
+        dk = [dims[L - 1]] + dims[:L - 1]
+        mk = 0
+        ptrs = [base + int(offs[L - 1]) * 4] + [base + int(offs[m]) * 4 for m in range(L - 1)]
+    lib = _lib.load()
+    cd = (ctypes.c_int * L)(*dk)
+    nb = int(lib.tfx_mttkrp_tc_scratch_bytes(L, cd, int(R), int(mk)))
+    scratch = torch.empty(nb, dtype=torch.uint8, device=T.device)
+    err = torch.zeros(1, dtype=torch.int32, device=T.device)
+    if out is None:
+        out = torch.empty((dims[mode], R) if not col_major else (R, dims[mode]), dtype=torch.float32, device=T.device)
+    pw = (ctypes.c_void_p * L)(*ptrs)
+    _lib.call("tfx_mttkrp_tc", _vp(Tk), L, cd, int(R), ctypes.cast(pw, ctypes.c_void_p), int(mk), _vp(out), 1 if col_major else 0, _vp(scratch), nb,
+              _vp(err), _st())
+    return out, err

@@ -51,15 +51,19 @@ class _Aligned:
         self.nbytes = int(nbytes)
 
 
-def dgn_mttkrp(provider, dims, R, x0, options, precision, tnorm2, meanabs):
+def dgn_mttkrp(provider, dims, R, x0, options, precision, tnorm2, meanabs, error_fn=None):
     """dGN from the flat start ``x0`` (device, working precision).
 
-    ``provider(Wrm, Mrm, modes)`` writes ``T_(l) KR_l`` for every l in
+    ``provider(W, Wrm, Mrm, modes)`` writes ``T_(l) KR_l`` for every l in
     ``modes`` into the row-major block of ``Mrm`` at offset R*sum(dims[:l]),
-    from the row-major factors ``Wrm`` (same offsets).  ``tnorm2`` = ||T||^2,
-    ``meanabs`` = mean |T| over every entry of the tensor (absent ones
-    included).  Returns ``(best, step_sizes, errors, improv, gradients, stop,
-    matvecs)`` with ``best`` a device vector."""
+    from the factors (flat ``W``, or their row-major copy ``Wrm`` at the same
+    offsets).  ``tnorm2`` = ||T||^2, ``meanabs`` = mean |T| over every entry of
+    the tensor (absent ones included).  ``error_fn(W, out)``, when given,
+    writes ||T - [[W]]||^2 (a device double at address ``out``) instead of the
+    MTTKRP identity -- a dense tensor's direct residual keeps the error's
+    precision where the identity would cancel.  Returns ``(best, step_sizes,
+    errors, improv, gradients, stop, matvecs)`` with ``best`` a device
+    vector."""
     o = options
     lib = _lib.load()
     L = len(dims)
@@ -95,8 +99,11 @@ def dgn_mttkrp(provider, dims, R, x0, options, precision, tnorm2, meanabs):
         _lib.call("tfx_factors_to_rows", dt, L, cd, int(R), _vp(src), _vp(Wrm), st)
 
     def model_error(Wsrc):
+        if error_fn is not None:
+            error_fn(Wsrc, sp + 8 * 8)
+            return
         rows(Wsrc)
-        provider(Wrm, Mrm, [0])
+        provider(Wsrc, Wrm, Mrm, [0])
         _lib.call("tfx_coo_model_error", dt, L, cd, int(R), _vp(Wsrc), _vp(Mrm), float(tnorm2),
                   ctypes.c_void_p(sp + 8 * 8), _vp(errw), int(errw.numel()), st)
 
@@ -116,7 +123,7 @@ def dgn_mttkrp(provider, dims, R, x0, options, precision, tnorm2, meanabs):
     for it in range(maxiter):
         old_error = error
         rows(W)
-        provider(Wrm, Mrm, list(range(1 if m0_valid else 0, L)))
+        provider(W, Wrm, Mrm, list(range(1 if m0_valid else 0, L)))
         _lib.call("tfx_coo_dgn_cg", dt, L, cd, int(R), _vp(W), _vp(Mrm), ctypes.c_double(damp),
                   int(budgets[it]), ctypes.c_double(float(o.cg_tol)), _vp(y), _vp(grad), _vp(jtj),
                   ctypes.c_void_p(sp), ctypes.c_void_p(cgw.ptr), cgw.nbytes, st)
@@ -131,7 +138,7 @@ def dgn_mttkrp(provider, dims, R, x0, options, precision, tnorm2, meanabs):
         matvecs += int(s[0])
         error = float(np.sqrt(max(s[8], 0.0))) / Tsize
         den, ss2, xo2, gmax = float(s[6]), float(s[4]), float(s[5]), float(s[7])
-        m0_valid = True
+        m0_valid = error_fn is None
         if it > 3 and error > o.tol_jump * old_error:
             error = _dogleg(lib, dt, n, x, y, grad, jtj, W, bY, xa, xb, error, damp, Tsize, model_error,
                             scal, dgw, st)
@@ -223,3 +230,56 @@ def _dogleg(lib, dt, n, x, y, grad, jtj, W, bY, xa, xb, error, damp, Tsize, mode
     y.copy_(bY)
     W.copy_(bW)
     return best_error
+
+
+def dense_provider(Td, dims, R):
+    """MTTKRP provider of a dense FP32 tensor on the tensor cores
+    (``tfx_mttkrp_tc``); the last mode reads a copy of the tensor with that
+    mode moved first, made once."""
+    from . import kernels
+    dims = [int(d) for d in dims]
+    L = len(dims)
+    offs = np.concatenate([[0], np.cumsum([R * d for d in dims])])
+    state = {}
+
+    def provide(W, Wrm, Mrm, modes):
+        for l in modes:
+            if l == L - 1 and 'last' not in state:
+                state['last'] = kernels.last_mode_first(Td, dims)
+            blk = Mrm[int(offs[l]):int(offs[l + 1])].view(dims[l], R)
+            _, err = kernels.mttkrp_tc(Td, dims, W, R, l, T_last=state.get('last'), out=blk)
+            state.setdefault('errs', []).append(err)
+    return provide
+
+
+def dense_supported(Td, R, options, precision):
+    """The tensor-core MTTKRP path applies to this full-tensor dGN run."""
+    from . import kernels
+    dims = [int(d) for d in Td.shape]
+    if precision != 'fp32' or Td.dtype != torch.float32 or len(dims) < 3 or R > 64:
+        return False
+    if options.symm or float(options.factors_norm) > 0 or isinstance(options.init_damp, list):
+        return False
+    if not {_inner_of(options, it) for it in range(int(options.maxiter))} <= {'cg', 'cg_static'}:
+        return False
+    return all(kernels.mttkrp_tc_supported(Td, dims, R, l) for l in range(len(dims)))
+
+
+def dgn_dense(Td, x0, R, options):
+    """dGN on a large dense FP32 tensor (the refinement on the full tensor,
+    TensorFox.py:583-604, or a run without compression): gradients from the
+    tensor-core MTTKRP, the error from the direct residual (``tfx_cp_residual``),
+    CG on the Gramians.  Same return values as ``dgn_mttkrp``."""
+    from . import kernels
+    dims = [int(d) for d in Td.shape]
+    nrm = kernels.tensor_norms(Td).cpu().numpy()
+    lib = _lib.load()
+    scratch = torch.empty(int(lib.tfx_cp_residual_scratch_bytes()), dtype=torch.uint8, device=Td.device)
+    cd = _cint(dims)
+    L = len(dims)
+
+    def error_fn(W, out_addr):
+        _lib.call("tfx_cp_residual", _lib.F32, _vp(Td), L, cd, int(R), _vp(W), ctypes.c_void_p(out_addr),
+                  _vp(scratch), ctypes.c_void_p(_dev.stream()))
+    return dgn_mttkrp(dense_provider(Td, dims, R), dims, R, x0, options, 'fp32', float(nrm[0]),
+                      float(nrm[1]) / Td.numel(), error_fn=error_fn)

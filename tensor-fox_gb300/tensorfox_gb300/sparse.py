@@ -167,7 +167,7 @@ def coo_provider(X, R):
     offs = np.concatenate([[0], np.cumsum([R * d for d in dims])])
     cache = {}
 
-    def provide(Wrm, Mrm, modes):
+    def provide(W, Wrm, Mrm, modes):
         key = Wrm.data_ptr()
         if cache.get('key') != key:
             cache['key'] = key

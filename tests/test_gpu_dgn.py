@@ -184,3 +184,59 @@ def test_dgn_large_core_slab_split_gradient_vs_oracle(dims, R):
         o.precision = 'fp32'
         _, _, er2, _, _, _ = tfx.dGN(T.astype(np.float32), [w.copy() for w in init], R, o)
         np.testing.assert_allclose(er2[:6], er0[:6], rtol=1e-3)
+
+
+def test_dense_mttkrp_dgn_vs_oracle():
+    """The MTTKRP-driven dGN on a dense FP32 tensor (tensor-core MTTKRPs, the
+    direct residual, the grid-wide CG) from the same start as the FP64 oracle's
+    dGN: the errors agree within 1e-4 over the first iterations (FP32 against
+    FP64) and the run ends near the oracle's final error."""
+    import torch
+    from tensorfox_gb300 import mttkrp_dgn
+    rng = np.random.default_rng(41)
+    dims, R = (96, 80, 64), 8
+    W = [rng.standard_normal((d, R)) for d in dims]
+    T = orc.cpd2tens(W) + 1e-3 * rng.standard_normal(dims)
+    init = [w + 0.2 * rng.standard_normal(w.shape) for w in W]
+
+    class O:
+        inner_method = 'cg_static'
+        cg_maxiter = 10
+        maxiter = 30
+    _, ss0, er0, _, _, st0 = orc.dGN(T, [w.copy() for w in init], R, orc.make_options(O))
+    Td = torch.from_numpy(T.astype(np.float32)).cuda()
+    x0 = torch.from_numpy(orc.cpd2flat(init)).cuda().float()
+    best, ss1, er1, _, gr1, st1, mv = mttkrp_dgn.dgn_dense(Td, x0, R, tfx.make_options(O))
+    np.testing.assert_allclose(er1[:8], er0[:8], rtol=1e-4)
+    assert abs(min(er1) - min(er0)) <= 1e-2 * min(er0)
+
+
+def test_cpd_refine_fp32_on_tensor_cores_vs_oracle():
+    """cpd(refine=True) on a 256^3 FP32 tensor: the refinement on the full tensor
+    takes the MTTKRP-driven dGN (tensor-core MTTKRPs); its final error is
+    within 1e-2 of the FP64 oracle's refined error and the factors are
+    congruent (> 0.999) to the oracle's and to the planted ones."""
+    import torch
+    from scipy.optimize import linear_sum_assignment
+    rng = np.random.default_rng(43)
+    dims, R = (256, 256, 256), 12
+    W = [rng.standard_normal((d, R)) for d in dims]
+    T = orc.cpd2tens(W)
+    T = T + 1e-2 * np.linalg.norm(T) / np.sqrt(T.size) * rng.standard_normal(dims)
+
+    class O:
+        refine = True
+        maxiter = 60
+    np.random.seed(2)
+    f0, o0 = orc.cpd(T, R, orc.make_options(O))
+    np.random.seed(2)
+    f1, o1 = tfx.cpd(torch.from_numpy(T.astype(np.float32)).cuda(), R, tfx.make_options(O))
+    assert abs(o1.rel_error - o0.rel_error) <= 1e-2 * o0.rel_error
+
+    def cong(A, B):
+        C = np.ones((R, R))
+        for a, b in zip(A, B):
+            C *= np.abs((a / np.linalg.norm(a, axis=0)).T @ (b / np.linalg.norm(b, axis=0)))
+        r, c = linear_sum_assignment(-C)
+        return C[r, c].min()
+    assert cong(f1, f0) > 0.999 and cong(f1, W) > 0.999

@@ -62,3 +62,30 @@ def test_mixed_precision_cpd_c2_like():
     np.random.seed(0)
     _, out_f = tfx.cpd(T, R, o)
     assert abs(out_m.rel_error - out_f.rel_error) <= 1e-2 * out_f.rel_error
+
+
+@pytest.mark.parametrize("dims,R", [((64, 48, 40), 10), ((300, 128, 8), 64), ((130, 70, 36), 33),
+                                    ((30, 20, 16, 12), 7), ((512, 96, 64), 50), ((9, 260, 300), 5)])
+def test_tc_mttkrp_all_modes_vs_fp64(dims, R):
+    """The tcgen05 MTTKRP (TMA-fed tensor tiles, 3xTF32, FP32 accumulation) of
+    every mode against the FP64 oracle's T_(l) KR_l: within 1e-5 relative
+    (norm-wise and entry-wise against the largest entry); the last mode reads
+    the copy with that mode moved first."""
+    from tensorfox_gb300 import kernels
+    rng = np.random.default_rng(14)
+    T = rng.standard_normal(dims).astype(np.float32)
+    W = [rng.standard_normal((d, R)).astype(np.float32) for d in dims]
+    Td = torch.from_numpy(T).cuda()
+    flat = torch.from_numpy(orc.cpd2flat([w.astype(np.float64) for w in W])).cuda().float()
+    Tl = [orc.unfold(T.astype(np.float64), l + 1) for l in range(len(dims))]
+    W64 = [w.astype(np.float64) for w in W]
+    for l in range(len(dims)):
+        assert kernels.mttkrp_tc_supported(Td, list(dims), R, l)
+        got, err = kernels.mttkrp_tc(Td, list(dims), flat, R, l)
+        assert int(err.item()) == 0
+        got = got.double().cpu().numpy()
+        ref = orc.mttkrp(Tl, W64, l)
+        assert np.linalg.norm(got - ref) <= 1e-5 * np.linalg.norm(ref)
+        assert np.abs(got - ref).max() <= 1e-5 * np.abs(ref).max()
+        gc, _ = kernels.mttkrp_tc(Td, list(dims), flat, R, l, col_major=True)
+        np.testing.assert_array_equal(gc.cpu().numpy().T, got.astype(np.float32))
