@@ -298,6 +298,7 @@ def run_ours(args):
     c1_leg = run_c1(args) if not args.no_batched else None
     autograd_leg = run_autograd(args) if not args.no_batched else None
     als_leg = run_als(Td, R, args) if not args.no_batched else None
+    refine_leg = run_refine(Td, R, args) if not args.no_batched else None
     inner_leg = run_inner(args) if not args.no_batched else None
     clk.__exit__(None, None, None)
     clk_summary = clk.summary()
@@ -359,6 +360,8 @@ def run_ours(args):
         line["als"] = als_leg
     if inner_leg is not None:
         line["dgn_inner_methods"] = inner_leg
+    if refine_leg is not None:
+        line["refine"] = refine_leg
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:
@@ -447,6 +450,14 @@ def kernel_rooflines(Td, R, opts, t_step):
     out.append({"kernel": "k_residual_tc (tcgen05 3xTF32 ||T - [[W]]||^2, 512^3, rank 50)", "bound": "hbm",
                 "achieved": N * 4 / t_r / 1e9, "peak": hbm, "unit": "GB/s", "frac": N * 4 / t_r / 1e9 / hbm,
                 "traffic": None, "ms": t_r * 1e3, "share": t_r / t_step})
+    # tensor-core MTTKRP of mode 0 on the full tensor (the refinement's gradient)
+    Wf32 = Wf.float().contiguous()
+    t_m = _time_events(lambda: kernels.mttkrp_tc(Td, list(DIMS), Wf32, R, 0), 10)
+    by_m = N * 4 + sum(DIMS) * R * 4
+    out.append({"kernel": "k_mttkrp_tc (tcgen05 3xTF32 MTTKRP, TMA-fed, mode 0 of 512^3, rank 50)", "bound": "hbm",
+                "achieved": by_m / t_m / 1e9, "peak": hbm, "unit": "GB/s", "frac": by_m / t_m / 1e9 / hbm,
+                "traffic": None, "ms": t_m * 1e3, "share": 0.0,
+                "note": "not in the headline step (compressed path); three per iteration of the refinement"})
     # eigen-step of one 512-row mode (Krylov block, Rayleigh-Ritz, Jacobi)
     G = kernels.mode_gram_tc(Td, list(DIMS), 0)
     om = np.random.default_rng(0).standard_normal((512, 60))
@@ -607,6 +618,28 @@ def run_als(Td, R, args):
     t = a.elapsed_time(b) / 1e3 / reps
     return {"workload": "as the headline, method='als'", "value": t, "unit": "s", "rel_error": float(out.rel_error),
             "num_steps": int(out.num_steps), "stop": [int(s) for s in out.stop]}
+
+
+def run_refine(Td, R, args):
+    """The headline workload with refine=True: after the compressed solve, dGN
+    runs on the full 512^3 tensor with tensor-core MTTKRP gradients, the
+    direct residual and the grid-wide CG (TensorFox.py:583-604)."""
+    import torch
+    import tensorfox_gb300 as tfx
+    o = tfx.make_options(None)
+    o.precision = "mixed"
+    o.refine = True
+    np.random.seed(0)
+    tfx.cpd(Td, R, o)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    np.random.seed(0)
+    _, out = tfx.cpd(Td, R, o)
+    torch.cuda.synchronize()
+    t = time.perf_counter() - t0
+    return {"workload": "as the headline, refine=True (full-tensor dGN on the tensor-core MTTKRP)", "value": t,
+            "unit": "s", "rel_error": float(out.rel_error), "num_steps": int(out.num_steps),
+            "refine_steps": int(len(out.errors[1])), "stop": [int(v) for v in out.stop]}
 
 
 def run_inner(args, seed=102):

@@ -243,6 +243,17 @@ int tfx_coo_sort_mode(int dtype, const int* idx32, const void* vals, long long n
  * (GaussNewton.py:401-427 on sparse2dense, Conversion.py:144-164). */
 int tfx_coo_mttkrp(int dtype, const int* sidx, const void* svals, long long nnz, const long long* rowptr, int L,
                    const int* dims, int R, int mode, const void* const* Wrow_dev, void* out, void* stream);
+/* The same COO MTTKRP from BF16 factor rows with per-column scaling (FP32
+ * values and sums): tfx_factors_bf16 writes row-major BF16 copies of the flat
+ * FP32 factors, column r of mode m divided by scale[m*R + r], a power of two
+ * near the column's largest magnitude; tfx_coo_mttkrp_bf16 gathers them
+ * (Wbf_dev: device array of L pointers) and multiplies the result by the other
+ * modes' scales; out (d_mode x R row-major, FP32).  R in {8, 16, 32, 64}.  No
+ * reference counterpart (the reference computes in FP64). */
+int tfx_factors_bf16(int L, const int* dims, int R, const float* W, void* Wbf, float* scale, void* stream);
+int tfx_coo_mttkrp_bf16(const int* sidx, const float* svals, long long nnz, const long long* rowptr, int L,
+                        const int* dims, int R, int mode, const void* const* Wbf_dev, const float* scale, float* out,
+                        void* stream);
 /* Critical.py:25-53 sparse_fastnorm^2: *out = sum over stored entries of
  * (value - model)^2. */
 size_t tfx_sparse_residual_scratch_bytes(void);

@@ -193,34 +193,43 @@ __global__ void __launch_bounds__(NT, 1)
         l4[e] = lo;
       }
     }
-    // B: 64 x 32, B[r][q] = before_p[r] * after_{q0+q}[r]
+    // B: 64 x 32, B[r][q] = before_p[r] * after_{q0+q}[r].  A thread takes one
+    // q (its lane) and eight ranks r = warp + 8 u: the indices of p and q are
+    // decomposed once per chunk (32-bit: P, Q < 2^31), then one factor load per
+    // other mode and rank.
     {
       const long long cc = cbeg + c;
-      const long long p = cc / qchunks;
-      const long long q0 = (cc - p * qchunks) * BK;
-      for (int e = tid; e < NR * BK; e += NT) {
-        const int r = e >> 5, qq = e & 31;
-        const long long q = q0 + qq;
+      const unsigned p = (unsigned)(cc / qchunks);
+      const unsigned q = (unsigned)(cc - (long long)p * qchunks) * BK + (unsigned)lane;
+      const bool qok = q < (unsigned)sh.Q;
+      int ib[TFX_MAX_ORDER], ia[TFX_MAX_ORDER];
+      {
+        unsigned rem = p;
+        for (int m = l - 1; m >= 0; --m) {
+          const unsigned dm = (unsigned)sh.dims[m];
+          const unsigned qm = rem / dm;
+          ib[m] = (int)(rem - qm * dm);
+          rem = qm;
+        }
+        rem = qok ? q : 0u;
+        for (int m = sh.L - 1; m > l; --m) {
+          const unsigned dm = (unsigned)sh.dims[m];
+          const unsigned qm = rem / dm;
+          ia[m] = (int)(rem - qm * dm);
+          rem = qm;
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < NR / 8; ++u) {
+        const int r = warp + 8 * u;
         float v = 0.f;
-        if (r < R && q < sh.Q) {
+        if (r < R && qok) {
           v = 1.f;
-          long long rem = p;
-          for (int m = l - 1; m >= 0; --m) {
-            const int dm = sh.dims[m];
-            const long long im = rem % dm;
-            rem /= dm;
-            v *= sh.W[m][(long long)r * dm + im];
-          }
-          rem = q;
-          for (int m = sh.L - 1; m > l; --m) {
-            const int dm = sh.dims[m];
-            const long long im = rem % dm;
-            rem /= dm;
-            v *= sh.W[m][(long long)r * dm + im];
-          }
+          for (int m = 0; m < l; ++m) v *= __ldg(sh.W[m] + (long long)r * sh.dims[m] + ib[m]);
+          for (int m = l + 1; m < sh.L; ++m) v *= __ldg(sh.W[m] + (long long)r * sh.dims[m] + ia[m]);
         }
         const float h = hi13(v);
-        const uint32_t o = sw_off(r, qq);
+        const uint32_t o = sw_off(r, lane);
         *(float*)(S.bhi[s] + o) = h;
         *(float*)(S.blo[s] + o) = v - h;
       }

@@ -19,6 +19,8 @@
 // so that the gather of one factor row per entry touches R*4 contiguous bytes.
 #include <math.h>
 
+#include <cuda_bf16.h>
+
 #include <algorithm>
 
 #include "tfx_capi_internal.h"
@@ -208,6 +210,97 @@ __global__ void __launch_bounds__(256) k_coo_mttkrp_f4(const int* __restrict__ s
       *reinterpret_cast<float4*>(out + (size_t)row * R + rq) = r4;
     }
   }
+}
+
+// BF16 COO MTTKRP with per-column scaling (R in {8, 16, 32, 64}): the
+// factors are gathered as BF16 rows (half the bytes of FP32), each column r of
+// mode m stored as W_m[:, r] / s_{m,r} with s_{m,r} a power of two near the
+// column's largest magnitude; products and sums in FP32 (float-float), the
+// result scaled back by prod_{m != mode} s_{m,r}.  A lane holds eight columns
+// (one 16-byte read per factor row), R / 8 lanes per entry, 256 / R entries
+// in flight per warp.  Rows of the output as in the FP32 kernel.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_coo_mttkrp_bf16(const int* __restrict__ sidx, const float* __restrict__ svals,
+                                                         long long nnz, const long long* __restrict__ rowptr,
+                                                         CooShape sh, int mode,
+                                                         const __nv_bfloat16* const* __restrict__ Wbf,
+                                                         const float* __restrict__ scale, float* __restrict__ out) {
+  const int R = sh.R;
+  const int lpe = R >> 3;              // lanes per entry (1, 2, 4 or 8)
+  const int lane = threadIdx.x & 31, q = lane % lpe, slot = lane / lpe, nslot = 32 / lpe;
+  const int warps = (gridDim.x * blockDim.x) >> 5;
+  const int d = sh.dims[mode];
+  const int c0 = 8 * q;                // this lane's eight columns
+  for (int row = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; row < d; row += warps) {
+    const long long b = rowptr[row], e = rowptr[row + 1];
+    Acc<float> acc[8];
+    for (long long k = b + slot; k < e; k += nslot) {
+      const float v = svals[k];
+      float p[8];
+#pragma unroll
+      for (int j = 0; j < 8; ++j) p[j] = v;
+      for (int m = 0; m < sh.L; ++m) {
+        if (m == mode) continue;
+        const uint4 raw = __ldg(reinterpret_cast<const uint4*>(Wbf[m] + (size_t)sidx[(size_t)m * nnz + k] * R + c0));
+        const uint32_t w4[4] = {raw.x, raw.y, raw.z, raw.w};
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          p[2 * j] *= __uint_as_float(w4[j] << 16);
+          p[2 * j + 1] *= __uint_as_float(w4[j] & 0xffff0000u);
+        }
+      }
+#pragma unroll
+      for (int j = 0; j < 8; ++j) acc[j].add(p[j]);
+    }
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      for (int o = lpe; o < 32; o <<= 1) {
+        const float oh = __shfl_xor_sync(0xffffffffu, acc[j].hi, o);
+        const float ol = __shfl_xor_sync(0xffffffffu, acc[j].lo, o);
+        acc[j].add2(oh, ol);
+      }
+    }
+    if (slot == 0) {
+#pragma unroll
+      for (int j = 0; j < 8; ++j) {
+        float sc = 1.f;
+        for (int m = 0; m < sh.L; ++m)
+          if (m != mode) sc *= scale[m * R + c0 + j];
+        out[(size_t)row * R + c0 + j] = (acc[j].hi + acc[j].lo) * sc;
+      }
+    }
+  }
+}
+
+// per-column power-of-two scales and the BF16 row-major copies of the flat
+// (column-major) factors: one CTA per column (mode l, column r)
+__global__ void __launch_bounds__(256) k_factors_bf16(CooShape sh, const float* __restrict__ W,
+                                                      __nv_bfloat16* __restrict__ Wbf, float* __restrict__ scale) {
+  __shared__ float smax[8];
+  const int L = sh.L, R = sh.R;
+  const int col = blockIdx.x;  // l * R + r
+  const int l = col / R, r = col - l * R;
+  long long off = 0;
+  for (int m = 0; m < l; ++m) off += (long long)sh.dims[m] * R;
+  const int d = sh.dims[l];
+  const float* w = W + off + (long long)r * d;
+  float mx = 0.f;
+  for (int i = threadIdx.x; i < d; i += blockDim.x) mx = fmaxf(mx, fabsf(w[i]));
+  for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  if ((threadIdx.x & 31) == 0) smax[threadIdx.x >> 5] = mx;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    float v = threadIdx.x < 8 ? smax[threadIdx.x] : 0.f;
+    for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+    if (threadIdx.x == 0) smax[0] = v;
+  }
+  __syncthreads();
+  // a power of two: dividing by it is exact, so the scaling adds no rounding
+  const float sc = smax[0] > 0.f ? exp2f(ceilf(log2f(smax[0]))) : 1.f;
+  if (threadIdx.x == 0) scale[l * R + r] = sc;
+  const float inv = 1.f / sc;
+  for (int i = threadIdx.x; i < d; i += blockDim.x) Wbf[off + (long long)i * R + r] = __float2bfloat16_rn(w[i] * inv);
+  (void)L;
 }
 
 // FP32 residual with R % 4 == 0: 16-byte gathers of the factor rows (when
@@ -699,4 +792,26 @@ extern "C" int tfx_sparse_ttmc(int dtype, const int* idx32, const void* vals, lo
   else
     k_sum_split<double><<<grid_for(tot), 256, 0, st>>>((const double*)scratch, tot, ks, (double*)S);
   return launched("ttmc_sum");
+}
+
+extern "C" int tfx_factors_bf16(int L, const int* dims, int R, const float* W, void* Wbf, float* scale, void* stream) {
+  CooShape sh;
+  if (fill_shape(sh, L, dims, R) || !W || !Wbf || !scale) return tfx_set_error(TFX_STATUS_ERR_ARG, "factors_bf16 args");
+  k_factors_bf16<<<L * R, 256, 0, (cudaStream_t)stream>>>(sh, W, (__nv_bfloat16*)Wbf, scale);
+  return launched("factors_bf16");
+}
+
+extern "C" int tfx_coo_mttkrp_bf16(const int* sidx, const float* svals, long long nnz, const long long* rowptr, int L,
+                                   const int* dims, int R, int mode, const void* const* Wbf_dev, const float* scale,
+                                   float* out, void* stream) {
+  CooShape sh;
+  if (fill_shape(sh, L, dims, R) || mode < 0 || mode >= L || !sidx || !svals || !rowptr || !Wbf_dev || !scale || !out)
+    return tfx_set_error(TFX_STATUS_ERR_ARG, "coo_mttkrp_bf16 args");
+  if (R != 8 && R != 16 && R != 32 && R != 64)
+    return tfx_set_error(TFX_STATUS_ERR_UNSUPPORTED, "coo_mttkrp_bf16: R must be 8, 16, 32 or 64");
+  const int d = dims[mode];
+  const int blocks = (int)std::max<long long>(1, std::min<long long>(((long long)d * 32 + 255) / 256, 16LL * sms()));
+  k_coo_mttkrp_bf16<<<blocks, 256, 0, (cudaStream_t)stream>>>(sidx, svals, nnz, rowptr, sh, mode,
+                                                               (const __nv_bfloat16* const*)Wbf_dev, scale, out);
+  return launched("coo_mttkrp_bf16");
 }

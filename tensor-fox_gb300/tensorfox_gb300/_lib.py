@@ -112,6 +112,8 @@ _EXTRA_SIGNATURES = {
     "tfx_step_sums": [_I, _LL, _P, _P, _P, _D, _P, _P, _P],
     "tfx_step_revert": [_I, _LL, _P, _P, _P, _P],
     "tfx_mttkrp_tc": [_P, _I, POINTER(c_int), _I, _P, _I, _P, _I, _P, _SZ, _P, _P],
+    "tfx_factors_bf16": [_I, POINTER(c_int), _I, _P, _P, _P, _P],
+    "tfx_coo_mttkrp_bf16": [_P, _P, _LL, _P, _I, POINTER(c_int), _I, _I, _P, _P, _P, _P],
     "tfx_gemm": [_I, _P, _P, _P, _LL, _LL, _LL, _LL, POINTER(c_longlong), _D, _D, _P],
     "tfx_orthonormalize": [_I, _P, _I, _I, _P],
     "tfx_ttm": [_I, _P, _LL, _I, _LL, _P, _I, _P, _P],

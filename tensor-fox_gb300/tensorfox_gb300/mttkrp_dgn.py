@@ -51,7 +51,7 @@ class _Aligned:
         self.nbytes = int(nbytes)
 
 
-def dgn_mttkrp(provider, dims, R, x0, options, precision, tnorm2, meanabs, error_fn=None):
+def dgn_mttkrp(provider, dims, R, x0, options, precision, tnorm2, meanabs, error_fn=None, ladder=False):
     """dGN from the flat start ``x0`` (device, working precision).
 
     ``provider(W, Wrm, Mrm, modes)`` writes ``T_(l) KR_l`` for every l in
@@ -61,9 +61,14 @@ def dgn_mttkrp(provider, dims, R, x0, options, precision, tnorm2, meanabs, error
     the tensor (absent ones included).  ``error_fn(W, out)``, when given,
     writes ||T - [[W]]||^2 (a device double at address ``out``) instead of the
     MTTKRP identity -- a dense tensor's direct residual keeps the error's
-    precision where the identity would cancel.  Returns ``(best, step_sizes,
-    errors, improv, gradients, stop, matvecs)`` with ``best`` a device
-    vector."""
+    precision where the identity would cancel.  ``ladder``: start with the
+    provider's low-precision MTTKRPs (``provider(..., low=True)``: BF16 factor
+    rows with per-column scales for a COO tensor) and switch to the working
+    precision for good at the first iteration that lowers the error by less
+    than 1% -- far from the solution the cheap gradient steers as well, near
+    it every digit counts.  Returns ``(best, step_sizes, errors, improv,
+    gradients, stop, matvecs)`` with ``best`` a device vector; the number of
+    low-precision iterations is ``dgn_mttkrp.low_iterations``."""
     o = options
     lib = _lib.load()
     L = len(dims)
@@ -98,12 +103,15 @@ def dgn_mttkrp(provider, dims, R, x0, options, precision, tnorm2, meanabs, error
     def rows(src):
         _lib.call("tfx_factors_to_rows", dt, L, cd, int(R), _vp(src), _vp(Wrm), st)
 
+    low = bool(ladder)
+    n_low = 0
+
     def model_error(Wsrc):
         if error_fn is not None:
             error_fn(Wsrc, sp + 8 * 8)
             return
         rows(Wsrc)
-        provider(Wsrc, Wrm, Mrm, [0])
+        provider(Wsrc, Wrm, Mrm, [0], low=low)
         _lib.call("tfx_coo_model_error", dt, L, cd, int(R), _vp(Wsrc), _vp(Mrm), float(tnorm2),
                   ctypes.c_void_p(sp + 8 * 8), _vp(errw), int(errw.numel()), st)
 
@@ -123,7 +131,7 @@ def dgn_mttkrp(provider, dims, R, x0, options, precision, tnorm2, meanabs, error
     for it in range(maxiter):
         old_error = error
         rows(W)
-        provider(W, Wrm, Mrm, list(range(1 if m0_valid else 0, L)))
+        provider(W, Wrm, Mrm, list(range(1 if m0_valid else 0, L)), low=low)
         _lib.call("tfx_coo_dgn_cg", dt, L, cd, int(R), _vp(W), _vp(Mrm), ctypes.c_double(damp),
                   int(budgets[it]), ctypes.c_double(float(o.cg_tol)), _vp(y), _vp(grad), _vp(jtj),
                   ctypes.c_void_p(sp), ctypes.c_void_p(cgw.ptr), cgw.nbytes, st)
@@ -147,6 +155,11 @@ def dgn_mttkrp(provider, dims, R, x0, options, precision, tnorm2, meanabs, error
                       ctypes.c_void_p(sp + 12 * 8), _vp(dgw), st)
             s = scal.cpu().numpy()
             den, ss2, xo2, gmax = float(s[12]), float(s[13]), float(s[14]), float(s[15])
+        if low:
+            n_low += 1
+            if old_error - error < 1e-2 * old_error:
+                low = False
+                m0_valid = False     # the kept mode-0 MTTKRP is a low-precision one
         gain = _gain_ratio(damp, old_error, error, Tsize, den)
         damp = _update_damp(damp, init_damp, gain, it)
         if error < best_error:
@@ -163,6 +176,7 @@ def dgn_mttkrp(provider, dims, R, x0, options, precision, tnorm2, meanabs, error
             break
     k = it + 1
     advance_rng(o, k)
+    dgn_mttkrp.low_iterations = n_low
     return best, step_sizes[:k].copy(), errors[:k].copy(), improv[:k].copy(), gradients[:k].copy(), stop, matvecs
 
 
@@ -242,7 +256,7 @@ def dense_provider(Td, dims, R):
     offs = np.concatenate([[0], np.cumsum([R * d for d in dims])])
     state = {}
 
-    def provide(W, Wrm, Mrm, modes):
+    def provide(W, Wrm, Mrm, modes, low=False):
         for l in modes:
             if l == L - 1 and 'last' not in state:
                 state['last'] = kernels.last_mode_first(Td, dims)

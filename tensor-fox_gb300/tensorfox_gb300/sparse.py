@@ -167,7 +167,22 @@ def coo_provider(X, R):
     offs = np.concatenate([[0], np.cumsum([R * d for d in dims])])
     cache = {}
 
-    def provide(W, Wrm, Mrm, modes):
+    def provide(W, Wrm, Mrm, modes, low=False):
+        if low and modes:
+            # BF16 factor rows, per-column power-of-two scales, FP32 sums
+            if 'bf' not in cache:
+                cache['bf'] = torch.empty(W.numel(), dtype=torch.bfloat16, device=W.device)
+                cache['scale'] = torch.empty(X.L * R, dtype=torch.float32, device=W.device)
+                cache['bptrs'] = torch.tensor([cache['bf'].data_ptr() + int(offs[l]) * 2 for l in range(X.L)],
+                                              dtype=torch.int64, device=W.device)
+            _lib.call("tfx_factors_bf16", X.L, _cint(dims), int(R), _vp(W), _vp(cache['bf']), _vp(cache['scale']),
+                      _st())
+            for l in modes:
+                rowptr, sidx, svals = X.sort_mode(l)
+                _lib.call("tfx_coo_mttkrp_bf16", _vp(sidx), _vp(svals), X.nnz, _vp(rowptr), X.L, _cint(dims),
+                          int(R), int(l), _vp(cache['bptrs']), _vp(cache['scale']),
+                          ctypes.c_void_p(Mrm.data_ptr() + int(offs[l]) * es), _st())
+            return
         key = Wrm.data_ptr()
         if cache.get('key') != key:
             cache['key'] = key
@@ -199,7 +214,9 @@ def tricpd_sparse_direct(X, data, R, o, prec, ordering, sdims, Tsize):
     x0 = torch.from_numpy(_dev.flat_factors(init)).to(device=X.vals.device, dtype=dt)
     nrm = kernels.tensor_norms(X.vals).cpu().numpy()
     meanabs = float(nrm[1]) / float(np.prod(np.array(dims, dtype=np.float64)))
-    return dgn_mttkrp(coo_provider(X, R), dims, R, x0, o, prec, float(nrm[0]), meanabs)
+    # precision 'mixed': BF16 gathers while the error falls fast, then FP32
+    ladder = o.precision == 'mixed' and dt == torch.float32 and R in (8, 16, 32, 64)
+    return dgn_mttkrp(coo_provider(X, R), dims, R, x0, o, prec, float(nrm[0]), meanabs, ladder=ladder)
 
 
 def tricpd_sparse(T, R, options):

@@ -252,3 +252,63 @@ def test_direct_coo_cpd_equals_dense_uncompressed_oracle():
         model *= f[l][idxs[:, l]]
     want = np.linalg.norm(data - model.sum(1)) / np.linalg.norm(data)
     assert abs(out.rel_error - want) <= 1e-10 * want
+
+
+@pytest.mark.parametrize("R", [8, 16, 32])
+def test_coo_mttkrp_bf16_per_column_scaling_vs_fp64(R):
+    """BF16 factor rows with per-column power-of-two scales (FP32 values and
+    sums) against the FP64 oracle: about 3e-3 relative, within 1e-2 for every
+    column even when the columns' magnitudes span twelve decades (the scales
+    keep each column's own relative accuracy)."""
+    import ctypes
+    from tensorfox_gb300 import _lib, _dev
+    dims, nnz = (40, 30, 20), 4000
+    data, idxs, W = coo(dims, R, nnz, 9)
+    colscale = 10.0 ** np.linspace(-6, 6, R)
+    W = [w * colscale[None, :] if l == 1 else w for l, w in enumerate(W)]
+    X = sparse.DeviceCOO(data, idxs, dims, torch.float32)
+    flat = torch.from_numpy(orc.cpd2flat(W)).cuda().float()
+    bf = torch.empty(flat.numel(), dtype=torch.bfloat16, device="cuda")
+    sc = torch.empty(3 * R, dtype=torch.float32, device="cuda")
+    cd = (ctypes.c_int * 3)(*dims)
+    _lib.call("tfx_factors_bf16", 3, cd, R, ctypes.c_void_p(flat.data_ptr()), ctypes.c_void_p(bf.data_ptr()),
+              ctypes.c_void_p(sc.data_ptr()), ctypes.c_void_p(_dev.stream()))
+    offs = np.concatenate([[0], np.cumsum([R * d for d in dims])])
+    ptrs = torch.tensor([bf.data_ptr() + int(offs[l]) * 2 for l in range(3)], dtype=torch.int64, device="cuda")
+    T = dense_of(data, idxs, dims)
+    Tl = [orc.unfold(T, l + 1) for l in range(3)]
+    for l in range(3):
+        rowptr, sidx, svals = X.sort_mode(l)
+        out = torch.empty((dims[l], R), dtype=torch.float32, device="cuda")
+        _lib.call("tfx_coo_mttkrp_bf16", ctypes.c_void_p(sidx.data_ptr()), ctypes.c_void_p(svals.data_ptr()), X.nnz,
+                  ctypes.c_void_p(rowptr.data_ptr()), 3, cd, R, l, ctypes.c_void_p(ptrs.data_ptr()),
+                  ctypes.c_void_p(sc.data_ptr()), ctypes.c_void_p(out.data_ptr()), ctypes.c_void_p(_dev.stream()))
+        got = out.double().cpu().numpy()
+        ref = orc.mttkrp(Tl, W, l)
+        colerr = np.linalg.norm(got - ref, axis=0) / np.linalg.norm(ref, axis=0)
+        assert colerr.max() <= 1e-2, colerr
+
+
+def test_direct_coo_precision_ladder_vs_fp64_oracle():
+    """precision='mixed' on the direct COO solver: BF16 gathers while the error
+    falls by more than 1% an iteration, FP32 after; it ends at the FP64
+    oracle's dGN error (same start, sparse2dense, FP64) within 1e-3."""
+    from tensorfox_gb300 import mttkrp_dgn
+    dims, R = (40, 35, 30), 8
+    data, idxs, _ = coo(dims, R, 8000, 12)
+    T = dense_of(data, idxs, dims)
+    rng = np.random.default_rng(13)
+    init = [rng.standard_normal((d, R)) for d in dims]
+
+    class O:
+        inner_method = 'cg_static'
+        cg_maxiter = 10
+        maxiter = 60
+    _, _, er0, _, _, _ = orc.dGN(T, [w.copy() for w in init], R, orc.make_options(O))
+    X = sparse.DeviceCOO(data, idxs, dims, torch.float32)
+    x0 = torch.from_numpy(orc.cpd2flat(init)).cuda().float()
+    _, _, er1, _, _, _, _ = mttkrp_dgn.dgn_mttkrp(sparse.coo_provider(X, R), list(dims), R, x0,
+                                                  tfx.make_options(O), 'fp32', float(np.sum(T * T)),
+                                                  float(np.mean(np.abs(T))), ladder=True)
+    assert mttkrp_dgn.dgn_mttkrp.low_iterations >= 1
+    assert abs(min(er1) - min(er0)) <= 1e-3 * min(er0)
