@@ -14,16 +14,17 @@
 //
 // A CTA owns 256 rows of M (two 128-row tiles, two TMEM accumulators of 64
 // columns) and a contiguous range of (p, 32-wide q chunk) pairs (split-K):
-//   * TMA brings the two 128 x 32 tensor tiles of a chunk (3-D map over
-//     (q, d, p), SWIZZLE_128B) into a two-stage ring;
-//   * the CTA's threads split every tile value x into x_hi = x with its 13 low
+//   * warp 0 (producer) brings the two 128 x 32 tensor tiles of a chunk by TMA
+//     (3-D map over (q, d, p), SWIZZLE_128B) into a two-stage ring, a stage
+//     being refilled as soon as the products that read it have completed;
+//   * warps 1-7 split every tile value x into x_hi = x with its 13 low
 //     mantissa bits cleared (exact in TF32) and x_lo = x - x_hi, and form the
 //     chunk's B operand (64 x 32, K-major, SWIZZLE_128B) the same way from the
 //     factor rows;
-//   * one thread issues tcgen05.mma kind::tf32 (M = 128, N = 64, K = 8):
+//   * one of them issues tcgen05.mma kind::tf32 (M = 128, N = 64, K = 8):
 //     A_hi B_hi + A_hi B_lo + A_lo B_hi per tile, FP32 accumulation in TMEM,
 //     so the product keeps FP32 accuracy (3xTF32), and commits to the stage's
-//     mbarrier; the stage is refilled once that commit lands.
+//     mbarrier, while the others convert the next chunk.
 // The accumulators are written as per-CTA partials and summed in a fixed
 // order (compensated FP32) by a second kernel.  Every wait is bounded; a wait
 // that runs out sets *err, the CTA drains its copies (bounded) and frees TMEM.
@@ -111,6 +112,8 @@ struct Smem {
   alignas(8) uint64_t done[STAGES];
   uint32_t tmem;
   int abort;
+  int issued;    // chunks whose copies the producer issued
+  int consumed;  // chunks whose products were issued
 };
 
 // The factors in the kernel's mode order: mode m of the (possibly permuted)
@@ -140,6 +143,8 @@ __global__ void __launch_bounds__(NT, 1)
       mbar_init(&S.done[s], 1);
     }
     S.abort = 0;
+    S.issued = 0;
+    S.consumed = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == 0) {
@@ -151,7 +156,7 @@ __global__ void __launch_bounds__(NT, 1)
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = S.tmem;
-  auto issue = [&](int c) {  // thread 0: TMA of chunk cbeg + c into stage c % 2
+  auto issue = [&](int c) {  // the producer: TMA of chunk cbeg + c into stage c % 2
     const long long cc = cbeg + c;
     const int p = (int)(cc / qchunks);
     const int q0 = (int)(cc - (long long)p * qchunks) * BK;
@@ -159,130 +164,131 @@ __global__ void __launch_bounds__(NT, 1)
     expect_tx(&S.full[s], NTILE * TILE_BYTES);
     for (int t = 0; t < NTILE; ++t) tma_3d(S.a[s][t], &tmap, &S.full[s], q0, row0 + t * BM, p);
   };
-  int issued = 0;
-  if (tid == 0) {
-    if (n > 0) issue(0);
-    if (n > 1) issue(1);
-    issued = n < 2 ? n : 2;
-  }
-  int consumed = 0;  // chunks whose copies were waited for (thread 0's view)
-  for (int c = 0; c < n; ++c) {
-    const int s = c & 1;
-    const uint32_t par = (uint32_t)(c >> 1) & 1u;
-    if (!wait_bar(&S.full[s], par)) {
-      if (lane == 0) {
-        atomicExch(err, 1);
-        S.abort = 1;
-      }
-    }
-    __syncthreads();
-    if (*(volatile int*)&S.abort) break;
-    if (tid == 0) consumed = c + 1;
-    // A: hi in place, lo beside it (element-wise: the layout is the same)
-    {
-      float4* a4 = reinterpret_cast<float4*>(&S.a[s][0][0]);
-      float4* l4 = reinterpret_cast<float4*>(&S.alo[s][0][0]);
-      for (int e = tid; e < NTILE * BM * BK / 4; e += NT) {
-        const float4 v = a4[e];
-        float4 h, lo;
-        h.x = hi13(v.x); lo.x = v.x - h.x;
-        h.y = hi13(v.y); lo.y = v.y - h.y;
-        h.z = hi13(v.z); lo.z = v.z - h.z;
-        h.w = hi13(v.w); lo.w = v.w - h.w;
-        a4[e] = h;
-        l4[e] = lo;
-      }
-    }
-    // B: 64 x 32, B[r][q] = before_p[r] * after_{q0+q}[r].  A thread takes one
-    // q (its lane) and eight ranks r = warp + 8 u: the indices of p and q are
-    // decomposed once per chunk (32-bit: P, Q < 2^31), then one factor load per
-    // other mode and rank.
-    {
-      const long long cc = cbeg + c;
-      const unsigned p = (unsigned)(cc / qchunks);
-      const unsigned q = (unsigned)(cc - (long long)p * qchunks) * BK + (unsigned)lane;
-      const bool qok = q < (unsigned)sh.Q;
-      int ib[TFX_MAX_ORDER], ia[TFX_MAX_ORDER];
-      {
-        unsigned rem = p;
-        for (int m = l - 1; m >= 0; --m) {
-          const unsigned dm = (unsigned)sh.dims[m];
-          const unsigned qm = rem / dm;
-          ib[m] = (int)(rem - qm * dm);
-          rem = qm;
-        }
-        rem = qok ? q : 0u;
-        for (int m = sh.L - 1; m > l; --m) {
-          const unsigned dm = (unsigned)sh.dims[m];
-          const unsigned qm = rem / dm;
-          ia[m] = (int)(rem - qm * dm);
-          rem = qm;
-        }
-      }
-#pragma unroll
-      for (int u = 0; u < NR / 8; ++u) {
-        const int r = warp + 8 * u;
-        float v = 0.f;
-        if (r < R && qok) {
-          v = 1.f;
-          for (int m = 0; m < l; ++m) v *= __ldg(sh.W[m] + (long long)r * sh.dims[m] + ib[m]);
-          for (int m = l + 1; m < sh.L; ++m) v *= __ldg(sh.W[m] + (long long)r * sh.dims[m] + ia[m]);
-        }
-        const float h = hi13(v);
-        const uint32_t o = sw_off(r, lane);
-        *(float*)(S.bhi[s] + o) = h;
-        *(float*)(S.blo[s] + o) = v - h;
-      }
-    }
-    // generic-proxy writes -> visible to the tensor core's async proxy
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-    __syncthreads();
-    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-    if (tid == 0) {
-      for (int t = 0; t < NTILE; ++t) {
-        const uint64_t ah = desc(S.a[s][t]), al = desc(S.alo[s][t]);
-        const uint64_t bh = desc(S.bhi[s]), bl = desc(S.blo[s]);
-        for (int pass = 0; pass < 3; ++pass) {
-          const uint64_t da = pass == 2 ? al : ah;
-          const uint64_t db = pass == 1 ? bl : bh;
-#pragma unroll
-          for (int kk = 0; kk < BK / 8; ++kk)
-            mma(tmem + (uint32_t)(t * NR), da + (uint64_t)(kk * 2), db + (uint64_t)(kk * 2),
-                (c > 0 || pass > 0 || kk > 0) ? 1u : 0u);
-        }
-      }
-      commit(&S.done[s]);
-      // the stage is free once these products have read it
-      if (c + 2 < n) {
-        if (!wait_bar(&S.done[s], par)) {
-          atomicExch(err, 2);
+  constexpr int NC = NT - 32;  // converter threads (warps 1..7)
+  if (warp == 0) {
+    // producer: chunk c goes into stage c % 2 once the products of chunk c - 2
+    // (the stage's last reader) have completed
+    if (lane == 0) {
+      for (int c = 0; c < n; ++c) {
+        const int s = c & 1;
+        if (c >= 2 && !wait_bar(&S.done[s], (uint32_t)((c - 2) >> 1) & 1u)) {
+          atomicExch(err, 4);
           S.abort = 1;
-        } else {
-          issue(c + 2);
-          issued = c + 3;
         }
+        if (*(volatile int*)&S.abort) break;
+        issue(c);
+        S.issued = c + 1;
       }
     }
-  }
-  // drain: every product issued has finished before TMEM is read or freed;
-  // after an abort, every copy issued has landed before the CTA exits
-  if (tid == 0) {
-    if (n > 0 && !*(volatile int*)&S.abort) {
+  } else {
+    const int ct = tid - 32;
+    for (int c = 0; c < n; ++c) {
+      const int s = c & 1;
+      const uint32_t par = (uint32_t)(c >> 1) & 1u;
+      if (!wait_bar(&S.full[s], par)) {
+        if (lane == 0) {
+          atomicExch(err, 1);
+          S.abort = 1;
+        }
+      }
+      asm volatile("bar.sync 1, %0;" ::"r"(NC) : "memory");
+      if (*(volatile int*)&S.abort) break;
+      // A: hi in place, lo beside it (element-wise: the layout is the same)
+      {
+        float4* a4 = reinterpret_cast<float4*>(&S.a[s][0][0]);
+        float4* l4 = reinterpret_cast<float4*>(&S.alo[s][0][0]);
+        for (int e = ct; e < NTILE * BM * BK / 4; e += NC) {
+          const float4 v = a4[e];
+          float4 h, lo;
+          h.x = hi13(v.x); lo.x = v.x - h.x;
+          h.y = hi13(v.y); lo.y = v.y - h.y;
+          h.z = hi13(v.z); lo.z = v.z - h.z;
+          h.w = hi13(v.w); lo.w = v.w - h.w;
+          a4[e] = h;
+          l4[e] = lo;
+        }
+      }
+      // B: 64 x 32, B[r][q] = before_p[r] * after_{q0+q}[r].  A thread takes
+      // one q (its lane) and the ranks r = (warp - 1) + 7 u: the indices of p
+      // and q are decomposed once per chunk (32-bit: P, Q < 2^31), then one
+      // factor load per other mode and rank.
+      {
+        const long long cc = cbeg + c;
+        const unsigned p = (unsigned)(cc / qchunks);
+        const unsigned q = (unsigned)(cc - (long long)p * qchunks) * BK + (unsigned)lane;
+        const bool qok = q < (unsigned)sh.Q;
+        int ib[TFX_MAX_ORDER], ia[TFX_MAX_ORDER];
+        {
+          unsigned rem = p;
+          for (int m = l - 1; m >= 0; --m) {
+            const unsigned dm = (unsigned)sh.dims[m];
+            const unsigned qm = rem / dm;
+            ib[m] = (int)(rem - qm * dm);
+            rem = qm;
+          }
+          rem = qok ? q : 0u;
+          for (int m = sh.L - 1; m > l; --m) {
+            const unsigned dm = (unsigned)sh.dims[m];
+            const unsigned qm = rem / dm;
+            ia[m] = (int)(rem - qm * dm);
+            rem = qm;
+          }
+        }
+        for (int r = warp - 1; r < NR; r += NC / 32) {
+          float v = 0.f;
+          if (r < R && qok) {
+            v = 1.f;
+            for (int m = 0; m < l; ++m) v *= __ldg(sh.W[m] + (long long)r * sh.dims[m] + ib[m]);
+            for (int m = l + 1; m < sh.L; ++m) v *= __ldg(sh.W[m] + (long long)r * sh.dims[m] + ia[m]);
+          }
+          const float h = hi13(v);
+          const uint32_t o = sw_off(r, lane);
+          *(float*)(S.bhi[s] + o) = h;
+          *(float*)(S.blo[s] + o) = v - h;
+        }
+      }
+      // generic-proxy writes -> visible to the tensor core's async proxy
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+      asm volatile("bar.sync 1, %0;" ::"r"(NC) : "memory");
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      if (tid == 32) {
+        for (int t = 0; t < NTILE; ++t) {
+          const uint64_t ah = desc(S.a[s][t]), al = desc(S.alo[s][t]);
+          const uint64_t bh = desc(S.bhi[s]), bl = desc(S.blo[s]);
+          for (int pass = 0; pass < 3; ++pass) {
+            const uint64_t da = pass == 2 ? al : ah;
+            const uint64_t db = pass == 1 ? bl : bh;
+#pragma unroll
+            for (int kk = 0; kk < BK / 8; ++kk)
+              mma(tmem + (uint32_t)(t * NR), da + (uint64_t)(kk * 2), db + (uint64_t)(kk * 2),
+                  (c > 0 || pass > 0 || kk > 0) ? 1u : 0u);
+          }
+        }
+        commit(&S.done[s]);
+        S.consumed = c + 1;
+      }
+    }
+    // every product has finished before TMEM is read
+    if (tid == 32 && n > 0 && !*(volatile int*)&S.abort) {
       const int c = n - 1;
       if (!wait_bar(&S.done[c & 1], (uint32_t)(c >> 1) & 1u)) {
         atomicExch(err, 3);
         S.abort = 1;
       }
-    } else if (*(volatile int*)&S.abort) {
-      for (int c = consumed; c < issued; ++c) wait_bar(&S.full[c & 1], (uint32_t)(c >> 1) & 1u);
-      // products committed before the abort: wait for the last commit (bounded)
-      if (consumed > 0) wait_bar(&S.done[(consumed - 1) & 1], (uint32_t)((consumed - 1) >> 1) & 1u);
     }
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  // after an abort: every copy issued lands and every product committed
+  // finishes (bounded waits) before the CTA frees TMEM and exits
+  if (tid == 0 && *(volatile int*)&S.abort) {
+    const int issued = S.issued, consumed = S.consumed;
+    for (int c = consumed; c < issued; ++c) wait_bar(&S.full[c & 1], (uint32_t)(c >> 1) & 1u);
+    if (consumed > 0) wait_bar(&S.done[(consumed - 1) & 1], (uint32_t)((consumed - 1) >> 1) & 1u);
+  }
+  __syncthreads();
   const bool ok = !*(volatile int*)&S.abort;
   // epilogue: warp w reads TMEM lanes 32 (w % 4) .. + 31 of tile w / 4
   {
