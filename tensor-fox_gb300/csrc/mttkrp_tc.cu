@@ -17,14 +17,14 @@
 //   * warp 0 (producer) brings the two 128 x 32 tensor tiles of a chunk by TMA
 //     (3-D map over (q, d, p), SWIZZLE_128B) into a two-stage ring, a stage
 //     being refilled as soon as the products that read it have completed;
-//   * warps 1-7 split every tile value x into x_hi = x with its 13 low
+//   * warps 2-7 split every tile value x into x_hi = x with its 13 low
 //     mantissa bits cleared (exact in TF32) and x_lo = x - x_hi, and form the
 //     chunk's B operand (64 x 32, K-major, SWIZZLE_128B) the same way from the
-//     factor rows;
-//   * one of them issues tcgen05.mma kind::tf32 (M = 128, N = 64, K = 8):
+//     factor rows, and arrive on the stage's "formed" mbarrier;
+//   * warp 1 issues tcgen05.mma kind::tf32 (M = 128, N = 64, K = 8):
 //     A_hi B_hi + A_hi B_lo + A_lo B_hi per tile, FP32 accumulation in TMEM,
 //     so the product keeps FP32 accuracy (3xTF32), and commits to the stage's
-//     mbarrier, while the others convert the next chunk.
+//     mbarrier, while the converters work on the next chunk.
 // The accumulators are written as per-CTA partials and summed in a fixed
 // order (compensated FP32) by a second kernel.  Every wait is bounded; a wait
 // that runs out sets *err, the CTA drains its copies (bounded) and frees TMEM.
@@ -110,6 +110,7 @@ struct Smem {
   alignas(1024) unsigned char blo[STAGES][NR * 128];
   alignas(8) uint64_t full[STAGES];
   alignas(8) uint64_t done[STAGES];
+  alignas(8) uint64_t conv[STAGES];
   uint32_t tmem;
   int abort;
   int issued;    // chunks whose copies the producer issued
@@ -141,6 +142,7 @@ __global__ void __launch_bounds__(NT, 1)
     for (int s = 0; s < STAGES; ++s) {
       mbar_init(&S.full[s], 1);
       mbar_init(&S.done[s], 1);
+      mbar_init(&S.conv[s], NT / 32 - 2);
     }
     S.abort = 0;
     S.issued = 0;
@@ -164,7 +166,7 @@ __global__ void __launch_bounds__(NT, 1)
     expect_tx(&S.full[s], NTILE * TILE_BYTES);
     for (int t = 0; t < NTILE; ++t) tma_3d(S.a[s][t], &tmap, &S.full[s], q0, row0 + t * BM, p);
   };
-  constexpr int NC = NT - 32;  // converter threads (warps 1..7)
+  constexpr int NCW = NT / 32 - 2;  // converter warps (2..7)
   if (warp == 0) {
     // producer: chunk c goes into stage c % 2 once the products of chunk c - 2
     // (the stage's last reader) have completed
@@ -180,79 +182,17 @@ __global__ void __launch_bounds__(NT, 1)
         S.issued = c + 1;
       }
     }
-  } else {
-    const int ct = tid - 32;
-    for (int c = 0; c < n; ++c) {
-      const int s = c & 1;
-      const uint32_t par = (uint32_t)(c >> 1) & 1u;
-      if (!wait_bar(&S.full[s], par)) {
-        if (lane == 0) {
-          atomicExch(err, 1);
+  } else if (warp == 1) {
+    // MMA issuer: the products of chunk c once its operands are formed
+    if (lane == 0) {
+      for (int c = 0; c < n; ++c) {
+        const int s = c & 1;
+        if (!wait_bar(&S.conv[s], (uint32_t)(c >> 1) & 1u)) {
+          atomicExch(err, 5);
           S.abort = 1;
         }
-      }
-      asm volatile("bar.sync 1, %0;" ::"r"(NC) : "memory");
-      if (*(volatile int*)&S.abort) break;
-      // A: hi in place, lo beside it (element-wise: the layout is the same)
-      {
-        float4* a4 = reinterpret_cast<float4*>(&S.a[s][0][0]);
-        float4* l4 = reinterpret_cast<float4*>(&S.alo[s][0][0]);
-        for (int e = ct; e < NTILE * BM * BK / 4; e += NC) {
-          const float4 v = a4[e];
-          float4 h, lo;
-          h.x = hi13(v.x); lo.x = v.x - h.x;
-          h.y = hi13(v.y); lo.y = v.y - h.y;
-          h.z = hi13(v.z); lo.z = v.z - h.z;
-          h.w = hi13(v.w); lo.w = v.w - h.w;
-          a4[e] = h;
-          l4[e] = lo;
-        }
-      }
-      // B: 64 x 32, B[r][q] = before_p[r] * after_{q0+q}[r].  A thread takes
-      // one q (its lane) and the ranks r = (warp - 1) + 7 u: the indices of p
-      // and q are decomposed once per chunk (32-bit: P, Q < 2^31), then one
-      // factor load per other mode and rank.
-      {
-        const long long cc = cbeg + c;
-        const unsigned p = (unsigned)(cc / qchunks);
-        const unsigned q = (unsigned)(cc - (long long)p * qchunks) * BK + (unsigned)lane;
-        const bool qok = q < (unsigned)sh.Q;
-        int ib[TFX_MAX_ORDER], ia[TFX_MAX_ORDER];
-        {
-          unsigned rem = p;
-          for (int m = l - 1; m >= 0; --m) {
-            const unsigned dm = (unsigned)sh.dims[m];
-            const unsigned qm = rem / dm;
-            ib[m] = (int)(rem - qm * dm);
-            rem = qm;
-          }
-          rem = qok ? q : 0u;
-          for (int m = sh.L - 1; m > l; --m) {
-            const unsigned dm = (unsigned)sh.dims[m];
-            const unsigned qm = rem / dm;
-            ia[m] = (int)(rem - qm * dm);
-            rem = qm;
-          }
-        }
-        for (int r = warp - 1; r < NR; r += NC / 32) {
-          float v = 0.f;
-          if (r < R && qok) {
-            v = 1.f;
-            for (int m = 0; m < l; ++m) v *= __ldg(sh.W[m] + (long long)r * sh.dims[m] + ib[m]);
-            for (int m = l + 1; m < sh.L; ++m) v *= __ldg(sh.W[m] + (long long)r * sh.dims[m] + ia[m]);
-          }
-          const float h = hi13(v);
-          const uint32_t o = sw_off(r, lane);
-          *(float*)(S.bhi[s] + o) = h;
-          *(float*)(S.blo[s] + o) = v - h;
-        }
-      }
-      // generic-proxy writes -> visible to the tensor core's async proxy
-      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-      asm volatile("bar.sync 1, %0;" ::"r"(NC) : "memory");
-      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      if (tid == 32) {
+        if (*(volatile int*)&S.abort) break;
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
         for (int t = 0; t < NTILE; ++t) {
           const uint64_t ah = desc(S.a[s][t]), al = desc(S.alo[s][t]);
           const uint64_t bh = desc(S.bhi[s]), bl = desc(S.blo[s]);
@@ -268,14 +208,85 @@ __global__ void __launch_bounds__(NT, 1)
         commit(&S.done[s]);
         S.consumed = c + 1;
       }
-    }
-    // every product has finished before TMEM is read
-    if (tid == 32 && n > 0 && !*(volatile int*)&S.abort) {
-      const int c = n - 1;
-      if (!wait_bar(&S.done[c & 1], (uint32_t)(c >> 1) & 1u)) {
-        atomicExch(err, 3);
-        S.abort = 1;
+      // every product has finished before TMEM is read
+      if (n > 0 && !*(volatile int*)&S.abort) {
+        const int c = n - 1;
+        if (!wait_bar(&S.done[c & 1], (uint32_t)(c >> 1) & 1u)) {
+          atomicExch(err, 3);
+          S.abort = 1;
+        }
       }
+    }
+  } else {
+    // converters (warps 2..7): split the tiles, form B, hand the stage over
+    const int ct = tid - 64;
+    for (int c = 0; c < n; ++c) {
+      const int s = c & 1;
+      if (!wait_bar(&S.full[s], (uint32_t)(c >> 1) & 1u)) {
+        if (lane == 0) {
+          atomicExch(err, 1);
+          S.abort = 1;
+        }
+      }
+      if (*(volatile int*)&S.abort) break;
+      // A: hi in place, lo beside it (element-wise: the layout is the same)
+      {
+        float4* a4 = reinterpret_cast<float4*>(&S.a[s][0][0]);
+        float4* l4 = reinterpret_cast<float4*>(&S.alo[s][0][0]);
+        for (int e = ct; e < NTILE * BM * BK / 4; e += NCW * 32) {
+          const float4 v = a4[e];
+          float4 h, lo;
+          h.x = hi13(v.x); lo.x = v.x - h.x;
+          h.y = hi13(v.y); lo.y = v.y - h.y;
+          h.z = hi13(v.z); lo.z = v.z - h.z;
+          h.w = hi13(v.w); lo.w = v.w - h.w;
+          a4[e] = h;
+          l4[e] = lo;
+        }
+      }
+      // B: 64 x 32, B[r][q] = before_p[r] * after_{q0+q}[r].  A thread takes
+      // one q (its lane) and the ranks r = (warp - 2) + 6 u; the indices of p
+      // and q are decomposed once per chunk (32-bit: P, Q < 2^31) into
+      // registers (loops unrolled over the modes), then one factor load per
+      // other mode and rank.
+      {
+        const long long cc = cbeg + c;
+        const unsigned p = (unsigned)(cc / qchunks);
+        const unsigned q = (unsigned)(cc - (long long)p * qchunks) * BK + (unsigned)lane;
+        const bool qok = q < (unsigned)sh.Q;
+        int idx[TFX_MAX_ORDER];
+        unsigned rb = p, ra = qok ? q : 0u;
+#pragma unroll
+        for (int m = TFX_MAX_ORDER - 1; m >= 0; --m) {
+          idx[m] = 0;
+          if (m < sh.L && m != l) {
+            const unsigned dm = (unsigned)sh.dims[m];
+            unsigned& rem = (m < l) ? rb : ra;
+            const unsigned qm = rem / dm;
+            idx[m] = (int)(rem - qm * dm);
+            rem = qm;
+          }
+        }
+        for (int r = warp - 2; r < NR; r += NCW) {
+          float v = 0.f;
+          if (r < R && qok) {
+            v = 1.f;
+#pragma unroll
+            for (int m = 0; m < TFX_MAX_ORDER; ++m)
+              if (m < sh.L && m != l) v *= __ldg(sh.W[m] + (long long)r * sh.dims[m] + idx[m]);
+          }
+          const float h = hi13(v);
+          const uint32_t o = sw_off(r, lane);
+          *(float*)(S.bhi[s] + o) = h;
+          *(float*)(S.blo[s] + o) = v - h;
+        }
+      }
+      // generic-proxy writes -> visible to the tensor core's async proxy; one
+      // arrival per converter warp
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+      __syncwarp();
+      if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(su32(&S.conv[s])) : "memory");
     }
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
