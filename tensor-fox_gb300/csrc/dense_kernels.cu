@@ -618,8 +618,7 @@ __global__ void __launch_bounds__(TFX_THREADS) k_orth(T* Y, int D, int k) {
 // ---------------------------------------------------------------------------
 template <class T>
 __global__ void __launch_bounds__(512) k_jacobi(const T* __restrict__ Ain, int n, T* __restrict__ evals,
-                                                        T* __restrict__ V, int max_sweeps, int* __restrict__ sweeps_out,
-                                                        int double_buffer) {
+                                                        T* __restrict__ V, int max_sweeps, int* __restrict__ sweeps_out) {
   extern __shared__ __align__(16) char smem[];
   const int m = (n + 1) & ~1;  // even size (a zero row/column pads odd n)
   T* A = (T*)smem;             // m x m
@@ -636,32 +635,11 @@ __global__ void __launch_bounds__(512) k_jacobi(const T* __restrict__ Ain, int n
     Vs[e] = (i == j) ? T(1) : T(0);
   }
   __syncthreads();
-  int sweep;
-  const T* Af = A;
-  if (double_buffer) {
-    // the second matrix buffer follows the block list
-    const int h = m / 2;
-    T* A1 = (T*)(((uintptr_t)(blk + h * (h + 1) / 2) + 15) & ~(uintptr_t)15);
-    for (int b = tid; b < h * (h + 1) / 2; b += blockDim.x) {
-      // the block list, as cta_jacobi builds it
-      int kp = 0, rem = b;
-      while (rem >= h - kp) {
-        rem -= h - kp;
-        ++kp;
-      }
-      blk[b] = ((unsigned)kp << 16) | (unsigned)(kp + rem);
-    }
-    __syncthreads();
-    int where = 0;
-    sweep = cta_jacobi_db<T>(A, A1, Vs, blk, (volatile int*)red, m, max_sweeps, &where);
-    Af = where ? A1 : A;
-  } else {
-    sweep = cta_jacobi<T>(A, Vs, cs, pr, red, m, max_sweeps, blk);
-  }
+  const int sweep = cta_jacobi<T>(A, Vs, cs, pr, red, m, max_sweeps, blk);
   // sort eigenvalues (descending) with their vectors
   for (int i = tid; i < n; i += blockDim.x) {
-    const int rank = eig_rank<T>(Af, m, n, i);
-    evals[rank] = Af[i * m + i];
+    const int rank = eig_rank<T>(A, m, n, i);
+    evals[rank] = A[i * m + i];
     for (int r = 0; r < n; ++r) V[(size_t)rank * n + r] = Vs[i * m + r];
   }
   if (tid == 0 && sweeps_out) *sweeps_out = sweep;
@@ -1067,31 +1045,21 @@ extern "C" size_t tfx_sym_eig_smem_bytes(int dtype, int n) {
   return b + 2 * (TFX_THREADS / 32) * sizeof(double) + h * (h + 1) / 2 * sizeof(unsigned);
 }
 
-// with a second m x m matrix buffer for the one-barrier rounds
-static size_t sym_eig_db_bytes(int dtype, int n) {
-  const int m = (n + 1) & ~1;
-  const size_t es = dtype == TFX_F64 ? 8 : 4;
-  return tfx_sym_eig_smem_bytes(dtype, n) + 16 + (size_t)m * m * es;
-}
-
 extern "C" int tfx_sym_eig(int dtype, const void* A, int n, void* evals, void* V, int max_sweeps, int* sweeps,
                            void* stream) {
   if (!A || !evals || !V || n < 1) return tfx_set_error(TFX_STATUS_ERR_ARG, "sym_eig args");
-  size_t sm = tfx_sym_eig_smem_bytes(dtype, n);
+  const size_t sm = tfx_sym_eig_smem_bytes(dtype, n);
   if (sm > 220 * 1024) return tfx_set_error(TFX_STATUS_ERR_UNSUPPORTED, "sym_eig matrix too large");
-  // one block barrier per round when the second matrix buffer fits
-  const int db = sym_eig_db_bytes(dtype, n) <= 200 * 1024 ? 1 : 0;
-  if (db) sm = sym_eig_db_bytes(dtype, n);
   cudaStream_t st = (cudaStream_t)stream;
   cudaError_t e;
   if (dtype == TFX_F32) {
     e = cudaFuncSetAttribute(k_jacobi<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     if (e != cudaSuccess) return tfx_set_cuda_error(e, "sym_eig attr");
-    k_jacobi<float><<<1, 512, sm, st>>>((const float*)A, n, (float*)evals, (float*)V, max_sweeps, sweeps, db);
+    k_jacobi<float><<<1, 512, sm, st>>>((const float*)A, n, (float*)evals, (float*)V, max_sweeps, sweeps);
   } else {
     e = cudaFuncSetAttribute(k_jacobi<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     if (e != cudaSuccess) return tfx_set_cuda_error(e, "sym_eig attr");
-    k_jacobi<double><<<1, 512, sm, st>>>((const double*)A, n, (double*)evals, (double*)V, max_sweeps, sweeps, db);
+    k_jacobi<double><<<1, 512, sm, st>>>((const double*)A, n, (double*)evals, (double*)V, max_sweeps, sweeps);
   }
   return check_launch("sym_eig");
 }

@@ -138,131 +138,6 @@ __device__ int cta_jacobi(T* A, T* Vs, T* cs, int* pr, double* red, int m, int m
 }
 
 // rank of eigenvalue i in descending order (ties by index)
-// The rotation of pair (p, q) from a_pp, a_qq, a_pq (the same threshold and
-// formulas as cta_jacobi).  Not inlined: every thread that needs a pair's
-// rotation runs this one instruction sequence, so they all get the same bits.
-template <class T>
-__device__ __noinline__ bool jacobi_angle(T app, T aqq, T apq, T tol, T* c_out, T* s_out) {
-  T c = T(1), s = T(0);
-  bool rot = false;
-  if (apq != T(0) && fabs(apq) * fabs(apq) > tol * tol * fabs(app * aqq)) {
-    T t;
-    if (sizeof(T) == 8) {
-      const T tau = (aqq - app) / (T(2) * apq);
-      const T at = fabs(tau);
-      t = (at > T(1e150)) ? T(1) / (T(2) * tau) : (tau >= T(0) ? T(1) : T(-1)) / (at + sqrt(T(1) + tau * tau));
-      c = T(1) / sqrt(T(1) + t * t);
-    } else {
-      const float tau = __fdividef((float)(aqq - app), 2.f * (float)apq);
-      const float at = fabsf(tau);
-      const float s2 = fmaf(tau, tau, 1.f);
-      const float tt = (at > 1e18f) ? __fdividef(0.5f, tau) : copysignf(__fdividef(1.f, at + s2 * rsqrtf(s2)), tau);
-      t = (T)tt;
-      c = (T)rsqrtf(fmaf(tt, tt, 1.f));
-    }
-    s = t * c;
-    rot = true;
-  }
-  *c_out = c;
-  *s_out = s;
-  return rot;
-}
-
-// The same Jacobi iteration with the matrix double-buffered: each round reads
-// A (current) and writes An (next), every thread forming the rotations of the
-// pairs its blocks touch from the current matrix, so a round needs ONE block
-// barrier instead of two (no thread waits for another's rotation angles).
-// A0, A1 (m x m) and Vs as in cta_jacobi; blk: the h(h+1)/2 upper-triangle
-// blocks (kp << 16 | kq); flags: three ints.  Returns the sweeps taken; the
-// final matrix is in A0 when the returned `where` is 0, else in A1.
-template <class T>
-__device__ int cta_jacobi_db(T* A0, T* A1, T* Vs, const unsigned* blk, volatile int* flag, int m, int max_sweeps,
-                             int* where) {
-  const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, wid = tid >> 5, nw = nt >> 5;
-  const int h = m / 2, nblk = h * (h + 1) / 2;
-  const T tol = sizeof(T) == 8 ? T(4.5e-16) : T(2.4e-7);
-  if (tid == 0) flag[0] = 0;
-  __syncthreads();
-  T* A = A0;
-  T* An = A1;
-  int cur = 0;
-  int sweep = 0;
-  auto pair_of = [&](int kk, int round, int& p, int& q) {
-    int a = kk + round, b = m - 1 - kk + round;
-    if (a >= m - 1) a -= m - 1;
-    if (b >= m - 1) b -= m - 1;
-    if (kk == 0) a = m - 1;
-    p = a < b ? a : b;
-    q = a < b ? b : a;
-  };
-  for (sweep = 0; sweep < max_sweeps; ++sweep) {
-    if (tid == 0) flag[(sweep + 1) % 3] = 0;
-    for (int round = 0; round < m - 1; ++round) {
-      bool rotated = false;
-      for (int e = tid; e < nblk; e += nt) {
-        const int kp = (int)(blk[e] >> 16), kq = (int)(blk[e] & 0xffffu);
-        int p, q, r, u;
-        pair_of(kp, round, p, q);
-        pair_of(kq, round, r, u);
-        T cp, sp, cr, sr;
-        rotated |= jacobi_angle<T>(A[p * m + p], A[q * m + q], A[p * m + q], tol, &cp, &sp);
-        jacobi_angle<T>(A[r * m + r], A[u * m + u], A[r * m + u], tol, &cr, &sr);
-        const T apr = A[p * m + r], apu = A[p * m + u], aqr = A[q * m + r], aqu = A[q * m + u];
-        T ypr = apr, ypu = apu, yqr = aqr, yqu = aqu;
-        if (sp != T(0) || sr != T(0)) {
-          // columns (r, u) rotated first, then rows (p, q)
-          const T xpr = cr * apr - sr * apu, xpu = sr * apr + cr * apu;
-          const T xqr = cr * aqr - sr * aqu, xqu = sr * aqr + cr * aqu;
-          ypr = cp * xpr - sp * xqr;
-          yqr = sp * xpr + cp * xqr;
-          ypu = cp * xpu - sp * xqu;
-          yqu = sp * xpu + cp * xqu;
-          if (kp == kq) {
-            // diagonal block: the rotation annihilates a_pq exactly
-            ypu = T(0);
-            yqr = T(0);
-          }
-        }
-        An[p * m + r] = ypr;
-        An[p * m + u] = ypu;
-        An[q * m + r] = yqr;
-        An[q * m + u] = yqu;
-        if (kp != kq) {
-          An[r * m + p] = ypr;
-          An[u * m + p] = ypu;
-          An[r * m + q] = yqr;
-          An[u * m + q] = yqu;
-        }
-      }
-      if (rotated) flag[sweep % 3] = 1;
-      // eigenvectors: the pair's columns of Vs, rotated in place (pairs are disjoint)
-      for (int kk = wid; kk < h; kk += nw) {
-        int p, q;
-        pair_of(kk, round, p, q);
-        T c, s;
-        jacobi_angle<T>(A[p * m + p], A[q * m + q], A[p * m + q], tol, &c, &s);
-        if (s == T(0)) continue;
-        T* vp = Vs + p * m;
-        T* vq = Vs + q * m;
-        for (int i = lane; i < m; i += 32) {
-          const T vip = vp[i], viq = vq[i];
-          vp[i] = c * vip - s * viq;
-          vq[i] = s * vip + c * viq;
-        }
-      }
-      __syncthreads();
-      T* t = A;
-      A = An;
-      An = t;
-      cur ^= 1;
-    }
-    if (!flag[sweep % 3]) break;
-  }
-  __syncthreads();
-  *where = cur;
-  return sweep;
-}
-
 template <class T>
 __device__ __forceinline__ int eig_rank(const T* A, int m, int n, int i) {
   const T li = A[i * m + i];
