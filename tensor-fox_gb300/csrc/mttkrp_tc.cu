@@ -267,18 +267,39 @@ __global__ void __launch_bounds__(NT, 1)
             rem = qm;
           }
         }
-        for (int r = warp - 2; r < NR; r += NCW) {
-          float v = 0.f;
-          if (r < R && qok) {
-            v = 1.f;
+        // every factor load of a mode is issued before any is used: one L2
+        // round trip per mode instead of one per rank
+        constexpr int NU = (NR + NCW - 1) / NCW;
+        float v[NU];
 #pragma unroll
-            for (int m = 0; m < TFX_MAX_ORDER; ++m)
-              if (m < sh.L && m != l) v *= __ldg(sh.W[m] + (long long)r * sh.dims[m] + idx[m]);
+        for (int u = 0; u < NU; ++u) {
+          const int r = warp - 2 + NCW * u;
+          v[u] = (r < R && qok) ? 1.f : 0.f;
+        }
+#pragma unroll
+        for (int m = 0; m < TFX_MAX_ORDER; ++m) {
+          if (m < sh.L && m != l) {
+            const float* wm = sh.W[m] + idx[m];
+            const long long dm = sh.dims[m];
+            float w[NU];
+#pragma unroll
+            for (int u = 0; u < NU; ++u) {
+              const int r = warp - 2 + NCW * u;
+              w[u] = (r < R && qok) ? __ldg(wm + (long long)r * dm) : 0.f;
+            }
+#pragma unroll
+            for (int u = 0; u < NU; ++u) v[u] *= w[u];
           }
-          const float h = hi13(v);
-          const uint32_t o = sw_off(r, lane);
-          *(float*)(S.bhi[s] + o) = h;
-          *(float*)(S.blo[s] + o) = v - h;
+        }
+#pragma unroll
+        for (int u = 0; u < NU; ++u) {
+          const int r = warp - 2 + NCW * u;
+          if (r < NR) {
+            const float h = hi13(v[u]);
+            const uint32_t o = sw_off(r, lane);
+            *(float*)(S.bhi[s] + o) = h;
+            *(float*)(S.blo[s] + o) = v[u] - h;
+          }
         }
       }
       // generic-proxy writes -> visible to the tensor core's async proxy; one

@@ -158,7 +158,7 @@ __device__ __forceinline__ float4 ld4(const float* p, bool aligned) {
 // entries of the row are in flight per warp.  Lanes with the same q combine
 // their float-float partial sums with shuffles at the end of the row.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) k_coo_mttkrp_f4(const int* __restrict__ sidx, const float* __restrict__ svals,
+__global__ void __launch_bounds__(256, 4) k_coo_mttkrp_f4(const int* __restrict__ sidx, const float* __restrict__ svals,
                                                        long long nnz, const long long* __restrict__ rowptr, CooShape sh,
                                                        int mode, const float* const* __restrict__ Wrow,
                                                        float* __restrict__ out, int r0) {
@@ -168,32 +168,53 @@ __global__ void __launch_bounds__(256) k_coo_mttkrp_f4(const int* __restrict__ s
   const int R = sh.R;
   const int rq = r0 + 4 * q;
   const bool on = rq < R;
-  const float* wb[TFX_MAX_ORDER];
   bool al = true;  // rows are 16-byte aligned when every factor base is (R % 4 == 0)
-  for (int m = 0; m < sh.L; ++m) {
-    wb[m] = Wrow[m] + rq;
-    al = al && ((unsigned long long)Wrow[m] & 15ull) == 0;
-  }
+  for (int m = 0; m < sh.L; ++m) al = al && ((unsigned long long)Wrow[m] & 15ull) == 0;
   for (int row = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; row < d; row += warps) {
     const long long b = rowptr[row], e = rowptr[row + 1];
     Acc<float> acc[4];
-    for (long long k = b + slot; k < e; k += 8) {
-      const float v = svals[k];
-      float p0 = v, p1 = v, p2 = v, p3 = v;
+    // four entries of the slot per pass (k, k + 8, k + 16, k + 24): per mode
+    // their four coordinates are loaded together, then their four factor
+    // rows, so a pass waits for two round trips per mode instead of eight;
+    // the sums keep the slot's entry order
+    constexpr int UNR = 4;
+    for (long long k = b + slot; k < e; k += 8 * UNR) {
+      float pv[UNR][4];
+#pragma unroll
+      for (int u = 0; u < UNR; ++u) {
+        const long long kk = k + 8 * u;
+        const float v = kk < e ? svals[kk] : 0.f;
+        pv[u][0] = pv[u][1] = pv[u][2] = pv[u][3] = v;
+      }
       if (on) {
         for (int m = 0; m < sh.L; ++m) {
           if (m == mode) continue;
-          const float4 w = ld4(wb[m] + (size_t)sidx[(size_t)m * nnz + k] * R, al);
-          p0 *= w.x;
-          p1 *= w.y;
-          p2 *= w.z;
-          p3 *= w.w;
+          const int* im = sidx + (size_t)m * nnz;
+          int ix[UNR];
+#pragma unroll
+          for (int u = 0; u < UNR; ++u) ix[u] = (k + 8 * u < e) ? im[k + 8 * u] : 0;
+          const float* wm = Wrow[m] + rq;
+          float4 w[UNR];
+#pragma unroll
+          for (int u = 0; u < UNR; ++u) w[u] = ld4(wm + (size_t)ix[u] * R, al);
+#pragma unroll
+          for (int u = 0; u < UNR; ++u) {
+            pv[u][0] *= w[u].x;
+            pv[u][1] *= w[u].y;
+            pv[u][2] *= w[u].z;
+            pv[u][3] *= w[u].w;
+          }
         }
       }
-      acc[0].add(p0);
-      acc[1].add(p1);
-      acc[2].add(p2);
-      acc[3].add(p3);
+#pragma unroll
+      for (int u = 0; u < UNR; ++u) {
+        if (k + 8 * u < e) {
+          acc[0].add(pv[u][0]);
+          acc[1].add(pv[u][1]);
+          acc[2].add(pv[u][2]);
+          acc[3].add(pv[u][3]);
+        }
+      }
     }
 #pragma unroll
     for (int u = 0; u < 4; ++u) {
