@@ -866,6 +866,18 @@ def run_case(case):
             b.launch(gauss_newton.auto_cluster(tuple(S.shape), RANK))
         torch.cuda.synchronize()
         print(json.dumps({"case": case, "result": b.result[0].cpu().numpy().tolist()}))
+    elif case == "mttkrp_tc_small":
+        # tcgen05 MTTKRP of a 512 x 256 x 512 FP32 tensor (268 MB), rank 50:
+        # modes 0 and 1, two launches each
+        dims = [512, 256, 512]
+        g = torch.Generator(device="cuda").manual_seed(0)
+        T = torch.randn(dims, device="cuda", generator=g)
+        Wf = torch.randn(RANK * sum(dims), device="cuda", generator=g)
+        for l in (0, 1):
+            for _ in range(2):
+                out, err = kernels.mttkrp_tc(T, dims, Wf, RANK, l)
+        torch.cuda.synchronize()
+        print(json.dumps({"case": case, "err": int(err.item()), "m00": float(out[0, 0])}))
     elif case == "residual_tc":
         # the full-tensor residual of the headline tensor (tcgen05 path), five launches
         T, W = make_problem()
@@ -917,7 +929,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-sparse", action="store_true")
-    ap.add_argument("--case", default=None, help="tc_gram_small | engine_core | residual_tc | c3_autograd | sparse_c5 | direct (profiling workloads)")
+    ap.add_argument("--case", default=None, help="tc_gram_small | mttkrp_tc_small | engine_core | residual_tc | c3_autograd | sparse_c5 | sparse_cpd | "
+                    "sparse_cpd_mid | sparse_direct_c5 | direct (profiling workloads)")
     args = ap.parse_args()
     if args.case:
         run_case(args.case)

@@ -292,7 +292,14 @@ int tfx_coo_gram(int dtype, const int* idx32, const void* vals, long long nnz, c
  * x = x_old + y, W = x, out2 = {(x - x_old).(grad + damp (x - x_old)),
  * |x - x_old|^2}; tfx_step_sums: out4 = {(x - x_old).(grad + damp (x -
  * x_old)), |x - x_old|^2, |x_old|^2, max|grad|}; tfx_step_revert: x_out =
- * x - y.  scratch: tfx_dogleg_scratch_bytes(). */
+ * x - y.  scratch: tfx_dogleg_scratch_bytes().
+ * tfx_step_update_wide: the step update of GaussNewton.py:284-297 without
+ * symmetric transform, fixed norm or fixed factor, over the whole grid: x +=
+ * y (rounded to the working type), W = x with balanced columns
+ * (Conversion.py:361-387), out4 = {|x - x_old|^2, |x_old|^2, (x - x_old).(grad +
+ * damp (x - x_old)), max|grad| (NaN if any entry is)} -- the out4 of
+ * tfx_dgn_step_update for the same call.  R <= 64; scratch:
+ * tfx_step_update_wide_scratch_bytes(). */
 size_t tfx_coo_dgn_cg_workspace_bytes(int dtype, int L, const int* dims, int R);
 int tfx_coo_dgn_cg(int dtype, int L, const int* dims, int R, const void* W, const void* Mrm, double damp, int budget,
                    double cg_tol, double* y, double* grad, double* jtj, double* out, void* work, size_t work_bytes,
@@ -309,6 +316,10 @@ int tfx_dogleg_trial(int dtype, long long n, const void* x_old, double* y, const
 int tfx_step_sums(int dtype, long long n, const void* x, const void* x_old, const double* grad, double damp,
                   double* out4, void* scratch, void* stream);
 int tfx_step_revert(int dtype, long long n, const void* x, const double* y, void* x_out, void* stream);
+size_t tfx_step_update_wide_scratch_bytes(int L, const int* dims, int R);
+int tfx_step_update_wide(int dtype, int L, const int* dims, int R, void* x, void* W, const double* y,
+                         const double* grad, double damp, double* out4, void* scratch, size_t scratch_bytes,
+                         void* stream);
 
 size_t tfx_sparse_ttmc_scratch_bytes(int dtype, long long nnz, int L, const int* n);
 int tfx_sparse_ttmc(int dtype, const int* idx32, const void* vals, long long nnz, int L, const int* dims, const int* n,

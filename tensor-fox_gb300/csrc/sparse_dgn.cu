@@ -460,18 +460,27 @@ __global__ void __launch_bounds__(TFX_THREADS) k_coo_err_partials(CooDgnShape sh
   }
 }
 
-__global__ void __launch_bounds__(TFX_THREADS) k_coo_err_final(CooDgnShape sh, int nb, const double* __restrict__ part,
+// the CTAs' partials summed per entry: one warp per (Gram entry | <W_0, M_0>),
+// lanes stride the CTAs, so the order is fixed
+__global__ void __launch_bounds__(256) k_coo_err_gsum(int nb, int ne, const double* __restrict__ part,
+                                                      double* __restrict__ G) {
+  const int lane = threadIdx.x & 31;
+  const int e = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (e >= ne) return;
+  double s = 0.0;
+  for (int c = lane; c < nb; c += 32) s += part[(size_t)c * ne + e];
+  s = warp_sum(s);
+  if (lane == 0) G[e] = s;
+}
+
+__global__ void __launch_bounds__(TFX_THREADS) k_coo_err_final(CooDgnShape sh, const double* __restrict__ G,
                                                                 double tnorm2, double* __restrict__ out) {
   __shared__ double swarp[TFX_THREADS / 32];
   const int L = sh.L, R = sh.R, RR = R * R, LRR = L * RR, tid = threadIdx.x;
   double model2 = 0.0;
   for (int pq = tid; pq < RR; pq += TFX_THREADS) {
     double prod = 1.0;
-    for (int l = 0; l < L; ++l) {
-      double s = 0.0;
-      for (int c = 0; c < nb; ++c) s += part[(size_t)c * (LRR + 1) + l * RR + pq];
-      prod *= s;
-    }
+    for (int l = 0; l < L; ++l) prod *= G[l * RR + pq];
     model2 += prod;
   }
   model2 = warp_sum(model2);
@@ -480,8 +489,7 @@ __global__ void __launch_bounds__(TFX_THREADS) k_coo_err_final(CooDgnShape sh, i
   if (tid == 0) {
     double m2 = 0.0;
     for (int w = 0; w < TFX_THREADS / 32; ++w) m2 += swarp[w];
-    double ip = 0.0;
-    for (int c = 0; c < nb; ++c) ip += part[(size_t)c * (LRR + 1) + LRR];
+    const double ip = G[LRR];
     out[0] = tnorm2 - 2.0 * ip + m2;
     out[1] = ip;
     out[2] = m2;
@@ -612,6 +620,171 @@ __global__ void k_revert(long long n, const T* __restrict__ x, const double* __r
     x_out[k] = x[k] - (T)y[k];
 }
 
+// ---------------------------------------------------------------------------
+// The step update of GaussNewton.py:284-297 for large factor vectors (no
+// symmetric transform, no fixed norm, no fixed factor): x += y, the step's
+// scalars, column balancing (Conversion.py:361-387) -- over the whole grid.
+// Work item = (column, segment of up to STEP_SEG rows), one warp each; the
+// column sums are kept per item, the step's scalars per CTA, and both are
+// summed in a fixed order, so the result does not vary between runs.
+// ---------------------------------------------------------------------------
+#define STEP_SEG 256
+#define STEP_THREADS 256
+
+struct StepShape {
+  int L, R, nseg_total;
+  int dims[TFX_MAX_ORDER];
+  long long off[TFX_MAX_ORDER + 1];
+  int segs[TFX_MAX_ORDER];        // segments per column of mode l
+  int item0[TFX_MAX_ORDER + 1];   // first item of mode l
+};
+
+// colp[item] = column norm^2 of x_new over the item's rows; blk[4 b ..] =
+// the CTA's {|x_old|^2, |dx|^2, dx.(g + damp dx), max|g| (NaN if any g is)}
+template <class T>
+__global__ void __launch_bounds__(STEP_THREADS) k_step_wide1(StepShape sh, T* __restrict__ x,
+                                                             const double* __restrict__ y,
+                                                             const double* __restrict__ grad, double damp,
+                                                             double* __restrict__ colp, double* __restrict__ blk) {
+  __shared__ double sw[STEP_THREADS / 32][4];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int warps = (gridDim.x * blockDim.x) >> 5;
+  double s0 = 0.0, s1 = 0.0, s2 = 0.0, gi = 0.0;
+  bool gnan = false;
+  for (int item = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; item < sh.nseg_total; item += warps) {
+    int l = 0;
+    while (item >= sh.item0[l + 1]) ++l;
+    const int loc = item - sh.item0[l];
+    const int r = loc / sh.segs[l], sg = loc - r * sh.segs[l];
+    const int d = sh.dims[l];
+    const long long base = sh.off[l] + (long long)r * d;
+    const int i0 = sg * STEP_SEG, i1 = min(d, i0 + STEP_SEG);
+    double cn = 0.0;
+#pragma unroll 4
+    for (int i = i0 + lane; i < i1; i += 32) {
+      const long long e = base + i;
+      const double xo = (double)x[e];
+      const T xn = (T)(xo + y[e]);
+      const double dv = (double)xn - xo;
+      const double g = grad[e];
+      s0 = fma(xo, xo, s0);
+      s1 = fma(dv, dv, s1);
+      s2 = fma(dv, g + damp * dv, s2);
+      if (g != g) gnan = true;
+      gi = fmax(gi, fabs(g));
+      cn = fma((double)xn, (double)xn, cn);
+      x[e] = xn;
+    }
+    cn = warp_sum(cn);
+    if (lane == 0) colp[item] = cn;
+  }
+  s0 = warp_sum(s0);
+  s1 = warp_sum(s1);
+  s2 = warp_sum(s2);
+  gi = warp_max(gi);
+  const int anynan = __any_sync(0xffffffffu, gnan);
+  if (lane == 0) {
+    sw[wid][0] = s0;
+    sw[wid][1] = s1;
+    sw[wid][2] = s2;
+    sw[wid][3] = anynan ? NAN : gi;
+  }
+  __syncthreads();
+  if (threadIdx.x < 4) {
+    const int k = threadIdx.x;
+    double v = 0.0;
+    bool vn = false;
+    for (int w = 0; w < STEP_THREADS / 32; ++w) {
+      const double q = sw[w][k];
+      if (k < 3) {
+        v += q;
+      } else {
+        if (q != q) vn = true;
+        v = fmax(v, q);
+      }
+    }
+    blk[(size_t)blockIdx.x * 4 + k] = (k == 3 && vn) ? NAN : v;
+  }
+}
+
+// column balancing factors (the reference's equalize: (prod_l n_l)^(1/L) / n_l,
+// 1 when a column vanishes) and the step's scalars out4 = {|dx|^2, |x_old|^2,
+// dx.(g + damp dx), max|g|}
+__global__ void __launch_bounds__(STEP_THREADS) k_step_wide2(StepShape sh, int nblk, const double* __restrict__ colp,
+                                                             const double* __restrict__ blk,
+                                                             double* __restrict__ fac, double* __restrict__ out) {
+  __shared__ double nrm[TFX_MAX_ORDER * 64];
+  __shared__ double sw[STEP_THREADS / 32][4];
+  const int L = sh.L, R = sh.R, tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  for (int c = wid; c < L * R; c += STEP_THREADS / 32) {
+    const int l = c / R, r = c - l * R;
+    const int it0 = sh.item0[l] + r * sh.segs[l];
+    double v = 0.0;
+    for (int q = lane; q < sh.segs[l]; q += 32) v += colp[it0 + q];
+    v = warp_sum(v);
+    if (lane == 0) nrm[c] = sqrt(v);
+  }
+  double a = 0.0, b = 0.0, c = 0.0, m = 0.0;
+  bool mn = false;
+  for (int q = tid; q < nblk; q += STEP_THREADS) {
+    const double* o = blk + (size_t)q * 4;
+    a += o[0];
+    b += o[1];
+    c += o[2];
+    if (o[3] != o[3]) mn = true;
+    m = fmax(m, o[3]);
+  }
+  a = warp_sum(a);
+  b = warp_sum(b);
+  c = warp_sum(c);
+  m = warp_max(m);
+  const int anynan = __any_sync(0xffffffffu, mn);
+  if (lane == 0) {
+    sw[wid][0] = a;
+    sw[wid][1] = b;
+    sw[wid][2] = c;
+    sw[wid][3] = anynan ? NAN : m;
+  }
+  __syncthreads();
+  for (int r = tid; r < R; r += STEP_THREADS) {
+    double prod = 1.0;
+    for (int l = 0; l < L; ++l) prod *= nrm[l * R + r];
+    if (prod != 0.0) {
+      const double num = pow(prod, 1.0 / (double)L);
+      for (int l = 0; l < L; ++l) fac[l * R + r] = num / nrm[l * R + r];
+    } else {
+      for (int l = 0; l < L; ++l) fac[l * R + r] = 1.0;
+    }
+  }
+  if (tid == 0) {
+    double t0 = 0.0, t1 = 0.0, t2 = 0.0, t3 = 0.0;
+    bool tn = false;
+    for (int w = 0; w < STEP_THREADS / 32; ++w) {
+      t0 += sw[w][0];
+      t1 += sw[w][1];
+      t2 += sw[w][2];
+      if (sw[w][3] != sw[w][3]) tn = true;
+      t3 = fmax(t3, sw[w][3]);
+    }
+    out[0] = t1;
+    out[1] = t0;
+    out[2] = t2;
+    out[3] = tn ? NAN : t3;
+  }
+}
+
+template <class T>
+__global__ void k_step_wide3(StepShape sh, const T* __restrict__ x, const double* __restrict__ fac,
+                             T* __restrict__ W) {
+  const long long n = sh.off[sh.L];
+  for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x) {
+    int l = 0;
+    while (e >= sh.off[l + 1]) ++l;
+    const int r = (int)((e - sh.off[l]) / sh.dims[l]);
+    W[e] = (T)(fac[l * sh.R + r] * (double)x[e]);
+  }
+}
+
 static int launched(const char* where) {
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return tfx_set_cuda_error(e, where);
@@ -706,7 +879,7 @@ extern "C" int tfx_coo_dgn_cg(int dtype, int L, const int* dims, int R, const vo
 }
 
 extern "C" size_t tfx_coo_model_error_scratch_bytes(int L, int R) {
-  return (size_t)sm_total() * ((size_t)L * R * R + 1) * 8 + 256;
+  return ((size_t)sm_total() + 1) * ((size_t)L * R * R + 1) * 8 + 256;
 }
 
 extern "C" int tfx_coo_model_error(int dtype, int L, const int* dims, int R, const void* W, const void* M0rm,
@@ -715,7 +888,8 @@ extern "C" int tfx_coo_model_error(int dtype, int L, const int* dims, int R, con
   if (fill_coo_shape(sh, L, dims, R) || !W || !M0rm || !out || !scratch)
     return tfx_set_error(TFX_STATUS_ERR_ARG, "coo_model_error args");
   const int nb = std::max(1, std::min(sm_total(), (sh.rowoff[L] + TFX_THREADS - 1) / TFX_THREADS));
-  const size_t need = (size_t)nb * ((size_t)L * R * R + 1) * 8;
+  const int ne = L * R * R + 1;
+  const size_t need = ((size_t)nb + 1) * ne * 8;
   if (scratch_bytes < need) return tfx_set_error(TFX_STATUS_ERR_ARG, "coo_model_error scratch");
   sh.nb = nb;
   cudaStream_t st = (cudaStream_t)stream;
@@ -724,7 +898,10 @@ extern "C" int tfx_coo_model_error(int dtype, int L, const int* dims, int R, con
   else
     k_coo_err_partials<float><<<nb, TFX_THREADS, 0, st>>>(sh, (const float*)W, (const float*)M0rm, (double*)scratch);
   if (int s = launched("coo_err_partials")) return s;
-  k_coo_err_final<<<1, TFX_THREADS, 0, st>>>(sh, nb, (const double*)scratch, tnorm2, out);
+  double* G = (double*)scratch + (size_t)nb * ne;
+  k_coo_err_gsum<<<(ne * 32 + 255) / 256, 256, 0, st>>>(nb, ne, (const double*)scratch, G);
+  if (int s = launched("coo_err_gsum")) return s;
+  k_coo_err_final<<<1, TFX_THREADS, 0, st>>>(sh, G, tnorm2, out);
   return launched("coo_err_final");
 }
 
@@ -796,4 +973,60 @@ extern "C" int tfx_step_revert(int dtype, long long n, const void* x, const doub
   else
     k_revert<float><<<blocks, 256, 0, st>>>(n, (const float*)x, y, (float*)x_out);
   return launched("step_revert");
+}
+
+static int fill_step_shape(StepShape& sh, int L, const int* dims, int R) {
+  if (L < 2 || L > TFX_MAX_ORDER || R < 1 || R > 64 || !dims) return 1;
+  sh.L = L;
+  sh.R = R;
+  sh.off[0] = 0;
+  sh.item0[0] = 0;
+  for (int l = 0; l < L; ++l) {
+    if (dims[l] < 1) return 1;
+    sh.dims[l] = dims[l];
+    sh.off[l + 1] = sh.off[l] + (long long)R * dims[l];
+    sh.segs[l] = (dims[l] + STEP_SEG - 1) / STEP_SEG;
+    sh.item0[l + 1] = sh.item0[l] + R * sh.segs[l];
+  }
+  sh.nseg_total = sh.item0[L];
+  return 0;
+}
+
+static int step_blocks(const StepShape& sh) {
+  return std::max(1, std::min((sh.nseg_total * 32 + STEP_THREADS - 1) / STEP_THREADS, 16 * sm_total()));
+}
+
+extern "C" size_t tfx_step_update_wide_scratch_bytes(int L, const int* dims, int R) {
+  StepShape sh;
+  if (fill_step_shape(sh, L, dims, R)) return 0;
+  return ((size_t)sh.nseg_total + (size_t)step_blocks(sh) * 4 + (size_t)L * R) * 8 + 256;
+}
+
+extern "C" int tfx_step_update_wide(int dtype, int L, const int* dims, int R, void* x, void* W, const double* y,
+                                    const double* grad, double damp, double* out4, void* scratch,
+                                    size_t scratch_bytes, void* stream) {
+  StepShape sh;
+  if (fill_step_shape(sh, L, dims, R) || !x || !W || !y || !grad || !out4 || !scratch)
+    return tfx_set_error(TFX_STATUS_ERR_ARG, "step_update_wide args (R <= 64)");
+  if (scratch_bytes < tfx_step_update_wide_scratch_bytes(L, dims, R))
+    return tfx_set_error(TFX_STATUS_ERR_ARG, "step_update_wide scratch");
+  const int b1 = step_blocks(sh);
+  double* colp = (double*)scratch;
+  double* blk = colp + sh.nseg_total;
+  double* fac = blk + (size_t)b1 * 4;
+  cudaStream_t st = (cudaStream_t)stream;
+  const long long n = sh.off[L];
+  const int b3 = (int)std::max<long long>(1, std::min<long long>((n + 255) / 256, 8LL * sm_total()));
+  if (dtype == TFX_F64)
+    k_step_wide1<double><<<b1, STEP_THREADS, 0, st>>>(sh, (double*)x, y, grad, damp, colp, blk);
+  else
+    k_step_wide1<float><<<b1, STEP_THREADS, 0, st>>>(sh, (float*)x, y, grad, damp, colp, blk);
+  if (int s = launched("step_wide1")) return s;
+  k_step_wide2<<<1, STEP_THREADS, 0, st>>>(sh, b1, colp, blk, fac, out4);
+  if (int s = launched("step_wide2")) return s;
+  if (dtype == TFX_F64)
+    k_step_wide3<double><<<b3, 256, 0, st>>>(sh, (const double*)x, fac, (double*)W);
+  else
+    k_step_wide3<float><<<b3, 256, 0, st>>>(sh, (const float*)x, fac, (float*)W);
+  return launched("step_wide3");
 }

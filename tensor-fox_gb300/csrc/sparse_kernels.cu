@@ -241,7 +241,7 @@ __global__ void __launch_bounds__(256, 4) k_coo_mttkrp_f4(const int* __restrict_
 // (one 16-byte read per factor row), R / 8 lanes per entry, 256 / R entries
 // in flight per warp.  Rows of the output as in the FP32 kernel.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) k_coo_mttkrp_bf16(const int* __restrict__ sidx, const float* __restrict__ svals,
+__global__ void __launch_bounds__(256, 4) k_coo_mttkrp_bf16(const int* __restrict__ sidx, const float* __restrict__ svals,
                                                          long long nnz, const long long* __restrict__ rowptr,
                                                          CooShape sh, int mode,
                                                          const __nv_bfloat16* const* __restrict__ Wbf,
@@ -255,23 +255,42 @@ __global__ void __launch_bounds__(256) k_coo_mttkrp_bf16(const int* __restrict__
   for (int row = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; row < d; row += warps) {
     const long long b = rowptr[row], e = rowptr[row + 1];
     Acc<float> acc[8];
-    for (long long k = b + slot; k < e; k += nslot) {
-      const float v = svals[k];
-      float p[8];
+    // two entries of the slot per pass, their coordinates and rows loaded
+    // together; the sums keep the slot's entry order
+    for (long long k = b + slot; k < e; k += 2 * nslot) {
+      float p[2][8];
 #pragma unroll
-      for (int j = 0; j < 8; ++j) p[j] = v;
+      for (int u = 0; u < 2; ++u) {
+        const long long kk = k + (long long)u * nslot;
+        const float v = kk < e ? svals[kk] : 0.f;
+#pragma unroll
+        for (int j = 0; j < 8; ++j) p[u][j] = v;
+      }
       for (int m = 0; m < sh.L; ++m) {
         if (m == mode) continue;
-        const uint4 raw = __ldg(reinterpret_cast<const uint4*>(Wbf[m] + (size_t)sidx[(size_t)m * nnz + k] * R + c0));
-        const uint32_t w4[4] = {raw.x, raw.y, raw.z, raw.w};
+        const int* im = sidx + (size_t)m * nnz;
+        int ix[2];
 #pragma unroll
-        for (int j = 0; j < 4; ++j) {
-          p[2 * j] *= __uint_as_float(w4[j] << 16);
-          p[2 * j + 1] *= __uint_as_float(w4[j] & 0xffff0000u);
+        for (int u = 0; u < 2; ++u) ix[u] = (k + (long long)u * nslot < e) ? im[k + (long long)u * nslot] : 0;
+        uint4 raw[2];
+#pragma unroll
+        for (int u = 0; u < 2; ++u)
+          raw[u] = __ldg(reinterpret_cast<const uint4*>(Wbf[m] + (size_t)ix[u] * R + c0));
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+          const uint32_t w4[4] = {raw[u].x, raw[u].y, raw[u].z, raw[u].w};
+#pragma unroll
+          for (int j = 0; j < 4; ++j) {
+            p[u][2 * j] *= __uint_as_float(w4[j] << 16);
+            p[u][2 * j + 1] *= __uint_as_float(w4[j] & 0xffff0000u);
+          }
         }
       }
 #pragma unroll
-      for (int j = 0; j < 8; ++j) acc[j].add(p[j]);
+      for (int u = 0; u < 2; ++u)
+        if (k + (long long)u * nslot < e)
+#pragma unroll
+          for (int j = 0; j < 8; ++j) acc[j].add(p[u][j]);
     }
 #pragma unroll
     for (int j = 0; j < 8; ++j) {

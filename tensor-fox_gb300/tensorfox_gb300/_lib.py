@@ -111,6 +111,7 @@ _EXTRA_SIGNATURES = {
     "tfx_dogleg_trial": [_I, _LL, _P, _P, _P, _D, _D, _D, _P, _P, _P, _P, _P],
     "tfx_step_sums": [_I, _LL, _P, _P, _P, _D, _P, _P, _P],
     "tfx_step_revert": [_I, _LL, _P, _P, _P, _P],
+    "tfx_step_update_wide": [_I, _I, POINTER(c_int), _I, _P, _P, _P, _P, _D, _P, _P, _SZ, _P],
     "tfx_mttkrp_tc": [_P, _I, POINTER(c_int), _I, _P, _I, _P, _I, _P, _SZ, _P, _P],
     "tfx_factors_bf16": [_I, POINTER(c_int), _I, _P, _P, _P, _P],
     "tfx_coo_mttkrp_bf16": [_P, _P, _LL, _P, _I, POINTER(c_int), _I, _I, _P, _P, _P, _P],
@@ -146,6 +147,7 @@ _SIZE_FUNCS = {
     "tfx_coo_dgn_cg_workspace_bytes": [_I, _I, POINTER(c_int), _I],
     "tfx_coo_model_error_scratch_bytes": [_I, _I],
     "tfx_dogleg_scratch_bytes": [],
+    "tfx_step_update_wide_scratch_bytes": [_I, POINTER(c_int), _I],
     "tfx_mttkrp_tc_scratch_bytes": [_I, POINTER(c_int), _I, _I],
 }
 

@@ -15,7 +15,8 @@ caller's MTTKRP provider, one host step per iteration:
    previous error evaluation);
 2. ``tfx_coo_dgn_cg``: Gramians, regularisation, preconditioner, gradient,
    J^T J grad and the preconditioned CG as one cooperative launch;
-3. ``tfx_dgn_step_update``: x += y, column balancing, ``transform``;
+3. ``tfx_step_update_wide``: x += y and column balancing over the whole
+   grid (``tfx_dgn_step_update``, one CTA, above rank 64);
 4. the mode-0 MTTKRP at the new factors and ``tfx_coo_model_error``;
 5. the host reads the iteration's scalars once and applies the gain ratio,
    damping, best-iterate and stop rules (shared with the stepped loop); after
@@ -98,6 +99,10 @@ def dgn_mttkrp(provider, dims, R, x0, options, precision, tnorm2, meanabs, error
     cgw = _Aligned(lib.tfx_coo_dgn_cg_workspace_bytes(dt, L, cd, int(R)), dev)
     errw = torch.empty(int(lib.tfx_coo_model_error_scratch_bytes(L, int(R))), dtype=torch.uint8, device=dev)
     dgw = torch.empty(int(lib.tfx_dogleg_scratch_bytes()), dtype=torch.uint8, device=dev)
+    # the whole-grid step update (rank <= 64); the one-CTA one otherwise
+    wide = R <= 64
+    upw = torch.empty(int(lib.tfx_step_update_wide_scratch_bytes(L, cd, int(R))) if wide else 1,
+                      dtype=torch.uint8, device=dev)
     sp = scal.data_ptr()
 
     def rows(src):
@@ -136,9 +141,13 @@ def dgn_mttkrp(provider, dims, R, x0, options, precision, tnorm2, meanabs, error
                   int(budgets[it]), ctypes.c_double(float(o.cg_tol)), _vp(y), _vp(grad), _vp(jtj),
                   ctypes.c_void_p(sp), ctypes.c_void_p(cgw.ptr), cgw.nbytes, st)
         x_prev.copy_(x)
-        _lib.call("tfx_dgn_step_update", dt, L, cd, int(R), _vp(x), _vp(W), _vp(y), _vp(grad),
-                  ctypes.c_double(damp), 0, 0, ctypes.c_double(0.0), 0, -1, None,
-                  ctypes.c_void_p(sp + 4 * 8), st)
+        if wide:
+            _lib.call("tfx_step_update_wide", dt, L, cd, int(R), _vp(x), _vp(W), _vp(y), _vp(grad),
+                      ctypes.c_double(damp), ctypes.c_void_p(sp + 4 * 8), _vp(upw), int(upw.numel()), st)
+        else:
+            _lib.call("tfx_dgn_step_update", dt, L, cd, int(R), _vp(x), _vp(W), _vp(y), _vp(grad),
+                      ctypes.c_double(damp), 0, 0, ctypes.c_double(0.0), 0, -1, None,
+                      ctypes.c_void_p(sp + 4 * 8), st)
         model_error(W)
         s = scal.cpu().numpy()
         if int(s[2]) != 0:

@@ -312,3 +312,37 @@ def test_direct_coo_precision_ladder_vs_fp64_oracle():
                                                   float(np.mean(np.abs(T))), ladder=True)
     assert mttkrp_dgn.dgn_mttkrp.low_iterations >= 1
     assert abs(min(er1) - min(er0)) <= 1e-3 * min(er0)
+
+
+@pytest.mark.parametrize("dims,R", [((5000, 3000, 70), 16), ((9, 8, 7, 6), 5), ((4100, 33, 2049), 64)])
+@pytest.mark.parametrize("dt", [torch.float64, torch.float32])
+def test_step_update_wide_matches_one_cta_update(dims, R, dt):
+    """The whole-grid step update against the one-CTA one (GaussNewton.py:284-297
+    with Conversion.py:361-387 balancing): the same rounded x, the same scalars
+    and the same balanced factors up to the order of the FP64 column sums."""
+    import ctypes
+    from tensorfox_gb300 import _dev, _lib
+    rng = np.random.default_rng(11)
+    n = R * sum(dims)
+    x0 = torch.from_numpy(rng.standard_normal(n)).to("cuda", dt)
+    y = torch.from_numpy(0.1 * rng.standard_normal(n)).cuda()
+    g = torch.from_numpy(rng.standard_normal(n)).cuda()
+    cd = (ctypes.c_int * len(dims))(*dims)
+    lib_dt = _dev.lib_dtype("fp64" if dt == torch.float64 else "fp32")
+    st = ctypes.c_void_p(_dev.stream())
+    vp = lambda t: ctypes.c_void_p(t.data_ptr())  # noqa: E731
+    xa, Wa, oa = x0.clone(), torch.empty_like(x0), torch.zeros(4, dtype=torch.float64, device="cuda")
+    _lib.call("tfx_dgn_step_update", lib_dt, len(dims), cd, R, vp(xa), vp(Wa), vp(y), vp(g), ctypes.c_double(0.3),
+              0, 0, ctypes.c_double(0.0), 0, -1, None, vp(oa), st)
+    xb, Wb, ob = x0.clone(), torch.empty_like(x0), torch.zeros(4, dtype=torch.float64, device="cuda")
+    nbytes = int(_lib.load().tfx_step_update_wide_scratch_bytes(len(dims), cd, R))
+    scr = torch.empty(nbytes, dtype=torch.uint8, device="cuda")
+    _lib.call("tfx_step_update_wide", lib_dt, len(dims), cd, R, vp(xb), vp(Wb), vp(y), vp(g), ctypes.c_double(0.3),
+              vp(ob), vp(scr), nbytes, st)
+    torch.cuda.synchronize()
+    assert torch.equal(xa, xb)
+    a, b = oa.cpu().numpy(), ob.cpu().numpy()
+    np.testing.assert_allclose(b[[0, 1, 3]], a[[0, 1, 3]], rtol=1e-12)
+    np.testing.assert_allclose(b[2], a[2], rtol=1e-9)      # a sum of terms of both signs
+    ulp = 1e-13 if dt == torch.float64 else 2 ** -23
+    np.testing.assert_allclose(Wb.double().cpu().numpy(), Wa.double().cpu().numpy(), rtol=2 * ulp, atol=0)
