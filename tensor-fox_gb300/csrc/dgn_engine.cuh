@@ -100,7 +100,7 @@ __host__ __device__ inline SmemPlan smem_plan(int TS, size_t es, int maxL, int m
   p.sB = o; o += al16((size_t)TFX_BK * (BN + 1) * es);
   p.sPart = o; o += al16((size_t)maxd * maxR * es);
   p.sAk = o; o += al16((size_t)maxL * maxR * maxncol * es);
-  p.sY = o; o += al16((size_t)maxL * maxR * maxncol * es);
+  p.sY = o; o += al16((size_t)maxL * maxR * ((maxncol + 3) & ~3) * es);
   p.sM = o; o += al16((size_t)maxL * maxncol * es);
   p.sDG = o; o += al16((size_t)maxL * maxncol * es);
   p.sGam = o; o += al16((size_t)maxL * maxncol * sizeof(double));
@@ -132,7 +132,7 @@ __host__ __device__ inline SmemPlan smem_plan(int TS, size_t es, int maxL, int m
   if (stage) {
     p.sQf = o; o += al16((size_t)maxnx * es);
     p.sWf = o; o += al16((size_t)maxnx * es);
-    p.sP1o = o; o += al16((size_t)maxL * maxR * maxncol * es);
+    p.sP1o = o; o += al16((size_t)maxL * maxR * ((maxncol + 3) & ~3) * es);
     p.sP2o = o; o += al16((size_t)maxL * maxL * maxR * maxncol * es);
     // the CTA's own slices of r, P, y, z and the expanded M, damp*Gamma
     const size_t own = (size_t)maxncol * (size_t)maxsumd;
@@ -186,6 +186,75 @@ __device__ __forceinline__ void stage_copy(T* sdst, const T* gsrc, int n) {
   for (int t = nv * V + threadIdx.x; t < n; t += TFX_THREADS) sdst[t] = __ldcg(gsrc + t);
 }
 
+// Two rows (dv0, dv1) of D_k against CN owned columns of W_k (column u at
+// wv + u dk): out[j][u] = sum_i dv_j[i] wv[u dk + i] as two chains, even and
+// odd i, added at the end.  V2: pairs of i as one 8- or 16-byte read (dk and
+// the offsets even).
+template <class T, int CN, bool V2>
+__device__ __forceinline__ void ak_tile(const int dk, const T* dv0, const T* dv1, const T* wv, T (&out)[2][4]) {
+  using T2 = typename std::conditional<sizeof(T) == 4, float2, double2>::type;
+  T ev[2][CN], od[2][CN];
+#pragma unroll
+  for (int u = 0; u < CN; ++u) ev[0][u] = ev[1][u] = od[0][u] = od[1][u] = T(0);
+  int i = 0;
+  if (V2) {
+#pragma unroll 2
+    for (; i < dk; i += 2) {
+      const T2 x0 = *reinterpret_cast<const T2*>(dv0 + i);
+      const T2 x1 = *reinterpret_cast<const T2*>(dv1 + i);
+#pragma unroll
+      for (int u = 0; u < CN; ++u) {
+        const T2 w = *reinterpret_cast<const T2*>(wv + u * dk + i);
+        ev[0][u] = fma((T)x0.x, (T)w.x, ev[0][u]);
+        od[0][u] = fma((T)x0.y, (T)w.y, od[0][u]);
+        ev[1][u] = fma((T)x1.x, (T)w.x, ev[1][u]);
+        od[1][u] = fma((T)x1.y, (T)w.y, od[1][u]);
+      }
+    }
+  } else {
+#pragma unroll 2
+    for (; i + 1 < dk; i += 2) {
+      const T x00 = dv0[i], x01 = dv0[i + 1], x10 = dv1[i], x11 = dv1[i + 1];
+#pragma unroll
+      for (int u = 0; u < CN; ++u) {
+        const T w0 = wv[u * dk + i], w1 = wv[u * dk + i + 1];
+        ev[0][u] = fma(x00, w0, ev[0][u]);
+        od[0][u] = fma(x01, w1, od[0][u]);
+        ev[1][u] = fma(x10, w0, ev[1][u]);
+        od[1][u] = fma(x11, w1, od[1][u]);
+      }
+    }
+    if (i < dk) {
+#pragma unroll
+      for (int u = 0; u < CN; ++u) {
+        ev[0][u] = fma(dv0[i], wv[u * dk + i], ev[0][u]);
+        ev[1][u] = fma(dv1[i], wv[u * dk + i], ev[1][u]);
+      }
+    }
+  }
+#pragma unroll
+  for (int u = 0; u < CN; ++u) {
+    out[0][u] = ev[0][u] + od[0][u];
+    out[1][u] = ev[1][u] + od[1][u];
+  }
+}
+
+// z rows of CN owned columns (the scalar-load path of the matvec's last pass):
+// a1[u] += W_l[i, r] Y_l[r, u], a2[u] += D_l[i, r] P1_l[r, u], r ascending
+template <class T, int CN>
+__device__ __forceinline__ void z_cols(const int R, const int dl, const T* wrow, const T* drow, const T* yc,
+                                       const int ys, const T* p1c, const int p1s, T (&a1)[4], T (&a2)[4]) {
+#pragma unroll 4
+  for (int r = 0; r < R; ++r) {
+    const T w = wrow[r * dl], dd = drow[r * dl];
+#pragma unroll
+    for (int u = 0; u < CN; ++u) {
+      a1[u] = fma(w, yc[r * ys + u], a1[u]);
+      a2[u] = fma(dd, p1c[r * p1s + u], a2[u]);
+    }
+  }
+}
+
 template <class T, bool STAGED>
 __device__ __forceinline__ void cg_matvec(const int L, const int R, const int nx, const int ncol, const int c0,
                                           const CgOffsets so, const T* Dglob, T* zout, const T* Wg, const T* P1g,
@@ -225,26 +294,44 @@ __device__ __forceinline__ void cg_matvec(const int L, const int R, const int nx
   const T* sP1o = (const T*)(sm + so.sP1o);
   const T* sP2o = (const T*)(sm + so.sP2o);
   const int RN = R * ncol;
-  // A_k = D_k^T W_k on the owned columns, one output per thread item; the
-  // dot runs as two interleaved chains so that loads overlap the FMAs
-  const int ncg = (ncol + 3) >> 2;
-  for (int e = tid; e < L * RN; e += TFX_THREADS) {
-    const int k = e / RN, q = e - k * RN, a = q / ncol, c = q - a * ncol;
-    const int dk = d[k];
-    const T* dv = Din + off[k] + a * dk;
-    const T* wv = Wr + off[k] + (c0 + c) * dk;
-    T acc0 = T(0), acc1 = T(0);
-    int i = 0;
-#pragma unroll 4
-    for (; i + 1 < dk; i += 2) {
-      acc0 = fma(dv[i], wv[i], acc0);
-      acc1 = fma(dv[i + 1], wv[i + 1], acc1);
+  // A_k = D_k^T W_k on the owned columns: a thread takes rows a and a + RP of
+  // D_k and up to four owned columns, so that every loaded value feeds two or
+  // more multiply-adds (the pass is bound by shared-memory wavefronts); each
+  // dot keeps its two interleaved chains (even and odd i), as one output per
+  // thread would.
+  {
+    const int RP = (R + 1) >> 1, ncg4 = (ncol + 3) >> 2;
+    for (int e = tid; e < L * ncg4 * RP; e += TFX_THREADS) {
+      const int k = e / (ncg4 * RP), rem = e - k * ncg4 * RP, cg = rem / RP, ap = rem - cg * RP;
+      const int a0 = ap, a1 = ap + RP < R ? ap + RP : ap;
+      const int dk = d[k], cb = cg * 4, cn = min(4, ncol - cb);
+      const T* dv0 = Din + off[k] + a0 * dk;
+      const T* dv1 = Din + off[k] + a1 * dk;
+      const T* wv = Wr + off[k] + (c0 + cb) * dk;
+      const bool v2 = ((dk | off[k]) & 1) == 0 &&
+                      (((unsigned long long)Din | (unsigned long long)Wr) & (2 * sizeof(T) - 1)) == 0;
+      T out[2][4];
+      switch (cn) {
+        case 1: v2 ? ak_tile<T, 1, true>(dk, dv0, dv1, wv, out) : ak_tile<T, 1, false>(dk, dv0, dv1, wv, out); break;
+        case 2: v2 ? ak_tile<T, 2, true>(dk, dv0, dv1, wv, out) : ak_tile<T, 2, false>(dk, dv0, dv1, wv, out); break;
+        case 3: v2 ? ak_tile<T, 3, true>(dk, dv0, dv1, wv, out) : ak_tile<T, 3, false>(dk, dv0, dv1, wv, out); break;
+        default: v2 ? ak_tile<T, 4, true>(dk, dv0, dv1, wv, out) : ak_tile<T, 4, false>(dk, dv0, dv1, wv, out); break;
+      }
+      T* o0 = sAk + (size_t)k * RN + a0 * ncol + cb;
+      T* o1 = sAk + (size_t)k * RN + a1 * ncol + cb;
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+        if (u < cn) {
+          o0[u] = out[0][u];
+          if (a1 != a0) o1[u] = out[1][u];
+        }
     }
-    if (i < dk) acc0 = fma(dv[i], wv[i], acc0);
-    sAk[e] = acc0 + acc1;
   }
   __syncthreads();
   ctick(2);
+  // Y_l (rows of stride ncp, the owned column count rounded up to four, so
+  // that the last pass reads four columns at once), one output per thread
+  const int ncp = (ncol + 3) & ~3;
   for (int e = tid; e < L * RN; e += TFX_THREADS) {
     const int l = e / RN, q = e - l * RN, a = q / ncol, c = q - a * ncol;
     T acc = T(0);
@@ -254,13 +341,14 @@ __device__ __forceinline__ void cg_matvec(const int L, const int R, const int nx
                           : P2g[((size_t)(l * L + k) * R + a) * R + c0 + c];
       acc += p2 * sAk[(size_t)k * RN + q];
     }
-    sY[e] = acc;
+    sY[((size_t)l * R + a) * ncp + c] = acc;
   }
   __syncthreads();
   ctick(3);
   // z_l = W_l Y_l + D_l P1_l over all owned outputs of all modes at once;
   // a thread takes one row i of one mode and four owned columns
   const int sumd = nx / R;
+  const int ncg = (ncol + 3) >> 2;
   for (int e = tid; e < ncg * sumd; e += TFX_THREADS) {
     const int cgi = e / sumd;
     int l = 0, i = e - cgi * sumd;
@@ -272,16 +360,17 @@ __device__ __forceinline__ void cg_matvec(const int L, const int R, const int nx
     const int dl = d[l], ol = off[l];
     const T* wrow = Wr + ol + i;
     const T* drow = Din + ol + i;
-    const T* yc = sY + (size_t)l * RN + cb;
-    const T* p1c = STAGED ? sP1o + (size_t)l * R * ncol + cb : P1g + (size_t)l * R * R + c0 + cb;
-    const int p1s = STAGED ? ncol : R;
+    const T* yc = sY + (size_t)l * R * ncp + cb;
+    const T* p1c = STAGED ? sP1o + (size_t)l * R * ncp + cb : P1g + (size_t)l * R * R + c0 + cb;
+    const int p1s = STAGED ? ncp : R;
     T a1[4] = {T(0), T(0), T(0), T(0)}, a2[4] = {T(0), T(0), T(0), T(0)};
-    if (sizeof(T) == 4 && STAGED && (ncol & 3) == 0) {
-      // four owned columns as one 16-byte read of Y and of P1 per r
+    if (sizeof(T) == 4 && STAGED) {
+      // four owned columns as one 16-byte read of Y and of P1 per r (a
+      // partial last group computes the padding columns and drops them)
 #pragma unroll 4
       for (int r = 0; r < R; ++r) {
         const T w = wrow[r * dl], dd = drow[r * dl];
-        const float4 y4 = *reinterpret_cast<const float4*>(yc + r * ncol);
+        const float4 y4 = *reinterpret_cast<const float4*>(yc + r * ncp);
         const float4 p4 = *reinterpret_cast<const float4*>(p1c + r * p1s);
         a1[0] = fma(w, (T)y4.x, a1[0]);
         a1[1] = fma(w, (T)y4.y, a1[1]);
@@ -293,15 +382,11 @@ __device__ __forceinline__ void cg_matvec(const int L, const int R, const int nx
         a2[3] = fma(dd, (T)p4.w, a2[3]);
       }
     } else {
-#pragma unroll 2
-      for (int r = 0; r < R; ++r) {
-        const T w = wrow[r * dl], dd = drow[r * dl];
-#pragma unroll
-        for (int u = 0; u < 4; ++u)
-          if (u < cn) {
-            a1[u] = fma(w, yc[r * ncol + u], a1[u]);
-            a2[u] = fma(dd, p1c[r * p1s + u], a2[u]);
-          }
+      switch (cn) {
+        case 1: z_cols<T, 1>(R, dl, wrow, drow, yc, ncp, p1c, p1s, a1, a2); break;
+        case 2: z_cols<T, 2>(R, dl, wrow, drow, yc, ncp, p1c, p1s, a1, a2); break;
+        case 3: z_cols<T, 3>(R, dl, wrow, drow, yc, ncp, p1c, p1s, a1, a2); break;
+        default: z_cols<T, 4>(R, dl, wrow, drow, yc, ncp, p1c, p1s, a1, a2); break;
       }
     }
 #pragma unroll
@@ -397,7 +482,9 @@ __device__ __forceinline__ int cg_team(const Team tm, const int L, const int R, 
     // Q = M P on the owned slice.  Staged: pushed straight into every team
     // member's shared-memory copy of the full vector (their previous reads of
     // it ended before the last team barrier); otherwise published through
-    // global memory.
+    // global memory.  (Measured alternatives: publishing through global
+    // memory and copying the full vector back from L2, by threads or by one
+    // multicast bulk copy, take as long as the push.)
     for (int l = 0; l < L; ++l) {
       const int dl = d[l], base = off[l] + c0 * dl, n = ncol * dl, lb = ncol * (off[l] / R);
       for (int e = tid; e < n; e += TFX_THREADS) {
@@ -410,6 +497,7 @@ __device__ __forceinline__ int cg_team(const Team tm, const int L, const int R, 
         }
       }
     }
+    ctick(1);
     tm.sync();
     ctick(0);
     cg_matvec<T, STAGED>(L, R, nx, ncol, c0, so, Q, z, Wg, P1g, P2g, STAGED ? vz : nullptr, cprof, STAGED);
@@ -588,7 +676,7 @@ struct Engine {
   const T* Wr;  // factors to read: shared-memory copy when staged
 
   __device__ __forceinline__ T& P1at(int l, int a, int c) {
-    return stage ? sP1o[((size_t)l * R + a) * ncol + c] : P1[((size_t)l * R + a) * R + c0 + c];
+    return stage ? sP1o[((size_t)l * R + a) * ((ncol + 3) & ~3) + c] : P1[((size_t)l * R + a) * R + c0 + c];
   }
   __device__ __forceinline__ T& P2at(int l, int k, int a, int c) {
     return stage ? sP2o[((size_t)(l * L + k) * R + a) * ncol + c] : P2[((size_t)(l * L + k) * R + a) * R + c0 + c];
@@ -757,7 +845,7 @@ struct Engine {
   // Needs every mode <= 64, d1*d2 % 4 == 0 and a 16-byte aligned tensor.
   // -------------------------------------------------------------------------
   template <bool STAGED>
-  __device__ void gradient_l3() {
+  __device__ __noinline__ void gradient_l3() {
     long long gt = gprof ? clock64() : 0;
     auto gtick = [&](int ph) {
       if (gprof) {
@@ -773,7 +861,7 @@ struct Engine {
     char* smb = dyn_smem();
     const T* Wl = STAGED ? (const T*)(smb + cgo.sWf) : W;
     const T* P1l = STAGED ? (const T*)(smb + cgo.sP1o) : P1;
-    const int p1s = STAGED ? ncol : R;  // P1 column stride
+    const int p1s = STAGED ? ((ncol + 3) & ~3) : R;  // P1 column stride
     const int p1c = STAGED ? 0 : c0;    // P1 column offset
     const int SL = (int)g3_stage(d1, d2);
     T* sT = (T*)(smb + g3off);                 // 3 stages
@@ -1007,7 +1095,7 @@ struct Engine {
   }
 
   template <bool STAGED>
-  __device__ void gradient_l3s() {
+  __device__ __noinline__ void gradient_l3s() {
     long long gt = gprof ? clock64() : 0;
     auto gtick = [&](int ph) {
       if (gprof) {
@@ -1021,7 +1109,7 @@ struct Engine {
     char* smb = dyn_smem();
     const T* Wl = STAGED ? (const T*)(smb + cgo.sWf) : W;
     const T* P1l = STAGED ? (const T*)(smb + cgo.sP1o) : P1;
-    const int p1s = STAGED ? ncol : R;  // P1 column stride
+    const int p1s = STAGED ? ((ncol + 3) & ~3) : R;  // P1 column stride
     const int p1c = STAGED ? 0 : c0;    // P1 column offset
     const int SL = (int)g3_stage(d1, d2);
     T* sT = (T*)(smb + g3off);  // 3 stages, then the M1 | M2 partials (64 columns a row)
