@@ -25,7 +25,7 @@
 namespace tfx {
 namespace rtc {
 
-constexpr int BM = 128, BN = 256, KP = 64, NT = 256;
+constexpr int BM = 128, BN = 256, KP = 64, NT = 256, BU = 8;
 constexpr uint32_t SPIN = 1u << 26;
 
 __device__ __forceinline__ uint32_t su32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -34,6 +34,16 @@ __device__ __forceinline__ uint32_t su32(const void* p) { return (uint32_t)__cvt
 // groups 1024 bytes apart, 16-byte chunk c stored at c ^ (r % 8)
 __device__ __forceinline__ uint32_t sw_off(int r, int k) {
   return (uint32_t)(r * 128 + ((((k >> 2) ^ (r & 7)) & 7) << 4) + ((k & 3) << 2));
+}
+
+// entry e of an operand tile (rows x KP ranks) -> (row n, rank k): lane bits
+// 0-2 are the row within 8, bits 3-4 the rank within 4, then rank groups of
+// four, then row groups of eight (KP % 4 == 0)
+__device__ __forceinline__ void tile_nk(int e, int& n, int& k) {
+  const int blk = e >> 5;
+  const int kb = blk % (KP / 4), nb = blk / (KP / 4);
+  n = nb * 8 + (e & 7);
+  k = kb * 4 + ((e >> 3) & 3);
 }
 
 __device__ __forceinline__ uint64_t desc(const void* tile) {
@@ -115,32 +125,83 @@ __global__ void __launch_bounds__(NT, 1) k_residual_tc(const float* __restrict__
   uint32_t phase = 0;
   for (int cb = blockIdx.x; cb < ncb; cb += gridDim.x) {
     const long long q0 = (long long)cb * BN;
-    // Khatri-Rao rows of the column block: hi and lo parts
-    for (int e = tid; e < BN * KP; e += NT) {
-      const int n = e / KP, k = e - n * KP;
-      const long long q = q0 + n;
-      float v = 0.f;
-      if (k < R && q < Q0) {
-        // Q0 < 2^31 (checked on the host): 32-bit division
-        const unsigned qq = (unsigned)q;
-        const unsigned j = qq / (unsigned)d2, kk = qq - j * (unsigned)d2;
-        v = sh.W1[(size_t)k * sh.d1 + j] * sh.W2[(size_t)k * d2 + kk];
+    // Khatri-Rao rows of the column block: hi and lo parts.  Eight entries
+    // a pass, their factor loads issued together (the loads come from L2);
+    // a warp covers 8 columns x 4 ranks, so that its loads of W2 are four
+    // 32-byte runs and its swizzled stores hit 32 distinct banks.
+    for (int e0 = tid; e0 < BN * KP; e0 += NT * BU) {
+      float f1[BU], f2[BU];
+#pragma unroll
+      for (int u = 0; u < BU; ++u) {
+        const int e = e0 + u * NT;
+        int n, k;
+        tile_nk(e, n, k);
+        const long long q = q0 + n;
+        f1[u] = 0.f;
+        f2[u] = 0.f;
+        if (e < BN * KP && k < R && q < Q0) {
+          // Q0 < 2^31 (checked on the host): 32-bit division
+          const unsigned qq = (unsigned)q;
+          const unsigned j = qq / (unsigned)d2, kk = qq - j * (unsigned)d2;
+          f1[u] = __ldg(sh.W1 + (size_t)k * sh.d1 + j);
+          f2[u] = __ldg(sh.W2 + (size_t)k * d2 + kk);
+        }
       }
-      const float h = tf32_hi(v);
-      const uint32_t o = sw_off(n, k & 31);
-      *(float*)(S.bhi[k >> 5] + o) = h;
-      *(float*)(S.blo[k >> 5] + o) = v - h;
+#pragma unroll
+      for (int u = 0; u < BU; ++u) {
+        const int e = e0 + u * NT;
+        if (e < BN * KP) {
+          int n, k;
+          tile_nk(e, n, k);
+          const float v = f1[u] * f2[u];
+          const float h = tf32_hi(v);
+          const uint32_t o = sw_off(n, k & 31);
+          *(float*)(S.bhi[k >> 5] + o) = h;
+          *(float*)(S.blo[k >> 5] + o) = v - h;
+        }
+      }
     }
     for (int ib = 0; ib < nib; ++ib) {
       const int i0 = ib * BM;
-      for (int e = tid; e < BM * KP; e += NT) {
-        const int m = e / KP, k = e - m * KP;
-        const int i = i0 + m;
-        const float v = (k < R && i < d0) ? sh.W0[(size_t)k * d0 + i] : 0.f;
-        const float h = tf32_hi(v);
-        const uint32_t o = sw_off(m, k & 31);
-        *(float*)(S.ahi[k >> 5] + o) = h;
-        *(float*)(S.alo[k >> 5] + o) = v - h;
+      // the thread's 128 tensor values of this tile (row 32 (warp % 4) + lane,
+      // columns (warp / 4) 128 ..), loaded before the operands are formed and
+      // the products issued, so that the whole tile is in flight meanwhile
+      const int erow = 32 * (warp & 3) + lane;
+      const int ei = i0 + erow;
+      const int ech = (warp >> 2) * (BN / 2);
+      const long long eqb = q0 + ech;
+      const bool efull = ei < d0 && eqb + BN / 2 <= Q0;
+      float4 tv[BN / 8];
+      if (efull) {
+        const float4* t4 = reinterpret_cast<const float4*>(T + (size_t)ei * Q0 + eqb);
+#pragma unroll
+        for (int u = 0; u < BN / 8; ++u) tv[u] = __ldcs(t4 + u);
+      }
+      // W0's rows of the block, eight entries a pass with their loads issued
+      // together (the shared-memory stores go through a generic pointer, so
+      // the compiler would not move later loads above them)
+      for (int e0 = tid; e0 < BM * KP; e0 += NT * BU) {
+        float f[BU];
+#pragma unroll
+        for (int u = 0; u < BU; ++u) {
+          const int e = e0 + u * NT;
+          int m, k;
+          tile_nk(e, m, k);
+          const int i = i0 + m;
+          f[u] = (e < BM * KP && k < R && i < d0) ? __ldg(sh.W0 + (size_t)k * d0 + i) : 0.f;
+        }
+#pragma unroll
+        for (int u = 0; u < BU; ++u) {
+          const int e = e0 + u * NT;
+          if (e < BM * KP) {
+            int m, k;
+            tile_nk(e, m, k);
+            const float h = tf32_hi(f[u]);
+            const uint32_t o = sw_off(m, k & 31);
+            *(float*)(S.ahi[k >> 5] + o) = h;
+            *(float*)(S.alo[k >> 5] + o) = f[u] - h;
+          }
+        }
       }
       // generic-proxy writes -> visible to the tensor core's async proxy
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -175,22 +236,10 @@ __global__ void __launch_bounds__(NT, 1) k_residual_tc(const float* __restrict__
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
       if (!*(volatile int*)&S.abort) {
         // warp w: TMEM lanes 32*(w % 4) .. +31 (rows), columns half w / 4
-        const int row = 32 * (warp & 3) + lane;
-        const int i = i0 + row;
-        const int ch = (warp >> 2) * (BN / 2);
-#pragma unroll 1
-        for (int cc = 0; cc < BN / 2; cc += 32) {
-          // the tensor values first: their loads overlap the TMEM read
-          float4 tv[8];
-          const long long qb = q0 + ch + cc;
-          const bool full = i < d0 && qb + 32 <= Q0;
-          if (full) {
-            const float4* t4 = reinterpret_cast<const float4*>(T + (size_t)i * Q0 + qb);
 #pragma unroll
-            for (int u = 0; u < 8; ++u) tv[u] = __ldcs(t4 + u);
-          }
+        for (int cc = 0; cc < BN / 2; cc += 32) {
           uint32_t v[32];
-          const uint32_t taddr = tmem + ((uint32_t)(32 * (warp & 3)) << 16) + (uint32_t)(ch + cc);
+          const uint32_t taddr = tmem + ((uint32_t)(32 * (warp & 3)) << 16) + (uint32_t)(ech + cc);
           asm volatile(
               "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
               "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
@@ -201,17 +250,19 @@ __global__ void __launch_bounds__(NT, 1) k_residual_tc(const float* __restrict__
                 "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
               : "r"(taddr));
           asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-          if (full) {
+          const long long qb = eqb + cc;
+          if (efull) {
 #pragma unroll
             for (int u = 0; u < 8; ++u) {
+              const float4 t = tv[cc / 4 + u];
               float df;
-              df = tv[u].x - __uint_as_float(v[4 * u + 0]); acc[0].fma_(df, df);
-              df = tv[u].y - __uint_as_float(v[4 * u + 1]); acc[1].fma_(df, df);
-              df = tv[u].z - __uint_as_float(v[4 * u + 2]); acc[2].fma_(df, df);
-              df = tv[u].w - __uint_as_float(v[4 * u + 3]); acc[3].fma_(df, df);
+              df = t.x - __uint_as_float(v[4 * u + 0]); acc[0].fma_(df, df);
+              df = t.y - __uint_as_float(v[4 * u + 1]); acc[1].fma_(df, df);
+              df = t.z - __uint_as_float(v[4 * u + 2]); acc[2].fma_(df, df);
+              df = t.w - __uint_as_float(v[4 * u + 3]); acc[3].fma_(df, df);
             }
-          } else if (i < d0) {
-            const float* trow = T + (size_t)i * Q0 + qb;
+          } else if (ei < d0) {
+            const float* trow = T + (size_t)ei * Q0 + qb;
             for (int u = 0; u < 32; ++u)
               if (qb + u < Q0) {
                 const float df = trow[u] - __uint_as_float(v[u]);
