@@ -17,10 +17,12 @@
 //   * warp 0 (producer) brings the two 128 x 32 tensor tiles of a chunk by TMA
 //     (3-D map over (q, d, p), SWIZZLE_128B) into a two-stage ring, a stage
 //     being refilled as soon as the products that read it have completed;
-//   * warps 2-7 split every tile value x into x_hi = x with its 13 low
-//     mantissa bits cleared (exact in TF32) and x_lo = x - x_hi, and form the
-//     chunk's B operand (64 x 32, K-major, SWIZZLE_128B) the same way from the
-//     factor rows, and arrive on the stage's "formed" mbarrier;
+//   * warps 2-7 form the chunk's B operand (64 x 32, K-major, SWIZZLE_128B)
+//     from the factor rows as soon as the stage's previous products are done
+//     (while the tensor tiles are still in flight), then split every tile
+//     value x into x_hi = x with its 13 low mantissa bits cleared (exact in
+//     TF32) and x_lo = x - x_hi, B the same way, and arrive on the stage's
+//     "formed" mbarrier;
 //   * warp 1 issues tcgen05.mma kind::tf32 (M = 128, N = 64, K = 8):
 //     A_hi B_hi + A_hi B_lo + A_lo B_hi per tile, FP32 accumulation in TMEM,
 //     so the product keeps FP32 accuracy (3xTF32), and commits to the stage's
@@ -218,32 +220,20 @@ __global__ void __launch_bounds__(NT, 1)
       }
     }
   } else {
-    // converters (warps 2..7): split the tiles, form B, hand the stage over
+    // converters (warps 2..7): form B, split the tiles, hand the stage over.
+    // B does not depend on the tensor tile: it is formed as soon as the
+    // stage's previous products (chunk c - 2) have completed, while the
+    // chunk's TMA copy is still in flight.
     const int ct = tid - 64;
     for (int c = 0; c < n; ++c) {
       const int s = c & 1;
-      if (!wait_bar(&S.full[s], (uint32_t)(c >> 1) & 1u)) {
+      if (c >= 2 && !wait_bar(&S.done[s], (uint32_t)((c - 2) >> 1) & 1u)) {
         if (lane == 0) {
-          atomicExch(err, 1);
+          atomicExch(err, 6);
           S.abort = 1;
         }
       }
       if (*(volatile int*)&S.abort) break;
-      // A: hi in place, lo beside it (element-wise: the layout is the same)
-      {
-        float4* a4 = reinterpret_cast<float4*>(&S.a[s][0][0]);
-        float4* l4 = reinterpret_cast<float4*>(&S.alo[s][0][0]);
-        for (int e = ct; e < NTILE * BM * BK / 4; e += NCW * 32) {
-          const float4 v = a4[e];
-          float4 h, lo;
-          h.x = hi13(v.x); lo.x = v.x - h.x;
-          h.y = hi13(v.y); lo.y = v.y - h.y;
-          h.z = hi13(v.z); lo.z = v.z - h.z;
-          h.w = hi13(v.w); lo.w = v.w - h.w;
-          a4[e] = h;
-          l4[e] = lo;
-        }
-      }
       // B: 64 x 32, B[r][q] = before_p[r] * after_{q0+q}[r].  A thread takes
       // one q (its lane) and the ranks r = (warp - 2) + 6 u; the indices of p
       // and q are decomposed once per chunk (32-bit: P, Q < 2^31) into
@@ -300,6 +290,28 @@ __global__ void __launch_bounds__(NT, 1)
             *(float*)(S.bhi[s] + o) = h;
             *(float*)(S.blo[s] + o) = v[u] - h;
           }
+        }
+      }
+      if (!wait_bar(&S.full[s], (uint32_t)(c >> 1) & 1u)) {
+        if (lane == 0) {
+          atomicExch(err, 1);
+          S.abort = 1;
+        }
+      }
+      if (*(volatile int*)&S.abort) break;
+      // A: hi in place, lo beside it (element-wise: the layout is the same)
+      {
+        float4* a4 = reinterpret_cast<float4*>(&S.a[s][0][0]);
+        float4* l4 = reinterpret_cast<float4*>(&S.alo[s][0][0]);
+        for (int e = ct; e < NTILE * BM * BK / 4; e += NCW * 32) {
+          const float4 v = a4[e];
+          float4 h, lo;
+          h.x = hi13(v.x); lo.x = v.x - h.x;
+          h.y = hi13(v.y); lo.y = v.y - h.y;
+          h.z = hi13(v.z); lo.z = v.z - h.z;
+          h.w = hi13(v.w); lo.w = v.w - h.w;
+          a4[e] = h;
+          l4[e] = lo;
         }
       }
       // generic-proxy writes -> visible to the tensor core's async proxy; one
