@@ -906,6 +906,69 @@ extern "C" int tfx_mode_gram(int dtype, const void* S, long long P, int D, long 
   return check_launch("gram_reduce");
 }
 
+// ---------------------------------------------------------------------------
+// C = alpha A B + beta C for a short left factor (M <= 64 rows) and a long K:
+// the eigen-step's products (60 x 512 by 512 x 512, 60 x 512 by 512 x 60).  A
+// CTA owns SK_NB columns of C and every row; its 256 threads are 64 rows x 4
+// quarters of each K chunk, each accumulating SK_NB outputs, and the four
+// quarter sums are added in a fixed order at the end.  One output per thread
+// over all of K (the general kernel's smallest tile) leaves a 512-long
+// dependent chain per thread.
+// ---------------------------------------------------------------------------
+#define SK_NB 16
+#define SK_KC 128
+
+template <class T>
+__global__ void __launch_bounds__(256) k_gemm_skinny(const T* __restrict__ A, const T* __restrict__ B, T* C,
+                                                     GemmArgs g) {
+  extern __shared__ __align__(16) char sk_smem[];
+  T* As = (T*)sk_smem;                         // [64][SK_KC + 1]
+  T* Bs = As + 64 * (SK_KC + 1);               // [SK_KC][SK_NB]
+  T* red = Bs + SK_KC * SK_NB;                 // [4][64][SK_NB]
+  const int tid = threadIdx.x, row = tid & 63, kq = tid >> 6;
+  const long long n0 = (long long)blockIdx.x * SK_NB;
+  const int M = (int)g.M;
+  T acc[SK_NB];
+#pragma unroll
+  for (int j = 0; j < SK_NB; ++j) acc[j] = T(0);
+  for (long long k0 = 0; k0 < g.K; k0 += SK_KC) {
+    const int kc = (int)(g.K - k0 < SK_KC ? g.K - k0 : SK_KC);
+    __syncthreads();  // the previous chunk is consumed
+    for (int e = tid; e < 64 * SK_KC; e += 256) {
+      const int m = e / SK_KC, k = e - m * SK_KC;
+      As[m * (SK_KC + 1) + k] = (m < M && k < kc) ? A[m * g.sAm + (k0 + k) * g.sAk] : T(0);
+    }
+    for (int e = tid; e < SK_KC * SK_NB; e += 256) {
+      const int k = e / SK_NB, j = e - k * SK_NB;
+      Bs[e] = (k < kc && n0 + j < g.N) ? B[(k0 + k) * g.sBk + (n0 + j) * g.sBn] : T(0);
+    }
+    __syncthreads();
+    const T* ar = As + row * (SK_KC + 1) + kq * (SK_KC / 4);
+    const T* br = Bs + kq * (SK_KC / 4) * SK_NB;
+#pragma unroll 4
+    for (int kk = 0; kk < SK_KC / 4; ++kk) {
+      const T a = ar[kk];
+#pragma unroll
+      for (int j = 0; j < SK_NB; ++j) acc[j] = fma(a, br[kk * SK_NB + j], acc[j]);
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < SK_NB; ++j) red[(kq * 64 + row) * SK_NB + j] = acc[j];
+  __syncthreads();
+  for (int e = tid; e < 64 * SK_NB; e += 256) {
+    const int m = e / SK_NB, j = e - m * SK_NB;
+    if (m >= M || n0 + j >= g.N) continue;
+    const T v = ((red[m * SK_NB + j] + red[(64 + m) * SK_NB + j]) + red[(128 + m) * SK_NB + j]) +
+                red[(192 + m) * SK_NB + j];
+    T* c = C + m * g.sCm + (n0 + j) * g.sCn;
+    *c = g.beta != 0.0 ? (T)(g.alpha * (double)v + g.beta * (double)*c) : (T)(g.alpha * (double)v);
+  }
+}
+
+static size_t skinny_smem(size_t es) {
+  return (size_t)(64 * (SK_KC + 1) + SK_KC * SK_NB + 4 * 64 * SK_NB) * es;
+}
+
 extern "C" int tfx_gemm(int dtype, const void* A, const void* B, void* C, long long M, long long N, long long K,
                         long long batch, const long long* strides /* sAb sAm sAk sBb sBk sBn sCb sCm sCn */,
                         double alpha, double beta, void* stream) {
@@ -928,6 +991,21 @@ extern "C" int tfx_gemm(int dtype, const void* A, const void* B, void* C, long l
   g.alpha = alpha;
   g.beta = beta;
   cudaStream_t st = (cudaStream_t)stream;
+  if (batch == 1 && M <= 64 && K >= 32 && N <= 65535LL * SK_NB) {
+    const size_t sm = skinny_smem(dtype == TFX_F32 ? 4 : 8);
+    const unsigned grid = (unsigned)((N + SK_NB - 1) / SK_NB);
+    cudaError_t e;
+    if (dtype == TFX_F32) {
+      e = cudaFuncSetAttribute(k_gemm_skinny<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+      if (e != cudaSuccess) return tfx_set_cuda_error(e, "gemm_skinny smem");
+      k_gemm_skinny<float><<<grid, 256, sm, st>>>((const float*)A, (const float*)B, (float*)C, g);
+    } else {
+      e = cudaFuncSetAttribute(k_gemm_skinny<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+      if (e != cudaSuccess) return tfx_set_cuda_error(e, "gemm_skinny smem");
+      k_gemm_skinny<double><<<grid, 256, sm, st>>>((const double*)A, (const double*)B, (double*)C, g);
+    }
+    return check_launch("gemm_skinny");
+  }
   // smaller tiles when the output is too small to fill the GPU with 64x64 tiles
   int ts = 4;
   const long long by = std::min<long long>(batch, 65535);
