@@ -627,6 +627,10 @@ __global__ void __launch_bounds__(512) k_jacobi(const T* __restrict__ Ain, int n
   int* pr = (int*)(cs + m);    // pairs
   double* red = (double*)(pr + m + 2);
   unsigned* blk = (unsigned*)(red + 2);  // (m/2)(m/2+1)/2 block indices
+  const int hb = m / 2;
+  // the second parameter slot of the pipelined sweep: c, s then the pairs
+  T* cs2 = (T*)(((uintptr_t)(blk + hb * (hb + 1) / 2) + 15) & ~(uintptr_t)15);
+  int* pr2 = (int*)(cs2 + m);
   const int tid = threadIdx.x;
   for (int e = tid; e < m * m; e += blockDim.x) {
     const int i = e / m, j = e - i * m;
@@ -635,7 +639,7 @@ __global__ void __launch_bounds__(512) k_jacobi(const T* __restrict__ Ain, int n
     Vs[e] = (i == j) ? T(1) : T(0);
   }
   __syncthreads();
-  const int sweep = cta_jacobi<T>(A, Vs, cs, pr, red, m, max_sweeps, blk);
+  const int sweep = cta_jacobi<T>(A, Vs, cs, pr, red, m, max_sweeps, blk, cs2, pr2);
   // sort eigenvalues (descending) with their vectors
   for (int i = tid; i < n; i += blockDim.x) {
     const int rank = eig_rank<T>(A, m, n, i);
@@ -1120,7 +1124,8 @@ extern "C" size_t tfx_sym_eig_smem_bytes(int dtype, int n) {
   size_t b = 2 * (size_t)m * m * es + (size_t)m * es + (size_t)(m + 2) * sizeof(int);
   b = (b + 15) & ~(size_t)15;
   const size_t h = (size_t)m / 2;
-  return b + 2 * (TFX_THREADS / 32) * sizeof(double) + h * (h + 1) / 2 * sizeof(unsigned);
+  return b + 2 * (TFX_THREADS / 32) * sizeof(double) + h * (h + 1) / 2 * sizeof(unsigned) + 16 + (size_t)m * es +
+         (size_t)(m + 2) * sizeof(int);
 }
 
 extern "C" int tfx_sym_eig(int dtype, const void* A, int n, void* evals, void* V, int max_sweeps, int* sweeps,
