@@ -155,6 +155,15 @@ int tfx_gemm(int dtype, const void* A, const void* B, void* C, long long M, long
  * tfx_gemm. */
 int tfx_ttm(int dtype, const void* S, long long P, int D, long long Q, const void* Ut, int n, void* out,
             void* stream);
+/* The same product on the tensor cores for precision 'mixed' (3xTF32: both
+ * operands split hi + lo, FP32 accumulation; Compression.py:123-137's
+ * truncation): FP32 S (P, D, Q) and Ut (n x D), both 16-byte aligned, out
+ * (P, n, Q); D % 32 == 0, n <= 64, Q >= 128, Q % 4 == 0 (tfx_ttm_tc_supported), else
+ * TFX_STATUS_ERR_UNSUPPORTED.  err: device int, non-zero when a bounded wait
+ * ran out. */
+int tfx_ttm_tc_supported(long long P, int D, long long Q, int n);
+int tfx_ttm_tc(const float* S, long long P, int D, long long Q, const float* Ut, int n, float* out, int* err,
+               void* stream);
 /* The same Gram on the 5th-generation tensor cores: TMA-fed SWIZZLE_128B tiles,
  * tcgen05.mma kind::tf32 into TMEM, FP32 accumulation, split-K partials summed
  * in compensated FP32.  FP32 input only; Q >= 32 and Q % 4 == 0; S 16-byte aligned.  *err

@@ -118,6 +118,7 @@ _EXTRA_SIGNATURES = {
     "tfx_gemm": [_I, _P, _P, _P, _LL, _LL, _LL, _LL, POINTER(c_longlong), _D, _D, _P],
     "tfx_orthonormalize": [_I, _P, _I, _I, _P],
     "tfx_ttm": [_I, _P, _LL, _I, _LL, _P, _I, _P, _P],
+    "tfx_ttm_tc": [_P, _LL, _I, _LL, _P, _I, _P, _P, _P],
     "tfx_sym_eig": [_I, _P, _I, _P, _P, _I, _P, _P],
     "tfx_flip_signs": [_I, _P, _I, _I, _P],
     "tfx_cp_residual": [_I, _P, _I, POINTER(c_int), _I, _P, _P, _P, _P],
@@ -147,6 +148,7 @@ _SIZE_FUNCS = {
     "tfx_coo_dgn_cg_workspace_bytes": [_I, _I, POINTER(c_int), _I],
     "tfx_coo_model_error_scratch_bytes": [_I, _I],
     "tfx_dogleg_scratch_bytes": [],
+    "tfx_ttm_tc_supported": [_LL, _I, _LL, _I],
     "tfx_step_update_wide_scratch_bytes": [_I, POINTER(c_int), _I],
     "tfx_mttkrp_tc_scratch_bytes": [_I, POINTER(c_int), _I, _I],
 }

@@ -121,7 +121,8 @@ def mlsvd_device(Td, R, options, speculate=True):
             Ut, sig, dim = _mode_svd(S, cur, l, n, tol_mlsvd, L, _ref_draw_cols(cur, l), tc)
             Uts.append(Ut)
             sigmas.append(sig)
-            S, cur = kernels.ttm(S, cur, l, Ut)
+            S, cur = kernels.ttm(S, cur, l, Ut, tensor_cores=tc)
+        kernels.check_ttm_flag()
     elif o.mlsvd_method == 'classic':
         for l in range(L):
             n = o.svd_n_components if o.svd_n_components is not None else min(R, shape[l])
@@ -130,7 +131,8 @@ def mlsvd_device(Td, R, options, speculate=True):
             sigmas.append(sig)
         S, cur = Td, list(shape)
         for l in range(L):
-            S, cur = kernels.ttm(S, cur, l, Uts[l])
+            S, cur = kernels.ttm(S, cur, l, Uts[l], tensor_cores=tc)
+        kernels.check_ttm_flag()
     else:
         raise NotImplementedError("mlsvd_method %r" % (o.mlsvd_method,))
     return _finish(S, Uts, sigmas, cur, o, L)
@@ -175,7 +177,7 @@ def mlsvd_launch(Td, R, o):
         Uts.append(Ut)
         lams.append(lam.double())
         ns.append(int(lam.shape[0]))
-        S, cur = kernels.ttm(S, cur, l, Ut)
+        S, cur = kernels.ttm(S, cur, l, Ut, tensor_cores=tc)
     return Pending(S.contiguous().view(*cur), Uts, cur, lams, errs, ns, state, tol_mlsvd)
 
 
@@ -188,6 +190,7 @@ def mlsvd_confirm(p):
     host = torch.cat(p.lams).cpu().numpy()
     for err in p.errs:
         kernels.check_gram_flag(err)
+    kernels.check_ttm_flag()
     L = len(p.ns)
     sigmas, off = [], 0
     for l in range(L):

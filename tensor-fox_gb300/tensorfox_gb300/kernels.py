@@ -100,20 +100,42 @@ def matmul(A, B, transA=False, transB=False):
     return gemm(A, B, C, M, N, K, 1, [0, sAm, sAk, 0, sBk, sBn, 0, N, 1])
 
 
-def ttm(S, shape, l, Ut):
+def ttm(S, shape, l, Ut, tensor_cores=False):
     """Mode-l product with U^T: out[p, j, q] = sum_i U[i, j] S[p, i, q].
 
-    ``Ut`` is (n, D) row-major, i.e. U (D x n) column-major."""
+    ``Ut`` is (n, D) row-major, i.e. U (D x n) column-major.  With
+    ``tensor_cores`` (precision 'mixed') an FP32 product whose shape the
+    tcgen05 kernel takes runs there (3xTF32, FP32 accumulation); its
+    bounded-wait flag is checked with the next read of the device
+    (``check_ttm_flag``)."""
     P = int(np.prod(shape[:l], dtype=np.int64))
     D = int(shape[l])
     Q = int(np.prod(shape[l + 1:], dtype=np.int64))
     n = int(Ut.shape[0])
     out = torch.empty(P * n * Q, dtype=S.dtype, device=S.device)
     Uc = Ut.contiguous()
-    _lib.call("tfx_ttm", _dt(S), _vp(S), P, D, Q, _vp(Uc), n, _vp(out), _st())
+    if (tensor_cores and S.dtype == torch.float32 and Uc.dtype == torch.float32 and S.data_ptr() % 16 == 0 and
+            Uc.data_ptr() % 16 == 0 and _lib.load().tfx_ttm_tc_supported(P, D, Q, n)):
+        err = torch.zeros(1, dtype=torch.int32, device=S.device)
+        _lib.call("tfx_ttm_tc", _vp(S), P, D, Q, _vp(Uc), n, _vp(out), _vp(err), _st())
+        _TTM_FLAGS.append(err)
+    else:
+        _lib.call("tfx_ttm", _dt(S), _vp(S), P, D, Q, _vp(Uc), n, _vp(out), _st())
     new_shape = list(shape)
     new_shape[l] = n
     return out.view(*new_shape), new_shape
+
+
+_TTM_FLAGS = []
+
+
+def check_ttm_flag():
+    """Raises if a tensor-core mode product issued since the last check ran out
+    of a bounded wait (one device read for all of them)."""
+    flags = list(_TTM_FLAGS)
+    _TTM_FLAGS.clear()
+    if flags and int(torch.cat(flags).max().item()) != 0:
+        raise _lib.TfxError("tensor-core mode product: a bounded wait ran out")
 
 
 def orthonormalize(Y):

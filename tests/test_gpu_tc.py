@@ -89,3 +89,30 @@ def test_tc_mttkrp_all_modes_vs_fp64(dims, R):
         assert np.abs(got - ref).max() <= 1e-5 * np.abs(ref).max()
         gc, _ = kernels.mttkrp_tc(Td, list(dims), flat, R, l, col_major=True)
         np.testing.assert_array_equal(gc.cpu().numpy().T, got.astype(np.float32))
+
+
+@pytest.mark.parametrize("shape,l,n", [((512, 64, 64), 0, 50), ((3, 64, 300), 1, 64), ((96, 40, 128), 0, 7),
+                                       ((5, 32, 129, 4), 1, 33), ((2, 512, 1000), 1, 50)])
+def test_tc_ttm_matches_fp64(shape, l, n):
+    """The tcgen05 mode product (3xTF32: operands split hi + lo, FP32
+    accumulation; precision 'mixed') against FP64: within 1e-5 of the
+    product's norm like the FP32 SIMT product, every tile tail (Q not a
+    multiple of 128, n below 64 and odd) included."""
+    rng = np.random.default_rng(3)
+    T = rng.standard_normal(shape).astype(np.float32)
+    D = shape[l]
+    U = rng.standard_normal((D, n)).astype(np.float32)
+    Td = torch.from_numpy(T).cuda()
+    Ut = torch.from_numpy(np.ascontiguousarray(U.T)).cuda()
+    P, Q = int(np.prod(shape[:l], dtype=np.int64)), int(np.prod(shape[l + 1:], dtype=np.int64))
+    from tensorfox_gb300 import _lib
+    assert _lib.load().tfx_ttm_tc_supported(P, D, Q, n)
+    got, new_shape = kernels.ttm(Td, list(shape), l, Ut, tensor_cores=True)
+    kernels.check_ttm_flag()
+    ref = np.moveaxis(np.tensordot(T.astype(np.float64), U.astype(np.float64), axes=([l], [0])), -1, l)
+    assert list(ref.shape) == list(new_shape)
+    got = got.double().cpu().numpy()
+    assert np.linalg.norm(got - ref) <= 1e-5 * np.linalg.norm(ref)
+    # the FP32 SIMT product of the same call, for comparison
+    simt, _ = kernels.ttm(Td, list(shape), l, Ut)
+    assert np.linalg.norm(simt.double().cpu().numpy() - ref) <= 1e-5 * np.linalg.norm(ref)
