@@ -18,8 +18,8 @@
 //   * warp 0 (producer) brings each chunk's 32 x 128 tensor tile and the
 //     chunk's 64 x 32 block of U^T (K-major SWIZZLE_128B) by TMA into a
 //     four-stage ring (a stage is refilled once the converters read it);
-//   * warps 2-5 (converters) each take 32 rows q of the tile and write them,
-//     split hi / lo, as rows of the A operands (128 x 32, K-major
+//   * warps 2-9 (converters) each take 32 rows q and half the d range of the
+//     tile and write them, split hi / lo, into the A operands (128 x 32, K-major
 //     SWIZZLE_128B: four d values as one 16-byte store, conflict-free), and
 //     split the U^T block in place of layout, into a two-stage ring;
 //   * warp 1 issues tcgen05.mma kind::tf32 (M = 128, N = 64, K = 8), three
@@ -41,7 +41,7 @@
 namespace tfx {
 namespace ttc {
 
-constexpr int BQ = 128, BD = 32, NJ = 64, NT = 192, TST = 4, AST = 2, DMAX = 8192;
+constexpr int BQ = 128, BD = 32, NJ = 64, NCW = 8, NT = 64 + 32 * NCW, TST = 4, AST = 2, DMAX = 8192;
 constexpr uint32_t SPIN = 1u << 26;
 constexpr uint32_t TTILE = BD * BQ * 4;      // one tensor tile, bytes
 constexpr uint32_t BCHUNK = NJ * BD * 4;     // one chunk of U^T, bytes
@@ -153,14 +153,14 @@ __global__ void __launch_bounds__(NT, 1)
   if (tid == 0) {
     for (int s = 0; s < TST; ++s) {
       mbar_init(&S.tfull[s], 1);
-      mbar_init(&S.tfree[s], 4);
+      mbar_init(&S.tfree[s], NCW);
     }
     for (int s = 0; s < AST; ++s) {
-      mbar_init(&S.afull[s], 4);
+      mbar_init(&S.afull[s], NCW);
       mbar_init(&S.afree[s], 1);
     }
     mbar_init(&S.accfull, 1);
-    mbar_init(&S.accfree, 4);
+    mbar_init(&S.accfree, NCW);
     S.abort = 0;
     S.tissued = 0;
     S.tconsumed = 0;
@@ -231,8 +231,10 @@ __global__ void __launch_bounds__(NT, 1)
       }
     }
   } else {
-    // converters (warps 2-5): transpose, then the epilogue of each finished tile
-    const int qr = (warp - 2) * 32 + lane;      // the row this thread transposes
+    // converters (warps 2-9): transpose, then the epilogue of each finished tile
+    const int cw = warp - 2;
+    const int qr = (cw & 3) * 32 + lane;        // the row this thread transposes
+    const int dh = cw >> 2;                     // its half of the chunk's d range
     const int erow = 32 * (warp & 3) + lane;    // the accumulator lane it reads
     for (int g = 0; g < nchunk; ++g) {
       const int s = g % TST, as = g % AST, c = g % DC, tl = g / DC;
@@ -254,7 +256,7 @@ __global__ void __launch_bounds__(NT, 1)
         const float* tt = reinterpret_cast<const float*>(S.t[s]);
         const uint32_t ro = (uint32_t)qr * 128;
 #pragma unroll
-        for (int d4 = 0; d4 < BD / 4; ++d4) {
+        for (int d4 = dh * (BD / 8); d4 < (dh + 1) * (BD / 8); ++d4) {
           float4 v, h, lo;
           v.x = tt[(4 * d4 + 0) * BQ + qr];
           v.y = tt[(4 * d4 + 1) * BQ + qr];
@@ -273,7 +275,7 @@ __global__ void __launch_bounds__(NT, 1)
         const float4* u4 = reinterpret_cast<const float4*>(S.u[s]);
         float4* bh4 = reinterpret_cast<float4*>(S.bhi[as]);
         float4* bl4 = reinterpret_cast<float4*>(S.blo[as]);
-        for (int e = qr; e < (int)(BCHUNK / 16); e += 128) {
+        for (int e = cw * 32 + lane; e < (int)(BCHUNK / 16); e += 32 * NCW) {
           const float4 v = u4[e];
           float4 h, lo;
           h.x = hi13(v.x); lo.x = v.x - h.x;
@@ -308,7 +310,7 @@ __global__ void __launch_bounds__(NT, 1)
         const long long q = q0 + erow;
         float* orow = out + (size_t)p * sh.n * sh.Q + q;
 #pragma unroll 1
-        for (int cc = 0; cc < NJ; cc += 32) {
+        for (int cc = dh * 32; cc < (dh + 1) * 32; cc += 32) {
           uint32_t v[32];
           const uint32_t taddr = tmem + ((uint32_t)(32 * (warp & 3)) << 16) + (uint32_t)cc;
           asm volatile(
