@@ -437,11 +437,12 @@ def kernel_rooflines(Td, R, opts, t_step):
                 "bound": "tensor", "achieved": fl_g / t_g / 1e12, "peak": bf16, "unit": "TFLOP/s",
                 "frac": fl_g / t_g / 1e12 / bf16, "traffic": traffic, "ms": t_g * 1e3, "share": t_g / t_step,
                 "peak_source": src + " bf16 dense (TF32 tensor rate is half of it)"})
-    # mode-1 truncation product
+    # mode-1 truncation product (the tcgen05 3xTF32 kernel of the mixed path)
     Ut0 = Uts[0]
-    t_t = _time_events(lambda: kernels.ttm(Td, list(DIMS), 0, Ut0), 20)
+    t_t = _time_events(lambda: kernels.ttm(Td, list(DIMS), 0, Ut0, tensor_cores=True), 20)
+    kernels.check_ttm_flag()
     by_t = N * 4 + Ut0.shape[0] * DIMS[1] * DIMS[2] * 4
-    out.append({"kernel": "tfx_ttm mode-1 truncation product (50 x 512 x 262144)", "bound": "hbm",
+    out.append({"kernel": "k_ttm_tc mode-1 truncation product (tcgen05 3xTF32, 50 x 512 x 262144)", "bound": "hbm",
                 "achieved": by_t / t_t / 1e9, "peak": hbm, "unit": "GB/s", "frac": by_t / t_t / 1e9 / hbm,
                 "traffic": None, "ms": t_t * 1e3, "share": t_t / t_step})
     # residual on the tensor cores (the final error)
