@@ -431,6 +431,91 @@ __device__ __forceinline__ void panel_cgs2_warp(T* Pb, int D, int cb) {
   }
 }
 
+// The same panel CGS2 on the first NWP warps: lane l of warp w holds rows
+// (w RPW + t) 32 + l, t < RPW (D <= 32 NWP RPW), so every dot product is a
+// warp sum plus a fixed-order sum of the NWP warp partials through shared
+// memory (part: 2 x NWP x ORTH_B values, used alternately), one named barrier
+// of the NWP warps per reduction.  Four warps take a quarter of the one-warp
+// form's multiply-adds per column.
+template <class T, int RPW, int NWP>
+__device__ __forceinline__ void panel_cgs2_warps(T* Pb, int D, int cb, T* part) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  T v[RPW][ORTH_B];
+#pragma unroll
+  for (int t = 0; t < RPW; ++t) {
+    const int r = (w * RPW + t) * 32 + lane;
+    if (r < D) {
+      load_row8<T>(Pb + (size_t)r * ORTH_B, v[t]);
+    } else {
+#pragma unroll
+      for (int c = 0; c < ORTH_B; ++c) v[t][c] = T(0);
+    }
+  }
+  int buf = 0;
+  // d[0..n) summed over the NWP warps, identical in every lane of every warp
+  auto allsum = [&](T (&d)[ORTH_B], int n) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+      for (int c2 = 0; c2 < ORTH_B; ++c2)
+        if (c2 < n) d[c2] += __shfl_xor_sync(0xffffffffu, d[c2], o);
+    T* pb = part + buf * NWP * ORTH_B;
+    if (lane == 0)
+#pragma unroll
+      for (int c2 = 0; c2 < ORTH_B; ++c2)
+        if (c2 < n) pb[w * ORTH_B + c2] = d[c2];
+    asm volatile("bar.sync 1, %0;" ::"r"(NWP * 32) : "memory");
+#pragma unroll
+    for (int c2 = 0; c2 < ORTH_B; ++c2)
+      if (c2 < n) {
+        T x = pb[c2];
+#pragma unroll
+        for (int q = 1; q < NWP; ++q) x += pb[q * ORTH_B + c2];
+        d[c2] = x;
+      }
+    buf ^= 1;
+  };
+#pragma unroll
+  for (int c = 0; c < ORTH_B; ++c) {
+    if (c < cb) {
+#pragma unroll
+      for (int pass = 0; pass < 2; ++pass) {
+        if (c > 0) {
+          T d[ORTH_B];
+#pragma unroll
+          for (int c2 = 0; c2 < ORTH_B; ++c2) {
+            d[c2] = T(0);
+            if (c2 < c)
+#pragma unroll
+              for (int t = 0; t < RPW; ++t) d[c2] = fma(v[t][c2], v[t][c], d[c2]);
+          }
+          allsum(d, c);
+#pragma unroll
+          for (int t = 0; t < RPW; ++t)
+#pragma unroll
+            for (int c2 = 0; c2 < ORTH_B; ++c2)
+              if (c2 < c) v[t][c] = fma(-d[c2], v[t][c2], v[t][c]);
+        }
+      }
+      T nq[ORTH_B];
+      nq[0] = T(0);
+#pragma unroll
+      for (int t = 0; t < RPW; ++t) nq[0] = fma(v[t][c], v[t][c], nq[0]);
+      allsum(nq, 1);
+      const T inv = nq[0] > T(0) ? T(1) / sqrt(nq[0]) : T(0);
+#pragma unroll
+      for (int t = 0; t < RPW; ++t) v[t][c] *= inv;
+    }
+  }
+#pragma unroll
+  for (int t = 0; t < RPW; ++t) {
+    const int r = (w * RPW + t) * 32 + lane;
+    if (r < D)
+#pragma unroll
+      for (int c = 0; c < ORTH_B; ++c) Pb[(size_t)r * ORTH_B + c] = v[t][c];
+  }
+}
+
 template <class T, int RPL>
 __global__ void __launch_bounds__(ORTH_NT) k_orth_bcgs(T* Y, int D, int k) {
   extern __shared__ __align__(16) char smem_b[];
@@ -505,10 +590,12 @@ __global__ void __launch_bounds__(ORTH_NT) k_orth_bcgs(T* Y, int D, int k) {
         __syncthreads();
       }
     }
-    // column CGS2 inside the panel by warp 0 alone: its sums are warp
-    // shuffles, so the 2 * ORTH_B - 1 dependent reductions of a panel cost no
-    // block barrier.  RPL > 0: the panel sits in registers (D <= 32 * RPL).
-    if (RPL > 0) {
+    // column CGS2 inside the panel by the first four warps (RPL >= 4, the
+    // panel in registers, D <= 32 * RPL; reductions at a named barrier of
+    // those warps) or by warp 0 alone (its sums are warp shuffles)
+    if (RPL >= 4) {
+      if (wid < 4) panel_cgs2_warps<T, (RPL >= 4 ? RPL / 4 : 1), 4>(Pb, D, cb, part);
+    } else if (RPL > 0) {
       if (wid == 0) panel_cgs2_warp<T, (RPL > 0 ? RPL : 1)>(Pb, D, cb);
     } else if (wid == 0) {
       for (int c = 0; c < cb; ++c) {
