@@ -131,6 +131,18 @@ __device__ int cta_jacobi(T* A, T* Vs, T* cs, int* pr, double* red, int m, int m
       }
     }
   };
+  // true when some pair still exceeds the rotation threshold (the test of
+  // params): a sweep after which none does would rotate nothing, so the loop
+  // stops without running it (same result, one sweep fewer)
+  auto pending = [&]() -> bool {
+    bool mine = false;
+    for (int p = wid; p < m; p += nw)
+      for (int q = p + 1 + lane; q < m; q += 32) {
+        const T apq = A[p * m + q], app = A[p * m + p], aqq = A[q * m + q];
+        if (apq != T(0) && fabs(apq) * fabs(apq) > tol * tol * fabs(app * aqq)) mine = true;
+      }
+    return __syncthreads_or(mine) != 0;
+  };
   __syncthreads();
   int sweep = 0;
   if (cs2 && pr2 && nw >= 2) {
@@ -157,6 +169,10 @@ __device__ int cta_jacobi(T* A, T* Vs, T* cs, int* pr, double* red, int m, int m
         }
         __syncthreads();
       }
+      if (!pending()) {
+        ++sweep;
+        break;
+      }
       const int rotated = flag[sweep % 3];
       if (!rotated) break;
     }
@@ -169,6 +185,10 @@ __device__ int cta_jacobi(T* A, T* Vs, T* cs, int* pr, double* red, int m, int m
         blocks(cs, pr);
         vupd(cs, pr, 0, nw);
         __syncthreads();
+      }
+      if (!pending()) {
+        ++sweep;
+        break;
       }
       const int rotated = flag[sweep % 3];
       if (!rotated) break;
