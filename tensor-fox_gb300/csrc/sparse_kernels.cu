@@ -186,7 +186,36 @@ __global__ void __launch_bounds__(256, 4) k_coo_mttkrp_f4(const int* __restrict_
         const float v = kk < e ? svals[kk] : 0.f;
         pv[u][0] = pv[u][1] = pv[u][2] = pv[u][3] = v;
       }
-      if (on) {
+      if (on && sh.L == 3) {
+        // third order: both other modes' coordinates, then both modes' rows,
+        // in flight together (two round trips a pass instead of four); the
+        // products keep the mode order of the general loop
+        const int ma = mode == 0 ? 1 : 0, mb = mode == 2 ? 1 : 2;
+        const int* ia = sidx + (size_t)ma * nnz;
+        const int* ib = sidx + (size_t)mb * nnz;
+        int xa[UNR], xb[UNR];
+#pragma unroll
+        for (int u = 0; u < UNR; ++u) {
+          const bool in = k + 8 * u < e;
+          xa[u] = in ? ia[k + 8 * u] : 0;
+          xb[u] = in ? ib[k + 8 * u] : 0;
+        }
+        const float* wa = Wrow[ma] + rq;
+        const float* wb = Wrow[mb] + rq;
+        float4 ya[UNR], yb[UNR];
+#pragma unroll
+        for (int u = 0; u < UNR; ++u) {
+          ya[u] = ld4(wa + (size_t)xa[u] * R, al);
+          yb[u] = ld4(wb + (size_t)xb[u] * R, al);
+        }
+#pragma unroll
+        for (int u = 0; u < UNR; ++u) {
+          pv[u][0] = pv[u][0] * ya[u].x * yb[u].x;
+          pv[u][1] = pv[u][1] * ya[u].y * yb[u].y;
+          pv[u][2] = pv[u][2] * ya[u].z * yb[u].z;
+          pv[u][3] = pv[u][3] * ya[u].w * yb[u].w;
+        }
+      } else if (on) {
         for (int m = 0; m < sh.L; ++m) {
           if (m == mode) continue;
           const int* im = sidx + (size_t)m * nnz;
