@@ -163,20 +163,6 @@ __global__ void __launch_bounds__(NT, 1) k_residual_tc(const float* __restrict__
     }
     for (int ib = 0; ib < nib; ++ib) {
       const int i0 = ib * BM;
-      // the thread's 128 tensor values of this tile (row 32 (warp % 4) + lane,
-      // columns (warp / 4) 128 ..), loaded before the operands are formed and
-      // the products issued, so that the whole tile is in flight meanwhile
-      const int erow = 32 * (warp & 3) + lane;
-      const int ei = i0 + erow;
-      const int ech = (warp >> 2) * (BN / 2);
-      const long long eqb = q0 + ech;
-      const bool efull = ei < d0 && eqb + BN / 2 <= Q0;
-      float4 tv[BN / 8];
-      if (efull) {
-        const float4* t4 = reinterpret_cast<const float4*>(T + (size_t)ei * Q0 + eqb);
-#pragma unroll
-        for (int u = 0; u < BN / 8; ++u) tv[u] = __ldcs(t4 + u);
-      }
       // W0's rows of the block, eight entries a pass with their loads issued
       // together (the shared-memory stores go through a generic pointer, so
       // the compiler would not move later loads above them)
@@ -202,6 +188,21 @@ __global__ void __launch_bounds__(NT, 1) k_residual_tc(const float* __restrict__
             *(float*)(S.alo[k >> 5] + o) = f[u] - h;
           }
         }
+      }
+      // the thread's 128 tensor values of this tile (row 32 (warp % 4) + lane,
+      // columns (warp / 4) 128 ..), loaded after W0's rows (issued first, the
+      // 32 16-byte loads a thread would hold the operand loads back) and
+      // before the products, so the tile is in flight while they run
+      const int erow = 32 * (warp & 3) + lane;
+      const int ei = i0 + erow;
+      const int ech = (warp >> 2) * (BN / 2);
+      const long long eqb = q0 + ech;
+      const bool efull = ei < d0 && eqb + BN / 2 <= Q0;
+      float4 tv[BN / 8];
+      if (efull) {
+        const float4* t4 = reinterpret_cast<const float4*>(T + (size_t)ei * Q0 + eqb);
+#pragma unroll
+        for (int u = 0; u < BN / 8; ++u) tv[u] = __ldcs(t4 + u);
       }
       // generic-proxy writes -> visible to the tensor core's async proxy
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
