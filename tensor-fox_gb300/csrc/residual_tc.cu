@@ -125,14 +125,15 @@ __global__ void __launch_bounds__(NT, 1) k_residual_tc(const float* __restrict__
   uint32_t phase = 0;
   for (int cb = blockIdx.x; cb < ncb; cb += gridDim.x) {
     const long long q0 = (long long)cb * BN;
-    // Khatri-Rao rows of the column block: hi and lo parts.  Eight entries
+    // Khatri-Rao rows of the column block: hi and lo parts.  Sixteen entries
     // a pass, their factor loads issued together (the loads come from L2);
     // a warp covers 8 columns x 4 ranks, so that its loads of W2 are four
     // 32-byte runs and its swizzled stores hit 32 distinct banks.
-    for (int e0 = tid; e0 < BN * KP; e0 += NT * BU) {
-      float f1[BU], f2[BU];
+    constexpr int BB = 2 * BU;  // sixteen entries a pass (the column block's operand is the larger one)
+    for (int e0 = tid; e0 < BN * KP; e0 += NT * BB) {
+      float f1[BB], f2[BB];
 #pragma unroll
-      for (int u = 0; u < BU; ++u) {
+      for (int u = 0; u < BB; ++u) {
         const int e = e0 + u * NT;
         int n, k;
         tile_nk(e, n, k);
@@ -148,7 +149,7 @@ __global__ void __launch_bounds__(NT, 1) k_residual_tc(const float* __restrict__
         }
       }
 #pragma unroll
-      for (int u = 0; u < BU; ++u) {
+      for (int u = 0; u < BB; ++u) {
         const int e = e0 + u * NT;
         if (e < BN * KP) {
           int n, k;
