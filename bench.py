@@ -879,6 +879,18 @@ def run_case(case):
                 out, err = kernels.mttkrp_tc(T, dims, Wf, RANK, l)
         torch.cuda.synchronize()
         print(json.dumps({"case": case, "err": int(err.item()), "m00": float(out[0, 0])}))
+    elif case == "ttm_tc":
+        # the mixed path's mode-1 truncation product of the headline tensor
+        # (tcgen05 3xTF32), five launches
+        T, _ = make_problem()
+        Td = torch.from_numpy(T).cuda()
+        g = torch.Generator(device="cuda").manual_seed(0)
+        Ut = torch.randn(RANK, DIMS[0], device="cuda", generator=g)
+        for _ in range(5):
+            S1, _ = kernels.ttm(Td, list(DIMS), 0, Ut, tensor_cores=True)
+        kernels.check_ttm_flag()
+        torch.cuda.synchronize()
+        print(json.dumps({"case": case, "s00": float(S1.reshape(-1)[0])}))
     elif case == "residual_tc":
         # the full-tensor residual of the headline tensor (tcgen05 path), five launches
         T, W = make_problem()
@@ -930,7 +942,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-sparse", action="store_true")
-    ap.add_argument("--case", default=None, help="tc_gram_small | mttkrp_tc_small | engine_core | residual_tc | c3_autograd | sparse_c5 | sparse_cpd | "
+    ap.add_argument("--case", default=None, help="tc_gram_small | mttkrp_tc_small | ttm_tc | engine_core | residual_tc | c3_autograd | sparse_c5 | sparse_cpd | "
                     "sparse_cpd_mid | sparse_direct_c5 | direct (profiling workloads)")
     args = ap.parse_args()
     if args.case:
