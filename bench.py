@@ -253,7 +253,13 @@ def run_ours(args):
     barrier()
     launches = _lib.launch_count() - l0
     t_dev = ev0.elapsed_time(ev1) / 1e3 / args.steps
-    # end to end: pinned host tensor in (H2D inside the call), NumPy factors out
+    # end to end: pinned host tensor in (H2D inside the call), NumPy factors out.
+    # One untimed call first: after the device-input loop the allocator's
+    # cached blocks are split, and the first host-input call pays a fresh
+    # 537 MB device allocation (~20 ms, once)
+    np.random.seed(0)
+    tfx.cpd(Th, R, opts)
+    barrier()
     t0 = time.perf_counter()
     for _ in range(args.steps):
         np.random.seed(0)
