@@ -36,7 +36,9 @@ def _cint(vals):
 class DeviceCOO:
     """COO tensor resident on the device: int32 SoA coordinates and values."""
 
-    def __init__(self, data, idxs, dims, dtype):
+    def __init__(self, data, idxs, dims, dtype, perm=None):
+        """``perm``: the modes of ``dims`` are the input coordinates' columns
+        ``perm[0], perm[1], ...`` (applied on the device, after the copy)."""
         dims = [int(d) for d in dims]
         self.dims = dims
         self.L = len(dims)
@@ -45,8 +47,16 @@ class DeviceCOO:
         dev = _dev.device()
         idx = torch.as_tensor(np.ascontiguousarray(np.asarray(idxs, dtype=np.int64).reshape(-1, self.L)),
                               device=dev)
+        if perm is not None and [int(v) for v in perm] != list(range(self.L)):
+            idx = idx[:, torch.as_tensor(np.asarray(perm, dtype=np.int64), device=dev)].contiguous()
         self.nnz = int(idx.shape[0])
-        self.vals = torch.as_tensor(np.asarray(data, dtype=np.float64), device=dev).to(dtype).contiguous()
+        # the values go over in their own type when it is the working one
+        # (float32 -> float64 -> float32 is exact, so the result is the same)
+        dv = np.asarray(data)
+        if not ((dv.dtype == np.float32 and dtype == torch.float32) or
+                (dv.dtype == np.float64 and dtype == torch.float64)):
+            dv = np.asarray(dv, dtype=np.float64)
+        self.vals = torch.as_tensor(np.ascontiguousarray(dv), device=dev).to(dtype).contiguous()
         self.idx32 = torch.empty((self.L, max(self.nnz, 1)), dtype=torch.int32, device=dev)
         err = torch.zeros(1, dtype=torch.int32, device=dev)
         _lib.call("tfx_coo_encode", _vp(idx), self.nnz, self.L, _cint(dims), _vp(self.idx32), _vp(err), _st())
@@ -226,7 +236,8 @@ def tricpd_sparse(T, R, options):
     if o.method not in ('dGN', 'als'):
         raise NotImplementedError("method %r is outside the damped Gauss-Newton and ALS paths" % (o.method,))
     data, idxs, dims = T
-    in_f32 = np.asarray(data).dtype == np.float32
+    data_in = np.asarray(data)
+    in_f32 = data_in.dtype == np.float32
     data = np.asarray(data, dtype=np.float64)
     idxs = np.asarray(idxs, dtype=np.int64).reshape(len(data), -1)
     dims = np.asarray(dims)
@@ -240,7 +251,7 @@ def tricpd_sparse(T, R, options):
     dt = _dev.torch_dtype(prec)
     ordering = np.argsort(-dims)
     sdims = dims[ordering]
-    X = DeviceCOO(data, idxs[:, ordering], sdims, dt)
+    X = DeviceCOO(data_in, idxs, sdims, dt, perm=ordering)
     Tsize = float(np.linalg.norm(data))
     if getattr(o, 'sparse_solver', None) == 'direct':
         if o.method != 'dGN':

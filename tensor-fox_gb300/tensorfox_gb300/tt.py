@@ -264,7 +264,7 @@ def cpd_tt(T, R, options):
         dt = _dev.torch_dtype(prec)
         ordering = np.argsort(-dims0)
         dims = [int(d) for d in dims0[ordering]]
-        X = DeviceCOO(data, idxs[:, ordering], dims, dt)
+        X = DeviceCOO(data, idxs, dims, dt, perm=ordering)
         Tsize = float(np.linalg.norm(data))
         tol = o.tol_mlsvd[0] if isinstance(o.tol_mlsvd, list) else o.tol_mlsvd
         if tol < 0:            # TensorFox.py:275-280
