@@ -231,15 +231,29 @@ def test_sym_eig_f32_graded(n):
 
 @pytest.mark.parametrize("M,K,N,tA,tB", [(60, 512, 512, False, False), (50, 60, 20480, False, False),
                                          (70, 64, 256, False, False), (60, 512, 60, False, True),
-                                         (33, 20, 130, False, False), (16, 48, 96, True, False)])
+                                         (33, 20, 130, False, False), (16, 48, 96, True, False),
+                                         (64, 300, 77, False, True), (1, 1000, 33, False, False)])
 def test_matmul_f32(M, K, N, tA, tB):
-    """FP32 device products: the wide ones on the register-tiled kernel, the rest on the tiled GEMM."""
+    """FP32 device products: the wide ones on the register-tiled kernel, short
+    left factors (M <= 64, K >= 32) on the K-quartered kernel (partial K
+    chunks and column blocks included), the rest on the tiled GEMM."""
     rng = np.random.default_rng(8)
     A = rng.standard_normal((K, M) if tA else (M, K)).astype(np.float32)
     B = rng.standard_normal((N, K) if tB else (K, N)).astype(np.float32)
     got = kernels.matmul(dev(A, torch.float32), dev(B, torch.float32), transA=tA, transB=tB).double().cpu().numpy()
     ref = (A.T if tA else A).astype(np.float64) @ (B.T if tB else B).astype(np.float64)
     np.testing.assert_allclose(got, ref, rtol=0, atol=2e-6 * np.sqrt(K) * np.abs(ref).max())
+
+
+@pytest.mark.parametrize("M,K,N,tB", [(60, 512, 512, False), (60, 512, 60, True), (7, 129, 40, False)])
+def test_matmul_f64_short_left_factor(M, K, N, tB):
+    """The K-quartered kernel in FP64: rounding-level agreement with NumPy."""
+    rng = np.random.default_rng(9)
+    A = rng.standard_normal((M, K))
+    B = rng.standard_normal((N, K) if tB else (K, N))
+    got = kernels.matmul(dev(A), dev(B), transB=tB).cpu().numpy()
+    ref = A @ (B.T if tB else B)
+    np.testing.assert_allclose(got, ref, rtol=0, atol=1e-13 * np.sqrt(K) * np.abs(ref).max())
 
 
 @pytest.mark.parametrize("dims,R", [((257, 131, 128), 50), ((129, 129, 256), 64), ((300, 140, 100), 1)])
