@@ -1024,23 +1024,46 @@ __global__ void __launch_bounds__(256) k_gemm_skinny(const T* __restrict__ A, co
   for (int j = 0; j < SK_NB; ++j) acc[j] = T(0);
   for (long long k0 = 0; k0 < g.K; k0 += SK_KC) {
     const int kc = (int)(g.K - k0 < SK_KC ? g.K - k0 : SK_KC);
+    // the chunk's operands: every load of a thread issued before any store
+    // (one L2 round trip a chunk instead of one per element)
+    constexpr int NA = 64 * SK_KC / 256, NB = SK_KC * SK_NB / 256;
+    T ra[NA], rb[NB];
+#pragma unroll
+    for (int u = 0; u < NA; ++u) {
+      const int e = tid + 256 * u, m = e / SK_KC, k = e - m * SK_KC;
+      ra[u] = (m < M && k < kc) ? A[m * g.sAm + (k0 + k) * g.sAk] : T(0);
+    }
+#pragma unroll
+    for (int u = 0; u < NB; ++u) {
+      const int e = tid + 256 * u, k = e / SK_NB, j = e - k * SK_NB;
+      rb[u] = (k < kc && n0 + j < g.N) ? B[(k0 + k) * g.sBk + (n0 + j) * g.sBn] : T(0);
+    }
     __syncthreads();  // the previous chunk is consumed
-    for (int e = tid; e < 64 * SK_KC; e += 256) {
-      const int m = e / SK_KC, k = e - m * SK_KC;
-      As[m * (SK_KC + 1) + k] = (m < M && k < kc) ? A[m * g.sAm + (k0 + k) * g.sAk] : T(0);
+#pragma unroll
+    for (int u = 0; u < NA; ++u) {
+      const int e = tid + 256 * u, m = e / SK_KC, k = e - m * SK_KC;
+      As[m * (SK_KC + 1) + k] = ra[u];
     }
-    for (int e = tid; e < SK_KC * SK_NB; e += 256) {
-      const int k = e / SK_NB, j = e - k * SK_NB;
-      Bs[e] = (k < kc && n0 + j < g.N) ? B[(k0 + k) * g.sBk + (n0 + j) * g.sBn] : T(0);
-    }
+#pragma unroll
+    for (int u = 0; u < NB; ++u) Bs[tid + 256 * u] = rb[u];
     __syncthreads();
     const T* ar = As + row * (SK_KC + 1) + kq * (SK_KC / 4);
     const T* br = Bs + kq * (SK_KC / 4) * SK_NB;
+    // B's row as 16-byte reads (broadcast across the warp): 4 (FP32) or 8
+    // (FP64) loads per k instead of 16
+    using V = typename std::conditional<sizeof(T) == 4, float4, double2>::type;
+    constexpr int PV = 16 / sizeof(T);
 #pragma unroll 4
     for (int kk = 0; kk < SK_KC / 4; ++kk) {
       const T a = ar[kk];
+      const V* bv = reinterpret_cast<const V*>(br + kk * SK_NB);
 #pragma unroll
-      for (int j = 0; j < SK_NB; ++j) acc[j] = fma(a, br[kk * SK_NB + j], acc[j]);
+      for (int j4 = 0; j4 < SK_NB / PV; ++j4) {
+        const V b = bv[j4];
+        const T* bb = reinterpret_cast<const T*>(&b);
+#pragma unroll
+        for (int u = 0; u < PV; ++u) acc[j4 * PV + u] = fma(a, bb[u], acc[j4 * PV + u]);
+      }
     }
   }
 #pragma unroll
