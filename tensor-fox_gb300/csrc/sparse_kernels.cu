@@ -383,7 +383,49 @@ __global__ void __launch_bounds__(256) k_sparse_residual_f4(const int* __restric
   const int R = sh.R, L = sh.L;
   bool al = true;
   for (int l = 0; l < L; ++l) al = al && ((unsigned long long)Wrow[l] & 15ull) == 0;
-  for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < nnz; k += (long long)gridDim.x * blockDim.x) {
+  const long long S = (long long)gridDim.x * blockDim.x;
+  if (L == 3) {
+    // third order: two entries a pass, their coordinates and then all six
+    // factor rows in flight together (the general loop indexes its row
+    // pointers at run time and waits on each mode in turn); products, sums
+    // and the order of the squared differences are those of the general loop
+    const float* W0 = Wrow[0];
+    const float* W1 = Wrow[1];
+    const float* W2 = Wrow[2];
+    for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < nnz; k += 2 * S) {
+      const long long k2 = k + S;
+      const bool two = k2 < nnz;
+      const int a0 = idx32[k], b0 = idx32[nnz + k], c0 = idx32[2 * nnz + k];
+      const int a1 = two ? idx32[k2] : 0, b1 = two ? idx32[nnz + k2] : 0, c1 = two ? idx32[2 * nnz + k2] : 0;
+      const float v0 = vals[k], v1 = two ? vals[k2] : 0.f;
+      const float* x0 = W0 + (size_t)a0 * R;
+      const float* y0 = W1 + (size_t)b0 * R;
+      const float* z0 = W2 + (size_t)c0 * R;
+      const float* x1 = W0 + (size_t)a1 * R;
+      const float* y1 = W1 + (size_t)b1 * R;
+      const float* z1 = W2 + (size_t)c1 * R;
+      float m0 = 0.f, m1 = 0.f;
+#pragma unroll 4
+      for (int r = 0; r < R; r += 4) {
+        float4 p = ld4(x0 + r, al), q = ld4(x1 + r, al);
+        const float4 u0 = ld4(y0 + r, al), u1 = ld4(y1 + r, al);
+        const float4 t0 = ld4(z0 + r, al), t1 = ld4(z1 + r, al);
+        p.x *= u0.x; p.y *= u0.y; p.z *= u0.z; p.w *= u0.w;
+        p.x *= t0.x; p.y *= t0.y; p.z *= t0.z; p.w *= t0.w;
+        q.x *= u1.x; q.y *= u1.y; q.z *= u1.z; q.w *= u1.w;
+        q.x *= t1.x; q.y *= t1.y; q.z *= t1.z; q.w *= t1.w;
+        m0 += (p.x + p.y) + (p.z + p.w);
+        m1 += (q.x + q.y) + (q.z + q.w);
+      }
+      const float d0 = v0 - m0;
+      acc.fma_(d0, d0);
+      if (two) {
+        const float d1 = v1 - m1;
+        acc.fma_(d1, d1);
+      }
+    }
+  } else
+  for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < nnz; k += S) {
     const float* w[TFX_MAX_ORDER];
     for (int l = 0; l < L; ++l) w[l] = Wrow[l] + (size_t)idx32[(size_t)l * nnz + k] * R;
     float model = 0.f;
