@@ -156,8 +156,8 @@ int tfx_gemm(int dtype, const void* A, const void* B, void* C, long long M, long
 int tfx_ttm(int dtype, const void* S, long long P, int D, long long Q, const void* Ut, int n, void* out,
             void* stream);
 /* The same product on the tensor cores for precision 'mixed' (3xTF32: both
- * operands split hi + lo, FP32 accumulation; Compression.py:123-137's
- * truncation): FP32 S (P, D, Q) and Ut (n x D), both 16-byte aligned, out
+ * operands split hi + lo, FP32 accumulation; the truncation of
+ * Compression.py:152-156 / 170-173): FP32 S (P, D, Q) and Ut (n x D), both 16-byte aligned, out
  * (P, n, Q); D % 32 == 0, n <= 64, Q >= 128, Q % 4 == 0 (tfx_ttm_tc_supported), else
  * TFX_STATUS_ERR_UNSUPPORTED.  err: device int, non-zero when a bounded wait
  * ran out. */

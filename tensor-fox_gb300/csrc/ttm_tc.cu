@@ -3,8 +3,9 @@
 //
 //   out[p, j, q] = sum_d U[d, j] T[p, d, q]
 //
-// the MLSVD's truncation step (Compression.py:123-137 via
-// MultilinearAlgebra.py:75-107 multilin_mult: the core S = T x_l U_l^T).  The
+// the MLSVD's truncation step (Compression.py:152-156, where the sequential
+// method forms U_l^T S_(l) as Sigma V^T, and :170-173 with
+// MultilinearAlgebra.py:72-105 multilin_mult for the classic one).  The
 // contraction index d is the strided one in memory (T[p, d, q] has q
 // contiguous), so the tensor is the A operand with M = q and K = d after a
 // transposition in shared memory; U^T (n x D, n <= 64) is the B operand.
